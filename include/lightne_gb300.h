@@ -1,0 +1,132 @@
+/*
+ * lightne_gb300 — C ABI of the GB300-native LightNE embedding pipeline.
+ *
+ * One library (liblightne_gb300.so) exports the stages of LightNE's hot path
+ * as plain C entry points: pointers and sizes, no C++ or torch types.  Every
+ * function returns an int status (LNE_OK == 0) and never exits the process;
+ * lne_last_error() gives the message of the calling thread's last failure.
+ * Work is ordered on the context's CUDA stream; a context is used by one
+ * host thread at a time.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   lne_sparsify        path_embed::generate_trunc_log_matrix_v2
+ *                       (LightNE/PathEmbed.h:81-369), the NetSMF sparsifier:
+ *                       path sampler, par_table aggregation, trunc-log and
+ *                       CSR build
+ *   lne_randsvd         mkl_redsvd::MKLRedSVD<FP> ctor + run()
+ *                       (LightNE/mklredsvd/mklredsvd.cc:54-403) followed by
+ *                       path_embed::compute_u_sigma_root
+ *                       (LightNE/PathEmbed.h:371-408)
+ *   lne_propagate       spectral_propagation::chebyshev_expansion up to the
+ *                       (A+I)a product (LightNE/SpectralPropagation.h:45-221)
+ *   lne_dense_embed     spectral_propagation::get_embedding_dense
+ *                       (LightNE/SpectralPropagation.h:16-43)
+ *   lne_spmm            mkl_sparse_s_mm on a CSR (the SpMM of
+ *                       LightNE/mklredsvd/mklredsvd.cc:235-245)
+ */
+#ifndef LIGHTNE_GB300_H
+#define LIGHTNE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define LNE_OK 0
+#define LNE_ERR_INVALID 1      /* bad argument */
+#define LNE_ERR_ALLOC 2        /* device or host allocation failed */
+#define LNE_ERR_TABLE_FULL 3   /* pair table overflow: the reference prints
+                                  "looping forever" and exits 0
+                                  (LightNE/par_table.h:104-107) */
+#define LNE_ERR_CUDA 4         /* CUDA runtime error */
+#define LNE_ERR_UNSUPPORTED 5  /* size beyond what this build handles */
+#define LNE_ERR_NUMERIC 6      /* factorisation failed (e.g. non-SPD Gram) */
+
+/* Dense operand precision of SpMM / propagation. */
+#define LNE_PREC_FP32 0
+#define LNE_PREC_BF16 1
+
+typedef struct lne_ctx lne_ctx;
+typedef struct lne_graph lne_graph;
+typedef struct lne_csr lne_csr;
+
+/* Last error message of the calling thread ("" if none). */
+const char* lne_last_error(void);
+/* Library version string. */
+const char* lne_version(void);
+
+/* Context: device, stream (a cudaStream_t, or NULL for a private stream). */
+int lne_ctx_create(lne_ctx** out, int device, void* stream);
+int lne_ctx_destroy(lne_ctx* ctx);
+/* Wait for all work queued on the context's stream. */
+int lne_ctx_synchronize(lne_ctx* ctx);
+
+/*
+ * Graph: symmetric CSR, offsets int64[n+1] (offsets[n] = number of directed
+ * entries), neighbours int32[offsets[n]], in the order of the AdjacencyGraph
+ * file (the walk depends on it).  Host pointers; the graph is copied to the
+ * device.  Replaces gbbs_io::read_unweighted_symmetric_graph's in-memory
+ * result (ligra/graph_io.h:233-250).
+ */
+int lne_graph_upload(lne_ctx* ctx, int64_t n, const int64_t* offsets, const int32_t* nbrs,
+                     lne_graph** out);
+/* Same, from device pointers (already resident in HBM). */
+int lne_graph_upload_device(lne_ctx* ctx, int64_t n, const int64_t* d_offsets,
+                            const int32_t* d_nbrs, lne_graph** out);
+int lne_graph_free(lne_graph* g);
+
+/* Parameters of the sparsifier; names and meaning as the LightNE flags
+ * (LightNE/LightNE.cc:31-43).  sample_ratio and mem_ratio are floats, as
+ * LightNE.cc:42-43 narrows them. */
+typedef struct lne_sparsify_params {
+  uint64_t seed;        /* pbbs::random seed (reference: time(0)) */
+  int64_t walk_len;     /* -walklen (T) */
+  int64_t table_size;   /* -tablesz */
+  int64_t negative;     /* -negative (b) */
+  int32_t sample;       /* -sample: 0 = every path, 1 = effective-resistance sampling */
+  int32_t upper;        /* -upper: keep the upper triangle only */
+  float sample_ratio;   /* -sample_ratio */
+  float mem_ratio;      /* -mem_ratio */
+} lne_sparsify_params;
+
+/* Diagnostics of one sparsifier call (the reference prints these). */
+typedef struct lne_sparsify_stats {
+  double logn, total_samples, inv_lambda, frac, factor, m_exact;
+  int64_t exp_rv_rounded, table_size, capacity, samples_emitted, distinct, nnz_upper, nnz;
+  float ms_sample, ms_trunclog, ms_csr; /* device time per stage (CUDA events) */
+  int32_t kernel_launches;              /* kernels this call launched */
+} lne_sparsify_stats;
+
+/*
+ * NetSMF sparsifier: S1-S9 of the hot path.  Output CSR (device-resident,
+ * owned by the caller, free with lne_csr_free) is canonical: rows ascending,
+ * columns ascending within a row, int64 row_ptr, int32 col, float32 val.
+ * Bit-exact with the reference's matrix (as a set of entries) for the same
+ * seed when sample == 0.  stats may be NULL.
+ */
+int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_params* p, lne_csr** out,
+                 lne_sparsify_stats* stats);
+
+/*
+ * Diagnostic: the double the trunc-log map takes the log of `adj` to
+ * (log(adjusted_wgh) at LightNE/PathEmbed.h:211) for n host values, as the
+ * sparsifier computes it on the device.  Used to check the exact-log path.
+ */
+int lne_trunc_log_values(lne_ctx* ctx, const double* x, int64_t n, double* out);
+
+/* CSR accessors. */
+int lne_csr_info(const lne_csr* c, int64_t* n, int64_t* nnz);
+int lne_csr_download(lne_ctx* ctx, const lne_csr* c, int64_t* row_ptr, int32_t* col, float* val);
+int lne_csr_device_ptrs(const lne_csr* c, const int64_t** row_ptr, const int32_t** col,
+                        const float** val);
+/* Wrap caller-owned device arrays as a CSR (not freed by lne_csr_free). */
+int lne_csr_wrap_device(lne_ctx* ctx, int64_t n, int64_t nnz, const int64_t* d_row_ptr,
+                        const int32_t* d_col, const float* d_val, lne_csr** out);
+int lne_csr_free(lne_csr* c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIGHTNE_GB300_H */

@@ -1,0 +1,125 @@
+"""ctypes binding of liblightne_gb300.so (the C ABI in include/lightne_gb300.h).
+
+The shared library is the product: importing this module loads it and fails
+loudly when it is missing — there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblightne_gb300.so")
+
+LNE_OK = 0
+LNE_ERR_INVALID = 1
+LNE_ERR_ALLOC = 2
+LNE_ERR_TABLE_FULL = 3
+LNE_ERR_CUDA = 4
+LNE_ERR_UNSUPPORTED = 5
+LNE_ERR_NUMERIC = 6
+
+LNE_PREC_FP32 = 0
+LNE_PREC_BF16 = 1
+
+_STATUS_NAMES = {
+    LNE_ERR_INVALID: "LNE_ERR_INVALID",
+    LNE_ERR_ALLOC: "LNE_ERR_ALLOC",
+    LNE_ERR_TABLE_FULL: "LNE_ERR_TABLE_FULL",
+    LNE_ERR_CUDA: "LNE_ERR_CUDA",
+    LNE_ERR_UNSUPPORTED: "LNE_ERR_UNSUPPORTED",
+    LNE_ERR_NUMERIC: "LNE_ERR_NUMERIC",
+}
+
+
+class LneError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s (%d): %s" % (_STATUS_NAMES.get(status, "LNE_ERR"), status, msg))
+        self.status = status
+
+
+class SparsifyParams(ctypes.Structure):
+    _fields_ = [
+        ("seed", ctypes.c_uint64),
+        ("walk_len", ctypes.c_int64),
+        ("table_size", ctypes.c_int64),
+        ("negative", ctypes.c_int64),
+        ("sample", ctypes.c_int32),
+        ("upper", ctypes.c_int32),
+        ("sample_ratio", ctypes.c_float),
+        ("mem_ratio", ctypes.c_float),
+    ]
+
+
+class SparsifyStats(ctypes.Structure):
+    _fields_ = [
+        ("logn", ctypes.c_double),
+        ("total_samples", ctypes.c_double),
+        ("inv_lambda", ctypes.c_double),
+        ("frac", ctypes.c_double),
+        ("factor", ctypes.c_double),
+        ("m_exact", ctypes.c_double),
+        ("exp_rv_rounded", ctypes.c_int64),
+        ("table_size", ctypes.c_int64),
+        ("capacity", ctypes.c_int64),
+        ("samples_emitted", ctypes.c_int64),
+        ("distinct", ctypes.c_int64),
+        ("nnz_upper", ctypes.c_int64),
+        ("nnz", ctypes.c_int64),
+        ("ms_sample", ctypes.c_float),
+        ("ms_trunclog", ctypes.c_float),
+        ("ms_csr", ctypes.c_float),
+        ("kernel_launches", ctypes.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+VP = ctypes.c_void_p
+I64 = ctypes.c_int64
+I32 = ctypes.c_int32
+PVP = ctypes.POINTER(ctypes.c_void_p)
+
+# name -> (restype, argtypes).  Every symbol include/lightne_gb300.h declares.
+SIGNATURES = {
+    "lne_last_error": (ctypes.c_char_p, []),
+    "lne_version": (ctypes.c_char_p, []),
+    "lne_ctx_create": (ctypes.c_int, [PVP, ctypes.c_int, VP]),
+    "lne_ctx_destroy": (ctypes.c_int, [VP]),
+    "lne_ctx_synchronize": (ctypes.c_int, [VP]),
+    "lne_graph_upload": (ctypes.c_int, [VP, I64, VP, VP, PVP]),
+    "lne_graph_upload_device": (ctypes.c_int, [VP, I64, VP, VP, PVP]),
+    "lne_graph_free": (ctypes.c_int, [VP]),
+    "lne_sparsify": (ctypes.c_int, [VP, VP, ctypes.POINTER(SparsifyParams), PVP, ctypes.POINTER(SparsifyStats)]),
+    "lne_trunc_log_values": (ctypes.c_int, [VP, VP, I64, VP]),
+    "lne_csr_info": (ctypes.c_int, [VP, ctypes.POINTER(I64), ctypes.POINTER(I64)]),
+    "lne_csr_download": (ctypes.c_int, [VP, VP, VP, VP, VP]),
+    "lne_csr_device_ptrs": (ctypes.c_int, [VP, PVP, PVP, PVP]),
+    "lne_csr_wrap_device": (ctypes.c_int, [VP, I64, I64, VP, VP, VP, PVP]),
+    "lne_csr_free": (ctypes.c_int, [VP]),
+}
+
+_lib = None
+
+
+def load():
+    """Load the library (once).  Raises ImportError if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("liblightne_gb300.so not found at %s: run `python -m lightne_gb300.build` "
+                          "(the CUDA library is required; there is no CPU path)" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != LNE_OK:
+        raise LneError(status, load().lne_last_error().decode(errors="replace"))

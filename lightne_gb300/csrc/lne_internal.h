@@ -1,0 +1,85 @@
+// Host-side internals shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/lightne_gb300.h"
+
+namespace lne {
+
+// Per-thread error message, returned by lne_last_error().
+void set_error(const std::string& msg);
+void clear_error();
+
+// Device flags word layout (ctx->d_flags, int32[kFlagWords]).
+enum FlagIndex : int {
+  kFlagTableFull = 0,   // a probe sequence exceeded the probe limit
+  kFlagCountOverflow = 1,
+  kFlagSortOverflow = 2,  // a row exceeded the sort scratch
+  kFlagNumeric = 3,     // Cholesky / Jacobi breakdown
+  kFlagWords = 8,
+};
+
+}  // namespace lne
+
+struct lne_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int* d_flags = nullptr;       // device int32[kFlagWords]
+  int num_sms = 0;
+  size_t smem_optin = 0;
+};
+
+struct lne_graph {
+  int64_t n = 0;
+  int64_t m_dir = 0;            // directed CSR entries (2m)
+  uint2* vdata = nullptr;       // {offset, degree} per vertex (offsets < 2^32)
+  uint32_t* nbrs = nullptr;     // neighbour ids in file order
+  uint32_t* src = nullptr;      // source vertex of each directed entry
+  int64_t* off64 = nullptr;     // offsets as given (int64[n+1])
+  int64_t max_degree = 0;
+};
+
+struct lne_csr {
+  int64_t n = 0;
+  int64_t nnz = 0;
+  int64_t* row_ptr = nullptr;
+  int32_t* col = nullptr;
+  float* val = nullptr;
+  bool owned = true;
+  cudaStream_t stream = nullptr;
+};
+
+#define LNE_CUDA_TRY(expr)                                                           \
+  do {                                                                               \
+    cudaError_t _e = (expr);                                                         \
+    if (_e != cudaSuccess) {                                                         \
+      ::lne::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));          \
+      return LNE_ERR_CUDA;                                                           \
+    }                                                                                \
+  } while (0)
+
+#define LNE_CHECK_ARG(cond, msg)               \
+  do {                                         \
+    if (!(cond)) {                             \
+      ::lne::set_error(std::string(msg));      \
+      return LNE_ERR_INVALID;                  \
+    }                                          \
+  } while (0)
+
+namespace lne {
+
+// Stream-ordered allocation on the context's stream; returns LNE_OK or
+// LNE_ERR_ALLOC with the message set.
+int dalloc(lne_ctx* ctx, void** p, size_t bytes, const char* what);
+void dfree(lne_ctx* ctx, void* p);
+
+// Exclusive scan of int64 counts[0..n) into out[0..n] (out[n] = total),
+// on ctx->stream.  tmp must hold scan_tmp_bytes(n).
+size_t scan_tmp_bytes(int64_t n);
+void scan_exclusive_i64(const int64_t* counts, int64_t* out, int64_t n, void* tmp,
+                        cudaStream_t stream);
+
+}  // namespace lne

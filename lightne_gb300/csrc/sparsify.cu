@@ -1,0 +1,657 @@
+// NetSMF sparsifier on the device: path sampler, pair-count table,
+// trunc-log map and canonical CSR build.
+//
+// Reference: path_embed::generate_trunc_log_matrix_v2 (LightNE/PathEmbed.h:81-369)
+// with par_table (LightNE/par_table.h).
+//
+// Layout in HBM during one call:
+//   table   Slot[capacity]       16 B per slot: u64 key, u64 count (or f64 weight)
+//   rowcnt  i64[n]               kept entries per row, then the scatter cursor
+//   row_ptr i64[n+1]             exclusive scan of rowcnt (the output row_ptr)
+//   packed  u64[nnz]             (col << 32 | float bits) per entry; rows sorted in place
+//   col/val i32[nnz], f32[nnz]   output CSR
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <string>
+
+#include "lne_internal.h"
+#include "lne_math.cuh"
+
+namespace lne {
+
+struct __align__(16) Slot {
+  unsigned long long key;
+  unsigned long long val;
+};
+static constexpr unsigned long long kEmptyKey = ~0ULL;
+// Probe limit of one insert.  The reference gives up after 10^7 probes
+// (LightNE/par_table.h:104-107); under its sizing rule (capacity >= 2x the
+// requested size) a linear-probe run this long only occurs in a table that
+// is essentially full, so the status is the same and the wait is bounded.
+static constexpr uint32_t kMaxProbes = 1u << 16;
+
+struct SampleArgs {
+  uint64_t seed;
+  uint64_t walk_len;
+  uint64_t exp_rv;
+  double frac;
+  double logn;
+  uint64_t mask;
+  int use_frac;
+};
+
+__device__ __forceinline__ bool table_full(const int* flags) {
+  return __ldcg(flags + kFlagTableFull) != 0;
+}
+
+__global__ void k_table_init(Slot* __restrict__ T, uint64_t cap) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x)
+    T[i] = Slot{kEmptyKey, 0ULL};
+}
+
+// Linear-probe insert-or-add (par_table::insert_add, LightNE/par_table.h:86-109).
+// Keys never change once written, so a stale read of a key is still a valid
+// key; a stale EMPTY is resolved by the compare-and-swap.
+template <bool WEIGHTED>
+__device__ __forceinline__ bool table_insert_add(Slot* __restrict__ T, uint64_t mask, uint64_t key,
+                                                 double w, int* flags) {
+  uint64_t h = hash64_2(key) & mask;
+  for (uint32_t p = 0; p < kMaxProbes; ++p) {
+    unsigned long long k = __ldcg(&T[h].key);
+    if (k == kEmptyKey) k = atomicCAS(&T[h].key, kEmptyKey, (unsigned long long)key);
+    if (k == kEmptyKey || k == key) {
+      if (WEIGHTED)
+        atomicAdd(reinterpret_cast<double*>(&T[h].val), w);
+      else
+        atomicAdd(&T[h].val, 1ULL);
+      return true;
+    }
+    h = (h + 1) & mask;
+    if ((p & 1023u) == 1023u && table_full(flags)) return false;
+  }
+  atomicExch(flags + kFlagTableFull, 1);
+  return false;
+}
+
+// One thread per directed CSR entry (u, v): LightNE/PathEmbed.h:128-171.
+// The per-edge generator state is a chain (every draw advances it), so the
+// samples of one edge are sequential; the loop below is a flat state machine
+// that advances one walk step per iteration so the lanes of a warp stay in
+// step regardless of each sample's walk length.
+template <bool SAMPLE>
+__global__ void __launch_bounds__(256) k_sample(const uint2* __restrict__ vd, const uint32_t* __restrict__ nbrs,
+                                                const uint32_t* __restrict__ src, int64_t m_dir, SampleArgs a,
+                                                Slot* __restrict__ table, int* flags,
+                                                unsigned long long* __restrict__ emitted_total) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long emitted = 0;
+  if (e < m_dir) {
+    const uint32_t u = __ldg(src + e), v = __ldg(nbrs + e);
+    uint64_t s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
+    uint64_t todo = a.exp_rv;
+    if (a.use_frac) {
+      todo += (map_uint64(rng_rand(s)) < a.frac) ? 1u : 0u;
+      s = rng_next(s);
+    }
+    double p = 1.0, ipw = 1.0;
+    if (SAMPLE) {
+      const double du = (double)__ldg(&vd[u].y), dv = (double)__ldg(&vd[v].y);
+      p = __dmul_rn(__dadd_rn(__ddiv_rn(1.0, du), __ddiv_rn(1.0, dv)), a.logn);
+      p = p < 1.0 ? p : 1.0;
+      ipw = __ddiv_rn(1.0, p);
+    }
+    uint32_t cur = u, x = 0, left1 = 0, left2 = 0;
+    int phase = 0;  // 0: start a sample, 1: walking from u, 2: walking from v
+    uint32_t since_check = 0;
+    while (true) {
+      if (phase == 0) {
+        if (todo == 0) break;
+        if (++since_check == 32) {
+          since_check = 0;
+          if (table_full(flags)) break;
+        }
+        --todo;
+        if (SAMPLE) {
+          const double eff = map_uint64(rng_rand(s));
+          s = rng_next(s);
+          if (!(eff < p)) continue;
+        }
+        const uint64_t r = rng_rand(s) % a.walk_len + 1;
+        s = rng_next(s);
+        const uint64_t k = rng_rand(s) % r + 1;
+        s = rng_next(s);
+        left1 = (uint32_t)(k - 1);
+        left2 = (uint32_t)(r - k);
+        cur = u;
+        phase = 1;
+      }
+      if (phase == 1 && left1 == 0) {
+        x = cur;
+        cur = v;
+        phase = 2;
+      }
+      if (phase == 2 && left2 == 0) {
+        const uint32_t lo = x < cur ? x : cur, hi = x < cur ? cur : x;
+        if (!table_insert_add<SAMPLE>(table, a.mask, ((uint64_t)lo << 32) + (uint64_t)hi, ipw, flags)) break;
+        ++emitted;
+        phase = 0;
+        continue;
+      }
+      const uint2 d = __ldg(vd + cur);
+      if (d.y == 0) break;  // unreachable for a validated (symmetric) graph
+      const uint32_t idx = mod_u64_u32(rng_rand(s), d.y);
+      cur = __ldg(nbrs + d.x + idx);
+      s = rng_next(s);
+      if (phase == 1)
+        --left1;
+      else
+        --left2;
+    }
+  }
+  // block total of emitted samples
+  for (int o = 16; o > 0; o >>= 1) emitted += __shfl_down_sync(0xffffffffu, emitted, o);
+  __shared__ unsigned long long bsum;
+  if (threadIdx.x == 0) bsum = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0 && emitted) atomicAdd(&bsum, emitted);
+  __syncthreads();
+  if (threadIdx.x == 0 && bsum) atomicAdd(emitted_total, bsum);
+}
+
+// Sum of weights and number of occupied slots (PathEmbed.h:175-188).  Counts
+// are integers and summed exactly; weights (sample mode) are summed per block
+// and then in block order, so the result depends only on the table layout.
+template <bool WEIGHTED>
+__global__ void k_table_sum(const Slot* __restrict__ T, uint64_t cap, unsigned long long* __restrict__ cnt,
+                            unsigned long long* __restrict__ distinct, double* __restrict__ block_w) {
+  unsigned long long c = 0, dcount = 0;
+  double w = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+    const Slot s = T[i];
+    if (s.key != kEmptyKey) {
+      ++dcount;
+      if (WEIGHTED)
+        w += __longlong_as_double((long long)s.val);
+      else
+        c += s.val;
+    }
+  }
+  __shared__ double sw[32];
+  __shared__ unsigned long long sc[32], sd[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    c += __shfl_down_sync(0xffffffffu, c, o);
+    dcount += __shfl_down_sync(0xffffffffu, dcount, o);
+    w += __shfl_down_sync(0xffffffffu, w, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sc[wid] = c; sd[wid] = dcount; sw[wid] = w; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tc = 0, td = 0;
+    double tw = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { tc += sc[i]; td += sd[i]; tw += sw[i]; }
+    if (tc) atomicAdd(cnt, tc);
+    if (td) atomicAdd(distinct, td);
+    block_w[blockIdx.x] = tw;
+  }
+}
+
+__global__ void k_sum_blocks(const double* __restrict__ block_w, int nb, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < nb; ++i) s += block_w[i];
+    *out = s;
+  }
+}
+
+// log(adj) as the reference's double result: CUDA's log (within 1 ulp) where
+// that cannot change the float the value is narrowed to, otherwise the
+// correctly rounded double from the double-double evaluation.
+__device__ __forceinline__ double trunc_log_value(double adj) {
+  double L = log(adj);
+  if (float_rounding_is_close(L)) {
+    const dd r = log_dd(adj);
+    L = __dadd_rn(r.hi, r.lo);
+  }
+  return L;
+}
+
+__global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = trunc_log_value(x[i]);
+}
+
+// Trunc-log map (PathEmbed.h:203-218) fused with the per-row counts of the
+// CSR build (PathEmbed.h:226-288).  Kept slots get the float bits of the
+// log value in `val`; dropped slots become empty.
+template <bool WEIGHTED>
+__global__ void k_trunclog(Slot* __restrict__ T, uint64_t cap, const uint2* __restrict__ vd, double factor,
+                           int upper, unsigned long long* __restrict__ rowcnt,
+                           unsigned long long* __restrict__ kept_total) {
+  unsigned long long kept = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned long long key = T[i].key;
+    if (key == kEmptyKey) continue;
+    const uint32_t u = (uint32_t)(key >> 32), v = (uint32_t)key;
+    const double du = (double)__ldg(&vd[u].y), dv = (double)__ldg(&vd[v].y);
+    const unsigned long long raw = T[i].val;
+    double w = WEIGHTED ? __longlong_as_double((long long)raw) : __ull2double_rn(raw);
+    if (u == v) w = __dmul_rn(w, 2.0);
+    const double adj = __ddiv_rn(__ddiv_rn(__dmul_rn(w, factor), du), dv);
+    const double L = trunc_log_value(adj);
+    if (L > 0.0) {
+      const float f = __double2float_rn(L);
+      T[i].val = (unsigned long long)__float_as_uint(f);
+      atomicAdd(&rowcnt[u], 1ULL);
+      if (!upper && u != v) atomicAdd(&rowcnt[v], 1ULL);
+      ++kept;
+    } else {
+      T[i].key = kEmptyKey;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) kept += __shfl_down_sync(0xffffffffu, kept, o);
+  if ((threadIdx.x & 31) == 0 && kept) atomicAdd(kept_total, kept);
+}
+
+// Scatter each kept entry into its row (and the mirrored row unless -upper),
+// PathEmbed.h:300-311.  rowcnt serves as a decrementing cursor.
+__global__ void k_scatter(const Slot* __restrict__ T, uint64_t cap, const int64_t* __restrict__ row_ptr,
+                          unsigned long long* __restrict__ cursor, int upper, uint64_t* __restrict__ packed) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned long long key = T[i].key;
+    if (key == kEmptyKey) continue;
+    const uint32_t u = (uint32_t)(key >> 32), v = (uint32_t)key;
+    const uint64_t fb = (uint32_t)T[i].val;
+    unsigned long long p = atomicAdd(&cursor[u], ~0ULL) - 1ULL;  // decrement
+    packed[row_ptr[u] + (int64_t)p] = ((uint64_t)v << 32) | fb;
+    if (!upper && u != v) {
+      p = atomicAdd(&cursor[v], ~0ULL) - 1ULL;
+      packed[row_ptr[v] + (int64_t)p] = ((uint64_t)u << 32) | fb;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per-row sort of the packed entries (ascending column), by row length class.
+// All classes use the ascending bitonic network in which the first
+// comparator of each merge stage pairs i with i ^ (k-1) and the following
+// ones pair i with i ^ j.  Every comparator keeps the minimum at the lower
+// index, so a row of length L sorts in place as if padded with +inf up to
+// the next power of two: comparators that touch an index >= L never swap.
+// ---------------------------------------------------------------------------
+enum RowClass { kClsWarp = 0, kClsSmall = 1, kClsMed = 2, kClsLarge = 3, kClsHuge = 4, kNumCls = 5 };
+static constexpr int kCapSmall = 256, kCapMed = 2048, kCapLarge = 16384;
+
+__device__ __forceinline__ void unpack_store(uint64_t x, int32_t* col, float* val, int64_t j) {
+  col[j] = (int32_t)(x >> 32);
+  val[j] = __uint_as_float((uint32_t)x);
+}
+
+__global__ void k_classify_rows(const int64_t* __restrict__ row_ptr, int64_t n, const uint64_t* __restrict__ packed,
+                                int32_t* __restrict__ col, float* __restrict__ val, int* __restrict__ cls_cnt,
+                                uint32_t* __restrict__ cls_rows, int64_t list_stride) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t a = row_ptr[i], L = row_ptr[i + 1] - a;
+  if (L == 0) return;
+  if (L == 1) {
+    unpack_store(packed[a], col, val, a);
+    return;
+  }
+  const int c = L <= 32 ? kClsWarp : L <= kCapSmall ? kClsSmall : L <= kCapMed ? kClsMed : L <= kCapLarge ? kClsLarge : kClsHuge;
+  const int slot = atomicAdd(&cls_cnt[c], 1);
+  cls_rows[(int64_t)c * list_stride + slot] = (uint32_t)i;
+}
+
+__global__ void k_sort_warp_rows(const int64_t* __restrict__ row_ptr, const int* __restrict__ cls_cnt,
+                                 const uint32_t* __restrict__ rows, const uint64_t* __restrict__ packed,
+                                 int32_t* __restrict__ col, float* __restrict__ val) {
+  const int lane = threadIdx.x & 31;
+  const int nrows = cls_cnt[kClsWarp];
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nrows;
+       w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const uint32_t r = rows[w];
+    const int64_t a = row_ptr[r];
+    const int L = (int)(row_ptr[r + 1] - a);
+    uint64_t x = lane < L ? packed[a + lane] : ~0ULL;
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const int partner = (j == (k >> 1)) ? (lane ^ (k - 1)) : (lane ^ j);
+        const uint64_t y = __shfl_sync(0xffffffffu, x, partner);
+        const bool low = lane < partner;
+        x = low ? (x < y ? x : y) : (x < y ? y : x);
+      }
+    }
+    if (lane < L) unpack_store(x, col, val, a + lane);
+  }
+}
+
+__device__ __forceinline__ void bitonic_smem(uint64_t* s, int L) {
+  int N = 1;
+  while (N < L) N <<= 1;
+  const int half = N >> 1;
+  for (int k = 2; k <= N; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int c = threadIdx.x; c < half; c += blockDim.x) {
+        int i, l;
+        if (j == (k >> 1)) {
+          const int blk = c / j, pos = c % j;
+          i = blk * k + pos;
+          l = blk * k + k - 1 - pos;
+        } else {
+          i = (c / j) * 2 * j + (c % j);
+          l = i + j;
+        }
+        if (l < L) {
+          const uint64_t x = s[i], y = s[l];
+          if (x > y) { s[i] = y; s[l] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <int CAP, int CLS>
+__global__ void k_sort_block_rows(const int64_t* __restrict__ row_ptr, const int* __restrict__ cls_cnt,
+                                  const uint32_t* __restrict__ rows, const uint64_t* __restrict__ packed,
+                                  int32_t* __restrict__ col, float* __restrict__ val) {
+  extern __shared__ uint64_t sbuf[];
+  const int nrows = cls_cnt[CLS];
+  for (int w = blockIdx.x; w < nrows; w += gridDim.x) {
+    const uint32_t r = rows[w];
+    const int64_t a = row_ptr[r];
+    const int L = (int)(row_ptr[r + 1] - a);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) sbuf[i] = packed[a + i];
+    __syncthreads();
+    bitonic_smem(sbuf, L);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) unpack_store(sbuf[i], col, val, a + i);
+    __syncthreads();
+  }
+}
+
+// Rows longer than the largest shared-memory class: the same network in
+// global memory, one block per row (rare: only hub rows of large graphs).
+__global__ void k_sort_huge_rows(const int64_t* __restrict__ row_ptr, const int* __restrict__ cls_cnt,
+                                 const uint32_t* __restrict__ rows, uint64_t* __restrict__ packed,
+                                 int32_t* __restrict__ col, float* __restrict__ val) {
+  const int nrows = cls_cnt[kClsHuge];
+  for (int w = blockIdx.x; w < nrows; w += gridDim.x) {
+    const uint32_t r = rows[w];
+    const int64_t a = row_ptr[r];
+    const int64_t L = row_ptr[r + 1] - a;
+    uint64_t* s = packed + a;
+    int64_t N = 1;
+    while (N < L) N <<= 1;
+    const int64_t half = N >> 1;
+    for (int64_t k = 2; k <= N; k <<= 1) {
+      for (int64_t j = k >> 1; j > 0; j >>= 1) {
+        for (int64_t c = threadIdx.x; c < half; c += blockDim.x) {
+          int64_t i, l;
+          if (j == (k >> 1)) {
+            const int64_t blk = c / j, pos = c % j;
+            i = blk * k + pos;
+            l = blk * k + k - 1 - pos;
+          } else {
+            i = (c / j) * 2 * j + (c % j);
+            l = i + j;
+          }
+          if (l < L) {
+            const uint64_t x = s[i], y = s[l];
+            if (x > y) { s[i] = y; s[l] = x; }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    for (int64_t i = threadIdx.x; i < L; i += blockDim.x) unpack_store(s[i], col, val, a + i);
+    __syncthreads();
+  }
+}
+
+static unsigned grid_for(int64_t items, int threads, int64_t cap_blocks) {
+  int64_t b = (items + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap_blocks) b = cap_blocks;
+  return (unsigned)b;
+}
+
+}  // namespace lne
+
+using namespace lne;
+
+namespace {
+
+struct Scratch {
+  lne_ctx* ctx;
+  void* p[12] = {};
+  int k = 0;
+  explicit Scratch(lne_ctx* c) : ctx(c) {}
+  int get(void** out, size_t bytes, const char* what) {
+    int rc = dalloc(ctx, out, bytes, what);
+    if (rc == LNE_OK) p[k++] = *out;
+    return rc;
+  }
+  void release(void* q) {
+    for (int i = 0; i < k; ++i)
+      if (p[i] == q) { dfree(ctx, q); p[i] = nullptr; }
+  }
+  ~Scratch() {
+    for (int i = 0; i < k; ++i) dfree(ctx, p[i]);
+  }
+};
+
+struct Events {
+  cudaEvent_t e[5] = {};
+  Events() { for (auto& x : e) cudaEventCreate(&x); }
+  ~Events() { for (auto& x : e) cudaEventDestroy(x); }
+};
+
+}  // namespace
+
+extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_params* p, lne_csr** out,
+                            lne_sparsify_stats* stats) {
+  LNE_CHECK_ARG(ctx && g && p && out, "lne_sparsify: NULL argument");
+  *out = nullptr;
+  LNE_CHECK_ARG(p->walk_len >= 1, "lne_sparsify: walk_len must be >= 1");
+  LNE_CHECK_ARG(p->negative >= 1, "lne_sparsify: negative must be >= 1");
+  LNE_CHECK_ARG(p->table_size >= 0, "lne_sparsify: table_size must be >= 0");
+  LNE_CHECK_ARG(g->m_dir >= 1, "lne_sparsify: the graph has no edges");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const int64_t n = g->n, m_dir = g->m_dir;
+
+  // Sampling parameters in the reference's evaluation order (PathEmbed.h:89-117).
+  const double logn = log((double)(size_t)n);
+  size_t table_size = (size_t)((double)((size_t)p->walk_len * (size_t)n) * logn * (double)p->mem_ratio);
+  if ((size_t)p->table_size > table_size) table_size = (size_t)p->table_size;
+  size_t bits = 0;
+  for (size_t b = 2 * table_size - 1; b > 0; b >>= 1) ++bits;  // pbbslib::log2_up(2 * table_size)
+  if (bits > 40) { set_error("lne_sparsify: table capacity above 2^40 slots"); return LNE_ERR_UNSUPPORTED; }
+  const uint64_t cap = (uint64_t)1 << bits;
+  const double M = (double)((size_t)p->walk_len * (size_t)n) * logn * (double)p->sample_ratio;
+  const double inv_lambda = M / (double)(size_t)m_dir;
+  const size_t exp_rv = (size_t)inv_lambda;
+  const double frac = inv_lambda - (double)exp_rv;
+
+  Scratch S(ctx);
+  Events ev;
+  Slot* table = nullptr;
+  unsigned long long* counters = nullptr;  // [0] emitted [1] count sum [2] distinct [3] kept
+  double* wsum = nullptr;
+  int rc;
+  if ((rc = S.get((void**)&table, sizeof(Slot) * cap, "pair table"))) return rc;
+  const int sum_blocks = 1024;
+  if ((rc = S.get((void**)&counters, 64 + sizeof(double) * (sum_blocks + 1), "counters"))) return rc;
+  wsum = (double*)((char*)counters + 64);
+  k_table_init<<<grid_for((int64_t)cap, 256, (int64_t)ctx->num_sms * 32), 256, 0, st>>>(table, cap);
+  LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 64, st));
+  LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, st));
+
+  SampleArgs a;
+  a.seed = p->seed;
+  a.walk_len = (uint64_t)p->walk_len;
+  a.exp_rv = (uint64_t)exp_rv;
+  a.frac = frac;
+  a.logn = logn;
+  a.mask = cap - 1;
+  a.use_frac = frac > 0.0000000001 ? 1 : 0;
+
+  cudaEventRecord(ev.e[0], st);
+  const unsigned sblocks = (unsigned)((m_dir + 255) / 256);
+  if (p->sample)
+    k_sample<true><<<sblocks, 256, 0, st>>>(g->vdata, g->nbrs, g->src, m_dir, a, table, ctx->d_flags, counters);
+  else
+    k_sample<false><<<sblocks, 256, 0, st>>>(g->vdata, g->nbrs, g->src, m_dir, a, table, ctx->d_flags, counters);
+  LNE_CUDA_TRY(cudaGetLastError());
+  cudaEventRecord(ev.e[1], st);
+
+  const unsigned tgrid = grid_for((int64_t)cap, 256, (int64_t)ctx->num_sms * 16);
+  const int sgrid = sum_blocks;
+  if (p->sample)
+    k_table_sum<true><<<sgrid, 256, 0, st>>>(table, cap, counters + 1, counters + 2, wsum);
+  else
+    k_table_sum<false><<<sgrid, 256, 0, st>>>(table, cap, counters + 1, counters + 2, wsum);
+  k_sum_blocks<<<1, 32, 0, st>>>(wsum, sgrid, wsum + sum_blocks);
+  unsigned long long h_cnt[3] = {0, 0, 0};
+  double h_w = 0.0;
+  int h_flags[kFlagWords];
+  LNE_CUDA_TRY(cudaMemcpyAsync(h_cnt, counters, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(&h_w, wsum + sum_blocks, sizeof(double), cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(h_flags, ctx->d_flags, sizeof(h_flags), cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaStreamSynchronize(st));
+  LNE_CUDA_TRY(cudaGetLastError());
+  if (h_flags[kFlagTableFull]) {
+    char buf[256];
+    snprintf(buf, sizeof(buf),
+             "lne_sparsify: pair table full (capacity %llu slots); raise -tablesz "
+             "(the reference prints \"looping forever\" and exits)",
+             (unsigned long long)cap);
+    set_error(buf);
+    return LNE_ERR_TABLE_FULL;
+  }
+  const double M_exact = p->sample ? h_w : (double)h_cnt[1];
+  // factor = vol * m / M_exact / 2 / negative, left to right (PathEmbed.h:199-200)
+  const double vol = (double)(size_t)m_dir;
+  const double factor = vol * (double)(size_t)m_dir / M_exact / 2 / (double)(size_t)p->negative;
+
+  unsigned long long* rowcnt = nullptr;
+  int64_t* row_ptr = nullptr;
+  void* scan_tmp = nullptr;
+  if ((rc = S.get((void**)&rowcnt, sizeof(unsigned long long) * n, "row counts"))) return rc;
+  if ((rc = dalloc(ctx, (void**)&row_ptr, sizeof(int64_t) * (n + 1), "row_ptr"))) return rc;
+  if ((rc = S.get(&scan_tmp, scan_tmp_bytes(n), "scan scratch"))) { dfree(ctx, row_ptr); return rc; }
+  LNE_CUDA_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(unsigned long long) * n, st));
+  if (p->sample)
+    k_trunclog<true><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper, rowcnt, counters + 3);
+  else
+    k_trunclog<false><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper, rowcnt, counters + 3);
+  cudaEventRecord(ev.e[2], st);
+  scan_exclusive_i64((const int64_t*)rowcnt, row_ptr, n, scan_tmp, st);
+  int64_t nnz = 0;
+  unsigned long long kept = 0;
+  LNE_CUDA_TRY(cudaMemcpyAsync(&nnz, row_ptr + n, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(&kept, counters + 3, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaStreamSynchronize(st));
+  LNE_CUDA_TRY(cudaGetLastError());
+
+  uint64_t* packed = nullptr;
+  if ((rc = S.get((void**)&packed, sizeof(uint64_t) * (nnz > 0 ? nnz : 1), "packed entries"))) {
+    dfree(ctx, row_ptr);
+    return rc;
+  }
+  k_scatter<<<tgrid, 256, 0, st>>>(table, cap, row_ptr, rowcnt, p->upper, packed);
+  S.release(table);
+  S.release(rowcnt);
+
+  int32_t* col = nullptr;
+  float* val = nullptr;
+  int* cls_cnt = nullptr;
+  uint32_t* cls_rows = nullptr;
+  if ((rc = dalloc(ctx, (void**)&col, sizeof(int32_t) * (nnz > 0 ? nnz : 1), "csr col")) ||
+      (rc = dalloc(ctx, (void**)&val, sizeof(float) * (nnz > 0 ? nnz : 1), "csr val")) ||
+      (rc = S.get((void**)&cls_cnt, sizeof(int) * 8, "row classes")) ||
+      (rc = S.get((void**)&cls_rows, sizeof(uint32_t) * kNumCls * n, "row class lists"))) {
+    dfree(ctx, row_ptr);
+    dfree(ctx, col);
+    dfree(ctx, val);
+    return rc;
+  }
+  LNE_CUDA_TRY(cudaMemsetAsync(cls_cnt, 0, sizeof(int) * 8, st));
+  k_classify_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(row_ptr, n, packed, col, val, cls_cnt, cls_rows, n);
+  const int64_t nrow_blocks = (int64_t)ctx->num_sms * 8;
+  k_sort_warp_rows<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, nrow_blocks * 4)), 256, 0, st>>>(
+      row_ptr, cls_cnt, cls_rows + (int64_t)kClsWarp * n, packed, col, val);
+  k_sort_block_rows<kCapSmall, kClsSmall><<<(unsigned)nrow_blocks, 128, kCapSmall * 8, st>>>(
+      row_ptr, cls_cnt, cls_rows + (int64_t)kClsSmall * n, packed, col, val);
+  k_sort_block_rows<kCapMed, kClsMed><<<(unsigned)nrow_blocks, 256, kCapMed * 8, st>>>(
+      row_ptr, cls_cnt, cls_rows + (int64_t)kClsMed * n, packed, col, val);
+  cudaFuncSetAttribute(k_sort_block_rows<kCapLarge, kClsLarge>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kCapLarge * 8);
+  k_sort_block_rows<kCapLarge, kClsLarge><<<(unsigned)ctx->num_sms, 1024, kCapLarge * 8, st>>>(
+      row_ptr, cls_cnt, cls_rows + (int64_t)kClsLarge * n, packed, col, val);
+  k_sort_huge_rows<<<(unsigned)ctx->num_sms, 1024, 0, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsHuge * n,
+                                                            packed, col, val);
+  cudaEventRecord(ev.e[3], st);
+  cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) {
+    dfree(ctx, row_ptr);
+    dfree(ctx, col);
+    dfree(ctx, val);
+    set_error(std::string("lne_sparsify: kernel launch failed: ") + cudaGetErrorString(le));
+    return LNE_ERR_CUDA;
+  }
+  if (stats) {
+    LNE_CUDA_TRY(cudaEventSynchronize(ev.e[3]));
+    stats->logn = logn;
+    stats->total_samples = M;
+    stats->inv_lambda = inv_lambda;
+    stats->frac = frac;
+    stats->factor = factor;
+    stats->m_exact = M_exact;
+    stats->exp_rv_rounded = (int64_t)exp_rv;
+    stats->table_size = (int64_t)table_size;
+    stats->capacity = (int64_t)cap;
+    stats->samples_emitted = (int64_t)h_cnt[0];
+    stats->distinct = (int64_t)h_cnt[2];
+    stats->nnz_upper = (int64_t)kept;
+    stats->nnz = nnz;
+    cudaEventElapsedTime(&stats->ms_sample, ev.e[0], ev.e[1]);
+    cudaEventElapsedTime(&stats->ms_trunclog, ev.e[1], ev.e[2]);
+    cudaEventElapsedTime(&stats->ms_csr, ev.e[2], ev.e[3]);
+    // init, sample, table sum, block sum, trunc-log, 3 scan, scatter,
+    // classify, 5 row-sort classes
+    stats->kernel_launches = 16;
+  }
+  lne_csr* c = new lne_csr();
+  c->n = n;
+  c->nnz = nnz;
+  c->row_ptr = row_ptr;
+  c->col = col;
+  c->val = val;
+  c->owned = true;
+  c->stream = st;
+  *out = c;
+  return LNE_OK;
+}
+
+extern "C" int lne_trunc_log_values(lne_ctx* ctx, const double* x, int64_t n, double* out) {
+  LNE_CHECK_ARG(ctx && x && out && n >= 0, "lne_trunc_log_values: bad argument");
+  if (n == 0) return LNE_OK;
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  double* d = nullptr;
+  int rc = dalloc(ctx, (void**)&d, sizeof(double) * 2 * n, "trunc-log values");
+  if (rc) return rc;
+  LNE_CUDA_TRY(cudaMemcpyAsync(d, x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  k_trunc_log_values<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(d, n, d + n);
+  LNE_CUDA_TRY(cudaMemcpyAsync(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  dfree(ctx, d);
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}

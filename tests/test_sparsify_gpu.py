@@ -1,0 +1,127 @@
+"""Parity of the device sparsifier (lne_sparsify through the C ABI) with the
+reference: the reference's own CSR for small graphs (tests/golden), and the
+oracle port (pinned to the reference) at config-1 size.  Bit-exact for
+-sample 0: row_ptr, col and the float bits of every value."""
+import glob
+import json
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from lightne_gb300 import graphs
+from lightne_gb300._lib import LNE_ERR_INVALID, LNE_ERR_TABLE_FULL, LneError
+from lightne_gb300.api import Graph, generate_trunc_log_matrix_v2
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+CASES = sorted(glob.glob(os.path.join(GOLDEN, "sparsify_*.npz")))
+
+
+def device_sparsify(ctx, off, nbrs, prm):
+    g = Graph.from_numpy(ctx, off, nbrs)
+    csr, st = generate_trunc_log_matrix_v2(ctx, g, prm["seed"], walk_len=prm["walk_len"], upper=prm["upper"],
+                                           sample=prm["sample"], table_size=prm["tablesz"],
+                                           negative=prm["negative"], sample_ratio=prm["sample_ratio"],
+                                           mem_ratio=prm["mem_ratio"])
+    out = csr.download()
+    csr.free()
+    g.free()
+    return out, st
+
+
+def assert_csr_equal(a, b, exact=True):
+    assert np.array_equal(a[0], b[0]), "row_ptr differs"
+    assert np.array_equal(a[1], b[1]), "col differs"
+    if exact:
+        diff = np.flatnonzero(a[2].view(np.uint32) != b[2].view(np.uint32))
+        assert diff.size == 0, "values differ at %s: %s vs %s" % (diff[:5], a[2][diff[:5]], b[2][diff[:5]])
+    else:
+        np.testing.assert_allclose(a[2], b[2], rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(c)[9:-4] for c in CASES])
+def test_device_matches_reference_golden(ctx, path):
+    z = np.load(path)
+    prm = json.loads(str(z["params"]))
+    got, st = device_sparsify(ctx, z["offsets"], z["nbrs"], prm)
+    assert_csr_equal(got, (z["row_ptr"], z["col"], z["val"]), exact=prm["sample"] == 0)
+    assert st["nnz"] == z["row_ptr"][-1]
+
+
+def test_device_matches_oracle_config1(ctx):
+    # config 1: Chung-Lu n=10,312, m=333,983, T=10, samples = 20*T*m (ratio as float)
+    off, nbrs = graphs.chung_lu(10312, 333983, 2.1, seed=1)
+    ratio = float(np.float32(70.095396))
+    prm = dict(seed=1, walk_len=10, tablesz=13_500_000, negative=1, sample=0, sample_ratio=ratio, mem_ratio=1.0,
+               upper=0)
+    got, st = device_sparsify(ctx, off, nbrs, prm)
+    ref, pst = port.sparsify(off, nbrs, 1, walk_len=10, tablesz=13_500_000, sample_ratio=ratio)
+    assert st["samples_emitted"] == pst["samples"]
+    assert st["distinct"] == pst["distinct"]
+    assert st["m_exact"] == pst["M_exact"] and st["factor"] == pst["factor"]
+    assert_csr_equal(got, ref)
+
+
+def test_device_matches_oracle_midsize_variants(ctx):
+    off, nbrs = graphs.chung_lu(5000, 40000, 2.1, seed=9)
+    for prm in [dict(seed=77, walk_len=5, tablesz=2_000_000, negative=3, sample=0, sample_ratio=0.8,
+                     mem_ratio=1.0, upper=1),
+                dict(seed=2 ** 63 + 11, walk_len=10, tablesz=2_000_000, negative=1, sample=0, sample_ratio=1.3,
+                     mem_ratio=1.0, upper=0)]:
+        got, _ = device_sparsify(ctx, off, nbrs, prm)
+        ref, _ = port.sparsify(off, nbrs, prm["seed"], walk_len=prm["walk_len"], tablesz=prm["tablesz"],
+                               negative=prm["negative"], sample_ratio=prm["sample_ratio"], upper=prm["upper"])
+        assert_csr_equal(got, ref)
+
+
+def test_device_is_deterministic(ctx):
+    off, nbrs = graphs.chung_lu(3000, 30000, 2.1, seed=4)
+    prm = dict(seed=5, walk_len=10, tablesz=2_000_000, negative=1, sample=0, sample_ratio=1.0, mem_ratio=1.0,
+               upper=0)
+    a, _ = device_sparsify(ctx, off, nbrs, prm)
+    b, _ = device_sparsify(ctx, off, nbrs, prm)
+    assert_csr_equal(a, b)
+
+
+def test_table_full_is_a_status_and_context_survives(ctx):
+    off, nbrs = graphs.chung_lu(2000, 20000, 2.1, seed=2)
+    prm = dict(seed=1, walk_len=10, tablesz=1000, negative=1, sample=0, sample_ratio=1.0, mem_ratio=0.0,
+               upper=0)
+    with pytest.raises(LneError) as ei:
+        device_sparsify(ctx, off, nbrs, prm)
+    assert ei.value.status == LNE_ERR_TABLE_FULL
+    # the same context keeps working
+    prm.update(tablesz=2_000_000, mem_ratio=1.0)
+    got, _ = device_sparsify(ctx, off, nbrs, prm)
+    assert got[0][-1] > 0
+
+
+def test_invalid_graph_rejected(ctx):
+    off = np.array([0, 1, 2], dtype=np.int64)
+    nbrs = np.array([1, 5], dtype=np.int32)  # 5 is out of range
+    with pytest.raises(LneError) as ei:
+        Graph.from_numpy(ctx, off, nbrs)
+    assert ei.value.status == LNE_ERR_INVALID
+    with pytest.raises(LneError):
+        Graph.from_numpy(ctx, np.array([0, 2, 1], dtype=np.int64), np.array([1, 0], dtype=np.int32))
+
+
+def test_trunc_log_hard_cases(ctx, lib):
+    cases = json.load(open(os.path.join(GOLDEN, "trunclog_log.json")))["cases"]
+    x = np.array([struct.unpack("<d", struct.pack("<Q", int(c[0], 16)))[0] for c in cases])
+    glibc = np.array([struct.unpack("<d", struct.pack("<Q", int(c[1], 16)))[0] for c in cases])
+    cr = np.array([struct.unpack("<d", struct.pack("<Q", int(c[2], 16)))[0] for c in cases])
+    out = np.empty_like(x)
+    import ctypes
+    rc = lib.lne_trunc_log_values(ctx.handle, ctypes.c_void_p(x.ctypes.data), x.size,
+                                  ctypes.c_void_p(out.ctypes.data))
+    assert rc == 0
+    assert np.array_equal(out.view(np.uint64), cr.view(np.uint64))
+    # against glibc: equal floats wherever glibc itself is correctly rounded
+    ok = glibc.view(np.uint64) == cr.view(np.uint64)
+    assert ok.mean() > 0.99
+    assert np.array_equal(out[ok].astype(np.float32).view(np.uint32), glibc[ok].astype(np.float32).view(np.uint32))
