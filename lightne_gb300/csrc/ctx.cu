@@ -245,10 +245,10 @@ static int graph_build_common(lne_ctx* ctx, lne_graph* g, const int32_t* d_nbrs_
   int* d_bad = nullptr;
   unsigned long long* d_maxdeg = nullptr;
   int rc;
-  if ((rc = dalloc(ctx, (void**)&d_bad, sizeof(int) + sizeof(unsigned long long) * 2, "graph check")))
-    return rc;
+  // [0, 4): int bad flag; [8, 16): u64 max degree
+  if ((rc = dalloc(ctx, (void**)&d_bad, 16, "graph check"))) return rc;
   d_maxdeg = (unsigned long long*)((char*)d_bad + 8);
-  LNE_CUDA_TRY(cudaMemsetAsync(d_bad, 0, 24, ctx->stream));
+  LNE_CUDA_TRY(cudaMemsetAsync(d_bad, 0, 16, ctx->stream));
   if (n > 0) {
     k_graph_build<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(g->off64, n, g->m_dir, g->vdata,
                                                                       d_bad, d_maxdeg);
