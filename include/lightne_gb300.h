@@ -116,6 +116,17 @@ int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_params* p,
  */
 int lne_trunc_log_values(lne_ctx* ctx, const double* x, int64_t n, double* out);
 
+/*
+ * SpMM: Y = alpha * A * X + beta * Y (mkl_sparse_s_mm, row-major,
+ * non-transposed, as LightNE/mklredsvd/mklredsvd.cc:235-245).  X is n x d
+ * with leading dimension ldx (device, FP32 or BF16 per x_prec; rows on
+ * 16-byte boundaries: ldx a multiple of 8), Y is n x d FP32 with ldy.
+ * beta == 0 does not read Y.  Sums are formed in a fixed order: the result
+ * is bitwise reproducible.  The first call on a matrix builds its work list.
+ */
+int lne_spmm(lne_ctx* ctx, const lne_csr* A, int x_prec, const void* X, int64_t ldx, int64_t d, float alpha,
+             float beta, float* Y, int64_t ldy);
+
 /* CSR accessors. */
 int lne_csr_info(const lne_csr* c, int64_t* n, int64_t* nnz);
 int lne_csr_download(lne_ctx* ctx, const lne_csr* c, int64_t* row_ptr, int32_t* col, float* val);

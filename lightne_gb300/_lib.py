@@ -93,6 +93,7 @@ SIGNATURES = {
     "lne_graph_free": (ctypes.c_int, [VP]),
     "lne_sparsify": (ctypes.c_int, [VP, VP, ctypes.POINTER(SparsifyParams), PVP, ctypes.POINTER(SparsifyStats)]),
     "lne_trunc_log_values": (ctypes.c_int, [VP, VP, I64, VP]),
+    "lne_spmm": (ctypes.c_int, [VP, VP, ctypes.c_int, VP, I64, I64, ctypes.c_float, ctypes.c_float, VP, I64]),
     "lne_csr_info": (ctypes.c_int, [VP, ctypes.POINTER(I64), ctypes.POINTER(I64)]),
     "lne_csr_download": (ctypes.c_int, [VP, VP, VP, VP, VP]),
     "lne_csr_device_ptrs": (ctypes.c_int, [VP, PVP, PVP, PVP]),

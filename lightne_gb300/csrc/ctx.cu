@@ -6,6 +6,7 @@
 #include <string>
 
 #include "lne_internal.h"
+#include "lne_math.cuh"
 
 namespace lne {
 
@@ -134,17 +135,18 @@ void scan_exclusive_i64(const int64_t* counts, int64_t* out, int64_t n, void* tm
 // pairs plus the source vertex of every directed entry.
 // ---------------------------------------------------------------------------
 __global__ void k_graph_build(const int64_t* __restrict__ off, int64_t n, int64_t m_dir,
-                              uint2* __restrict__ vdata, int* __restrict__ bad,
+                              Vertex* __restrict__ vdata, int* __restrict__ bad,
                               unsigned long long* __restrict__ maxdeg) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int64_t a = off[i], b = off[i + 1];
   if (a < 0 || b < a || b > m_dir) {
     atomicExch(bad, 1);
-    vdata[i] = make_uint2(0u, 0u);
+    vdata[i] = Vertex{0u, 0u, 1ull};
     return;
   }
-  vdata[i] = make_uint2((uint32_t)a, (uint32_t)(b - a));
+  const uint32_t d = (uint32_t)(b - a);
+  vdata[i] = Vertex{(uint32_t)a, d, gm_magic(d > 0 ? d : 1u)};
   atomicMax(maxdeg, (unsigned long long)(b - a));
 }
 
@@ -278,7 +280,7 @@ static int graph_alloc(lne_ctx* ctx, int64_t n, int64_t m_dir, lne_graph* g) {
   g->n = n;
   g->m_dir = m_dir;
   if ((rc = dalloc(ctx, (void**)&g->off64, sizeof(int64_t) * (n + 1), "graph offsets"))) return rc;
-  if ((rc = dalloc(ctx, (void**)&g->vdata, sizeof(uint2) * (n > 0 ? n : 1), "graph vertex data"))) return rc;
+  if ((rc = dalloc(ctx, (void**)&g->vdata, sizeof(Vertex) * (n > 0 ? n : 1), "graph vertex data"))) return rc;
   if ((rc = dalloc(ctx, (void**)&g->nbrs, sizeof(uint32_t) * (m_dir > 0 ? m_dir : 1), "graph neighbours"))) return rc;
   if ((rc = dalloc(ctx, (void**)&g->src, sizeof(uint32_t) * (m_dir > 0 ? m_dir : 1), "graph sources"))) return rc;
   return LNE_OK;
@@ -286,6 +288,7 @@ static int graph_alloc(lne_ctx* ctx, int64_t n, int64_t m_dir, lne_graph* g) {
 
 int lne_graph_free(lne_graph* g) {
   if (!g) return LNE_OK;
+  free_plan(g->plan);
   cudaFree(g->off64);
   cudaFree(g->vdata);
   cudaFree(g->nbrs);
@@ -401,6 +404,7 @@ int lne_csr_wrap_device(lne_ctx* ctx, int64_t n, int64_t nnz, const int64_t* d_r
 
 int lne_csr_free(lne_csr* c) {
   if (!c) return LNE_OK;
+  free_plan(c->plan);
   if (c->owned) {
     cudaFree(c->row_ptr);
     cudaFree(c->col);

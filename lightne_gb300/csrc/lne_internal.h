@@ -21,6 +21,30 @@ enum FlagIndex : int {
   kFlagWords = 8,
 };
 
+// Per-vertex record of a graph: CSR offset and degree (offsets < 2^32), and
+// the Granlund-Montgomery multiplier of the degree for `rand % degree`.
+struct __align__(16) Vertex {
+  uint32_t off;
+  uint32_t deg;
+  uint64_t magic;
+};
+
+// Work list of one sparse operator for the row-parallel SpMM (built once,
+// cached on the matrix or graph): rows with at most kChunkNnz entries are
+// one work item each; longer rows are cut into kChunkNnz-entry chunks.
+static constexpr int kChunkNnz = 2048;
+struct SpmmPlan {
+  int64_t n_short = 0;              // rows with <= kChunkNnz entries (incl. empty rows)
+  int64_t n_chunks = 0;             // chunks of long rows
+  int64_t n_long = 0;               // long rows
+  uint32_t* short_rows = nullptr;   // [n_short]
+  uint32_t* chunk_row = nullptr;    // [n_chunks]
+  int64_t* chunk_begin = nullptr;   // [n_chunks] first nonzero of each chunk
+  uint32_t* long_rows = nullptr;    // [n_long]
+  int64_t* long_first = nullptr;    // [n_long + 1] first chunk of each long row
+  void* mem = nullptr;              // one allocation backing the arrays
+};
+
 }  // namespace lne
 
 struct lne_ctx {
@@ -35,11 +59,13 @@ struct lne_ctx {
 struct lne_graph {
   int64_t n = 0;
   int64_t m_dir = 0;            // directed CSR entries (2m)
-  uint2* vdata = nullptr;       // {offset, degree} per vertex (offsets < 2^32)
+  lne::Vertex* vdata = nullptr; // {offset, degree, magic} per vertex
   uint32_t* nbrs = nullptr;     // neighbour ids in file order
   uint32_t* src = nullptr;      // source vertex of each directed entry
   int64_t* off64 = nullptr;     // offsets as given (int64[n+1])
   int64_t max_degree = 0;
+  lne::SpmmPlan plan;           // adjacency SpMM work list (propagation)
+  bool plan_ready = false;
 };
 
 struct lne_csr {
@@ -50,6 +76,8 @@ struct lne_csr {
   float* val = nullptr;
   bool owned = true;
   cudaStream_t stream = nullptr;
+  lne::SpmmPlan plan;
+  bool plan_ready = false;
 };
 
 #define LNE_CUDA_TRY(expr)                                                           \
@@ -81,5 +109,10 @@ void dfree(lne_ctx* ctx, void* p);
 size_t scan_tmp_bytes(int64_t n);
 void scan_exclusive_i64(const int64_t* counts, int64_t* out, int64_t n, void* tmp,
                         cudaStream_t stream);
+
+// SpMM work lists (built on ctx->stream; synchronises once).
+int build_plan_csr(lne_ctx* ctx, lne_csr* c);
+int build_plan_graph(lne_ctx* ctx, lne_graph* g);
+void free_plan(SpmmPlan& p);
 
 }  // namespace lne

@@ -39,10 +39,55 @@ LNE_HD double map_uint64(uint64_t u) {
 #endif
 }
 
+// One draw of the generator: returns rand() and advances the state with
+// next(), sharing the h(state) the two have in common.
+LNE_HD uint64_t rng_draw(uint64_t& s) {
+  const uint64_t x = hash64_2(s);
+  s = hash64_2(x);
+  return x;
+}
+
 // x mod d for a 64-bit x and a 32-bit d >= 1: the reference takes
 // `rand() % degree` in 64-bit unsigned arithmetic (LightNE/PathEmbed.h:43).
 LNE_HD uint32_t mod_u64_u32(uint64_t x, uint32_t d) {
   return (uint32_t)(x % (uint64_t)d);
+}
+
+// Division by an invariant 32-bit divisor with a precomputed multiplier,
+// after Granlund and Montgomery, "Division by invariant integers using
+// multiplication" (PLDI 1994), Figure 4.1 (unsigned, N = 64):
+//   l = ceil(log2 d),  m' = floor(2^64 (2^l - d) / d) + 1,
+//   t1 = MULUH(m', x),  q = (t1 + ((x - t1) >> min(l,1))) >> max(l-1,0).
+// Exact for every 64-bit x and 1 <= d < 2^32.
+LNE_HD uint32_t ceil_log2_u32(uint32_t d) {
+#ifdef __CUDA_ARCH__
+  return d <= 1 ? 0u : 32u - (uint32_t)__clz(d - 1);
+#else
+  return d <= 1 ? 0u : 32u - (uint32_t)__builtin_clz(d - 1);
+#endif
+}
+LNE_HD uint64_t gm_magic(uint32_t d) {
+  const uint32_t l = ceil_log2_u32(d);
+  const uint64_t hi = ((uint64_t)1 << l) - (uint64_t)d;  // < d
+  // floor(hi * 2^64 / d) by two base-2^32 long-division steps
+  const uint64_t t1 = hi << 32;
+  const uint64_t q1 = t1 / d, r1 = t1 % d;
+  const uint64_t q2 = (r1 << 32) / d;
+  return ((q1 << 32) + q2) + 1;
+}
+LNE_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+LNE_HD uint32_t gm_mod(uint64_t x, uint32_t d, uint64_t magic) {
+  const uint32_t l = ceil_log2_u32(d);
+  const uint32_t sh1 = l < 1 ? l : 1u, sh2 = l > 0 ? l - 1 : 0u;
+  const uint64_t t1 = umulhi64(magic, x);
+  const uint64_t q = (t1 + ((x - t1) >> sh1)) >> sh2;
+  return (uint32_t)(x - q * (uint64_t)d);
 }
 
 // ---------------------------------------------------------------------------

@@ -82,7 +82,7 @@ __device__ __forceinline__ bool table_insert_add(Slot* __restrict__ T, uint64_t 
 // that advances one walk step per iteration so the lanes of a warp stay in
 // step regardless of each sample's walk length.
 template <bool SAMPLE>
-__global__ void __launch_bounds__(256) k_sample(const uint2* __restrict__ vd, const uint32_t* __restrict__ nbrs,
+__global__ void __launch_bounds__(256) k_sample(const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs,
                                                 const uint32_t* __restrict__ src, int64_t m_dir, SampleArgs a,
                                                 Slot* __restrict__ table, int* flags,
                                                 unsigned long long* __restrict__ emitted_total) {
@@ -93,12 +93,11 @@ __global__ void __launch_bounds__(256) k_sample(const uint2* __restrict__ vd, co
     uint64_t s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
     uint64_t todo = a.exp_rv;
     if (a.use_frac) {
-      todo += (map_uint64(rng_rand(s)) < a.frac) ? 1u : 0u;
-      s = rng_next(s);
+      todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
     }
     double p = 1.0, ipw = 1.0;
     if (SAMPLE) {
-      const double du = (double)__ldg(&vd[u].y), dv = (double)__ldg(&vd[v].y);
+      const double du = (double)__ldg(&vd[u].deg), dv = (double)__ldg(&vd[v].deg);
       p = __dmul_rn(__dadd_rn(__ddiv_rn(1.0, du), __ddiv_rn(1.0, dv)), a.logn);
       p = p < 1.0 ? p : 1.0;
       ipw = __ddiv_rn(1.0, p);
@@ -115,14 +114,11 @@ __global__ void __launch_bounds__(256) k_sample(const uint2* __restrict__ vd, co
         }
         --todo;
         if (SAMPLE) {
-          const double eff = map_uint64(rng_rand(s));
-          s = rng_next(s);
+          const double eff = map_uint64(rng_draw(s));
           if (!(eff < p)) continue;
         }
-        const uint64_t r = rng_rand(s) % a.walk_len + 1;
-        s = rng_next(s);
-        const uint64_t k = rng_rand(s) % r + 1;
-        s = rng_next(s);
+        const uint64_t r = rng_draw(s) % a.walk_len + 1;
+        const uint64_t k = rng_draw(s) % r + 1;
         left1 = (uint32_t)(k - 1);
         left2 = (uint32_t)(r - k);
         cur = u;
@@ -140,11 +136,12 @@ __global__ void __launch_bounds__(256) k_sample(const uint2* __restrict__ vd, co
         phase = 0;
         continue;
       }
-      const uint2 d = __ldg(vd + cur);
-      if (d.y == 0) break;  // unreachable for a validated (symmetric) graph
-      const uint32_t idx = mod_u64_u32(rng_rand(s), d.y);
-      cur = __ldg(nbrs + d.x + idx);
-      s = rng_next(s);
+      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(vd + cur));
+      const uint32_t doff = raw.x, ddeg = raw.y;
+      const uint64_t dmagic = ((uint64_t)raw.w << 32) | raw.z;
+      if (ddeg == 0) break;  // unreachable for a validated (symmetric) graph
+      const uint32_t idx = gm_mod(rng_draw(s), ddeg, dmagic);
+      cur = __ldg(nbrs + doff + idx);
       if (phase == 1)
         --left1;
       else
@@ -228,7 +225,7 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 // CSR build (PathEmbed.h:226-288).  Kept slots get the float bits of the
 // log value in `val`; dropped slots become empty.
 template <bool WEIGHTED>
-__global__ void k_trunclog(Slot* __restrict__ T, uint64_t cap, const uint2* __restrict__ vd, double factor,
+__global__ void k_trunclog(Slot* __restrict__ T, uint64_t cap, const Vertex* __restrict__ vd, double factor,
                            int upper, unsigned long long* __restrict__ rowcnt,
                            unsigned long long* __restrict__ kept_total) {
   unsigned long long kept = 0;
@@ -236,7 +233,7 @@ __global__ void k_trunclog(Slot* __restrict__ T, uint64_t cap, const uint2* __re
     const unsigned long long key = T[i].key;
     if (key == kEmptyKey) continue;
     const uint32_t u = (uint32_t)(key >> 32), v = (uint32_t)key;
-    const double du = (double)__ldg(&vd[u].y), dv = (double)__ldg(&vd[v].y);
+    const double du = (double)__ldg(&vd[u].deg), dv = (double)__ldg(&vd[v].deg);
     const unsigned long long raw = T[i].val;
     double w = WEIGHTED ? __longlong_as_double((long long)raw) : __ull2double_rn(raw);
     if (u == v) w = __dmul_rn(w, 2.0);
@@ -281,18 +278,28 @@ __global__ void k_scatter(const Slot* __restrict__ T, uint64_t cap, const int64_
 // ones pair i with i ^ j.  Every comparator keeps the minimum at the lower
 // index, so a row of length L sorts in place as if padded with +inf up to
 // the next power of two: comparators that touch an index >= L never swap.
+// Rows longer than kCapXL are cut into kCapXL-entry segments sorted the same
+// way, then merged pairwise in global memory (merge path).
 // ---------------------------------------------------------------------------
-enum RowClass { kClsWarp = 0, kClsSmall = 1, kClsMed = 2, kClsLarge = 3, kClsHuge = 4, kNumCls = 5 };
-static constexpr int kCapSmall = 256, kCapMed = 2048, kCapLarge = 16384;
+enum RowClass { kClsWarp = 0, kClsS = 1, kClsM = 2, kClsL = 3, kClsXL = 4, kClsHuge = 5, kNumCls = 6 };
+static constexpr int kCapS = 256, kCapM = 1024, kCapL = 4096, kCapXL = 16384;
+
+struct Segment {  // a run of packed entries to sort in shared memory
+  int64_t start;
+  int32_t len;
+  int32_t final_;  // 1: a whole row, write col/val; 0: a chunk of a long row
+};
 
 __device__ __forceinline__ void unpack_store(uint64_t x, int32_t* col, float* val, int64_t j) {
   col[j] = (int32_t)(x >> 32);
   val[j] = __uint_as_float((uint32_t)x);
 }
 
+// cls_cnt: [kNumCls] counts, [kNumCls] = total entries of huge rows,
+// [kNumCls + 1] = longest huge row.
 __global__ void k_classify_rows(const int64_t* __restrict__ row_ptr, int64_t n, const uint64_t* __restrict__ packed,
-                                int32_t* __restrict__ col, float* __restrict__ val, int* __restrict__ cls_cnt,
-                                uint32_t* __restrict__ cls_rows, int64_t list_stride) {
+                                int32_t* __restrict__ col, float* __restrict__ val, unsigned long long* __restrict__ cls_cnt,
+                                uint32_t* __restrict__ cls_rows, int64_t list_stride, Segment* __restrict__ segs) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t a = row_ptr[i], L = row_ptr[i + 1] - a;
@@ -301,16 +308,35 @@ __global__ void k_classify_rows(const int64_t* __restrict__ row_ptr, int64_t n, 
     unpack_store(packed[a], col, val, a);
     return;
   }
-  const int c = L <= 32 ? kClsWarp : L <= kCapSmall ? kClsSmall : L <= kCapMed ? kClsMed : L <= kCapLarge ? kClsLarge : kClsHuge;
-  const int slot = atomicAdd(&cls_cnt[c], 1);
-  cls_rows[(int64_t)c * list_stride + slot] = (uint32_t)i;
+  if (L <= kCapL) {
+    const int c = L <= 32 ? kClsWarp : L <= kCapS ? kClsS : L <= kCapM ? kClsM : kClsL;
+    const unsigned long long slot = atomicAdd(&cls_cnt[c], 1ULL);
+    cls_rows[(int64_t)c * list_stride + (int64_t)slot] = (uint32_t)i;
+    return;
+  }
+  if (L <= kCapXL) {
+    const unsigned long long slot = atomicAdd(&cls_cnt[kClsXL], 1ULL);
+    segs[slot] = Segment{a, (int32_t)L, 1};
+    return;
+  }
+  const int64_t nseg = (L + kCapXL - 1) / kCapXL;
+  const unsigned long long s0 = atomicAdd(&cls_cnt[kClsXL], (unsigned long long)nseg);
+  for (int64_t c = 0; c < nseg; ++c) {
+    const int64_t b = c * kCapXL;
+    const int64_t len = (L - b) < kCapXL ? (L - b) : kCapXL;
+    segs[s0 + c] = Segment{a + b, (int32_t)len, 0};
+  }
+  const unsigned long long h = atomicAdd(&cls_cnt[kClsHuge], 1ULL);
+  cls_rows[(int64_t)kClsHuge * list_stride + (int64_t)h] = (uint32_t)i;
+  atomicAdd(&cls_cnt[kNumCls], (unsigned long long)L);
+  atomicMax(&cls_cnt[kNumCls + 1], (unsigned long long)L);
 }
 
-__global__ void k_sort_warp_rows(const int64_t* __restrict__ row_ptr, const int* __restrict__ cls_cnt,
+__global__ void k_sort_warp_rows(const int64_t* __restrict__ row_ptr, const unsigned long long* __restrict__ cls_cnt,
                                  const uint32_t* __restrict__ rows, const uint64_t* __restrict__ packed,
                                  int32_t* __restrict__ col, float* __restrict__ val) {
   const int lane = threadIdx.x & 31;
-  const int nrows = cls_cnt[kClsWarp];
+  const int64_t nrows = (int64_t)cls_cnt[kClsWarp];
   for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nrows;
        w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const uint32_t r = rows[w];
@@ -357,13 +383,13 @@ __device__ __forceinline__ void bitonic_smem(uint64_t* s, int L) {
   }
 }
 
-template <int CAP, int CLS>
-__global__ void k_sort_block_rows(const int64_t* __restrict__ row_ptr, const int* __restrict__ cls_cnt,
+template <int CLS>
+__global__ void k_sort_block_rows(const int64_t* __restrict__ row_ptr, const unsigned long long* __restrict__ cls_cnt,
                                   const uint32_t* __restrict__ rows, const uint64_t* __restrict__ packed,
                                   int32_t* __restrict__ col, float* __restrict__ val) {
   extern __shared__ uint64_t sbuf[];
-  const int nrows = cls_cnt[CLS];
-  for (int w = blockIdx.x; w < nrows; w += gridDim.x) {
+  const int64_t nrows = (int64_t)cls_cnt[CLS];
+  for (int64_t w = blockIdx.x; w < nrows; w += gridDim.x) {
     const uint32_t r = rows[w];
     const int64_t a = row_ptr[r];
     const int L = (int)(row_ptr[r + 1] - a);
@@ -375,42 +401,65 @@ __global__ void k_sort_block_rows(const int64_t* __restrict__ row_ptr, const int
   }
 }
 
-// Rows longer than the largest shared-memory class: the same network in
-// global memory, one block per row (rare: only hub rows of large graphs).
-__global__ void k_sort_huge_rows(const int64_t* __restrict__ row_ptr, const int* __restrict__ cls_cnt,
-                                 const uint32_t* __restrict__ rows, uint64_t* __restrict__ packed,
-                                 int32_t* __restrict__ col, float* __restrict__ val) {
-  const int nrows = cls_cnt[kClsHuge];
-  for (int w = blockIdx.x; w < nrows; w += gridDim.x) {
+// Segments of up to kCapXL entries: whole rows write col/val, chunks of
+// long rows are written back sorted in place for the merge passes.
+__global__ void k_sort_segments(const unsigned long long* __restrict__ cls_cnt, const Segment* __restrict__ segs,
+                                uint64_t* __restrict__ packed, int32_t* __restrict__ col, float* __restrict__ val) {
+  extern __shared__ uint64_t sbuf[];
+  const int64_t nseg = (int64_t)cls_cnt[kClsXL];
+  for (int64_t w = blockIdx.x; w < nseg; w += gridDim.x) {
+    const Segment sg = segs[w];
+    for (int i = threadIdx.x; i < sg.len; i += blockDim.x) sbuf[i] = packed[sg.start + i];
+    __syncthreads();
+    bitonic_smem(sbuf, sg.len);
+    if (sg.final_) {
+      for (int i = threadIdx.x; i < sg.len; i += blockDim.x) unpack_store(sbuf[i], col, val, sg.start + i);
+    } else {
+      for (int i = threadIdx.x; i < sg.len; i += blockDim.x) packed[sg.start + i] = sbuf[i];
+    }
+    __syncthreads();
+  }
+}
+
+// One merge pass over the long rows: runs of `run` sorted entries are merged
+// pairwise from `src` into `dst` (same offsets).  One block per (row, pair);
+// each thread finds its split of the merged output by binary search along
+// the merge-path diagonal and merges its share sequentially.  The last pass
+// writes col/val instead of dst.
+__global__ void k_merge_pass(const int64_t* __restrict__ row_ptr, const unsigned long long* __restrict__ cls_cnt,
+                             const uint32_t* __restrict__ rows, const uint64_t* __restrict__ src,
+                             uint64_t* __restrict__ dst, int64_t run, int last, int32_t* __restrict__ col,
+                             float* __restrict__ val) {
+  const int64_t nrows = (int64_t)cls_cnt[kClsHuge];
+  for (int64_t w = blockIdx.x; w < nrows; w += gridDim.x) {
     const uint32_t r = rows[w];
-    const int64_t a = row_ptr[r];
-    const int64_t L = row_ptr[r + 1] - a;
-    uint64_t* s = packed + a;
-    int64_t N = 1;
-    while (N < L) N <<= 1;
-    const int64_t half = N >> 1;
-    for (int64_t k = 2; k <= N; k <<= 1) {
-      for (int64_t j = k >> 1; j > 0; j >>= 1) {
-        for (int64_t c = threadIdx.x; c < half; c += blockDim.x) {
-          int64_t i, l;
-          if (j == (k >> 1)) {
-            const int64_t blk = c / j, pos = c % j;
-            i = blk * k + pos;
-            l = blk * k + k - 1 - pos;
-          } else {
-            i = (c / j) * 2 * j + (c % j);
-            l = i + j;
-          }
-          if (l < L) {
-            const uint64_t x = s[i], y = s[l];
-            if (x > y) { s[i] = y; s[l] = x; }
-          }
+    const int64_t base = row_ptr[r];
+    const int64_t L = row_ptr[r + 1] - base;
+    for (int64_t p0 = 0; p0 < L; p0 += 2 * run) {
+      const int64_t na = (L - p0) < run ? (L - p0) : run;
+      const int64_t rest = L - p0 - na;
+      const int64_t nb = rest < run ? rest : run;
+      const uint64_t* A = src + base + p0;
+      const uint64_t* B = A + na;
+      const int64_t tot = na + nb;
+      const int64_t per = (tot + blockDim.x - 1) / blockDim.x;
+      const int64_t d0 = (int64_t)threadIdx.x * per;
+      if (d0 < tot) {
+        const int64_t d1 = (d0 + per) < tot ? (d0 + per) : tot;
+        // largest i in [max(0, d0-nb), min(d0, na)] with A[i-1] <= B[d0-i]
+        int64_t lo = d0 - nb > 0 ? d0 - nb : 0, hi = d0 < na ? d0 : na;
+        while (lo < hi) {
+          const int64_t mid = (lo + hi + 1) >> 1;
+          if (A[mid - 1] <= B[d0 - mid]) lo = mid; else hi = mid - 1;
         }
-        __syncthreads();
+        int64_t i = lo, j = d0 - lo;
+        for (int64_t o = d0; o < d1; ++o) {
+          uint64_t x;
+          if (j >= nb || (i < na && A[i] <= B[j])) x = A[i++]; else x = B[j++];
+          if (last) unpack_store(x, col, val, base + p0 + o); else dst[base + p0 + o] = x;
+        }
       }
     }
-    for (int64_t i = threadIdx.x; i < L; i += blockDim.x) unpack_store(s[i], col, val, a + i);
-    __syncthreads();
   }
 }
 
@@ -571,32 +620,60 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
 
   int32_t* col = nullptr;
   float* val = nullptr;
-  int* cls_cnt = nullptr;
+  unsigned long long* cls_cnt = nullptr;
   uint32_t* cls_rows = nullptr;
+  Segment* segs = nullptr;
+  const int64_t max_segs = n + nnz / kCapXL + 8;
   if ((rc = dalloc(ctx, (void**)&col, sizeof(int32_t) * (nnz > 0 ? nnz : 1), "csr col")) ||
       (rc = dalloc(ctx, (void**)&val, sizeof(float) * (nnz > 0 ? nnz : 1), "csr val")) ||
-      (rc = S.get((void**)&cls_cnt, sizeof(int) * 8, "row classes")) ||
-      (rc = S.get((void**)&cls_rows, sizeof(uint32_t) * kNumCls * n, "row class lists"))) {
+      (rc = S.get((void**)&cls_cnt, sizeof(unsigned long long) * 16, "row classes")) ||
+      (rc = S.get((void**)&cls_rows, sizeof(uint32_t) * kNumCls * n, "row class lists")) ||
+      (rc = S.get((void**)&segs, sizeof(Segment) * max_segs, "sort segments"))) {
     dfree(ctx, row_ptr);
     dfree(ctx, col);
     dfree(ctx, val);
     return rc;
   }
-  LNE_CUDA_TRY(cudaMemsetAsync(cls_cnt, 0, sizeof(int) * 8, st));
-  k_classify_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(row_ptr, n, packed, col, val, cls_cnt, cls_rows, n);
-  const int64_t nrow_blocks = (int64_t)ctx->num_sms * 8;
-  k_sort_warp_rows<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, nrow_blocks * 4)), 256, 0, st>>>(
-      row_ptr, cls_cnt, cls_rows + (int64_t)kClsWarp * n, packed, col, val);
-  k_sort_block_rows<kCapSmall, kClsSmall><<<(unsigned)nrow_blocks, 128, kCapSmall * 8, st>>>(
-      row_ptr, cls_cnt, cls_rows + (int64_t)kClsSmall * n, packed, col, val);
-  k_sort_block_rows<kCapMed, kClsMed><<<(unsigned)nrow_blocks, 256, kCapMed * 8, st>>>(
-      row_ptr, cls_cnt, cls_rows + (int64_t)kClsMed * n, packed, col, val);
-  cudaFuncSetAttribute(k_sort_block_rows<kCapLarge, kClsLarge>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       kCapLarge * 8);
-  k_sort_block_rows<kCapLarge, kClsLarge><<<(unsigned)ctx->num_sms, 1024, kCapLarge * 8, st>>>(
-      row_ptr, cls_cnt, cls_rows + (int64_t)kClsLarge * n, packed, col, val);
-  k_sort_huge_rows<<<(unsigned)ctx->num_sms, 1024, 0, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsHuge * n,
-                                                            packed, col, val);
+  LNE_CUDA_TRY(cudaMemsetAsync(cls_cnt, 0, sizeof(unsigned long long) * 16, st));
+  int launches = 15;  // 9 before this point, 6 sort launches below
+  k_classify_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(row_ptr, n, packed, col, val, cls_cnt, cls_rows, n,
+                                                               segs);
+  const int64_t sms = ctx->num_sms;
+  k_sort_warp_rows<<<(unsigned)(sms * 16), 256, 0, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsWarp * n, packed,
+                                                          col, val);
+  k_sort_block_rows<kClsS><<<(unsigned)(sms * 16), 128, kCapS * 8, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsS * n,
+                                                                         packed, col, val);
+  k_sort_block_rows<kClsM><<<(unsigned)(sms * 8), 256, kCapM * 8, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsM * n,
+                                                                        packed, col, val);
+  k_sort_block_rows<kClsL><<<(unsigned)(sms * 4), 512, kCapL * 8, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsL * n,
+                                                                        packed, col, val);
+  cudaFuncSetAttribute(k_sort_segments, cudaFuncAttributeMaxDynamicSharedMemorySize, kCapXL * 8);
+  k_sort_segments<<<(unsigned)sms, 1024, kCapXL * 8, st>>>(cls_cnt, segs, packed, col, val);
+  unsigned long long h_cls[16];
+  LNE_CUDA_TRY(cudaMemcpyAsync(h_cls, cls_cnt, sizeof(h_cls), cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h_cls[kClsHuge] > 0) {
+    uint64_t* other = nullptr;
+    if ((rc = S.get((void**)&other, sizeof(uint64_t) * (nnz > 0 ? nnz : 1), "merge buffer"))) {
+      dfree(ctx, row_ptr);
+      dfree(ctx, col);
+      dfree(ctx, val);
+      return rc;
+    }
+    const int64_t maxL = (int64_t)h_cls[kNumCls + 1];
+    uint64_t* src = packed;
+    uint64_t* dst = other;
+    const unsigned mgrid = (unsigned)std::min<int64_t>((int64_t)h_cls[kClsHuge], sms * 8);
+    for (int64_t run = kCapXL; run < maxL; run *= 2) {
+      const int last = (2 * run >= maxL) ? 1 : 0;
+      k_merge_pass<<<mgrid, 512, 0, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsHuge * n, src, dst, run, last,
+                                          col, val);
+      ++launches;
+      uint64_t* t = src;
+      src = dst;
+      dst = t;
+    }
+  }
   cudaEventRecord(ev.e[3], st);
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) {
@@ -625,8 +702,8 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     cudaEventElapsedTime(&stats->ms_trunclog, ev.e[1], ev.e[2]);
     cudaEventElapsedTime(&stats->ms_csr, ev.e[2], ev.e[3]);
     // init, sample, table sum, block sum, trunc-log, 3 scan, scatter,
-    // classify, 5 row-sort classes
-    stats->kernel_launches = 16;
+    // classify, 5 row-sort classes, merge passes
+    stats->kernel_launches = launches;
   }
   lne_csr* c = new lne_csr();
   c->n = n;

@@ -1,0 +1,147 @@
+// SpMM front end: work-list planning, configuration dispatch and the
+// public lne_spmm entry point (mkl_sparse_s_mm, row-major, non-transposed).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "lne_internal.h"
+#include "spmm_core.cuh"
+#include "spmm_dispatch.cuh"
+
+namespace lne {
+
+template <class Rows>
+__global__ void k_plan_count(Rows R, int64_t n, int64_t* __restrict__ is_short, int64_t* __restrict__ nchunk,
+                             int64_t* __restrict__ is_long) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int64_t len = R.end(r) - R.begin(r);
+  const bool lg = len > kChunkNnz;
+  is_short[r] = lg ? 0 : 1;
+  is_long[r] = lg ? 1 : 0;
+  nchunk[r] = lg ? (len + kChunkNnz - 1) / kChunkNnz : 0;
+}
+
+template <class Rows>
+__global__ void k_plan_fill(Rows R, int64_t n, const int64_t* __restrict__ pos_short,
+                            const int64_t* __restrict__ pos_chunk, const int64_t* __restrict__ pos_long,
+                            SpmmPlan p) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int64_t b = R.begin(r), len = R.end(r) - b;
+  if (len <= kChunkNnz) {
+    p.short_rows[pos_short[r]] = (uint32_t)r;
+  } else {
+    const int64_t L = pos_long[r], c0 = pos_chunk[r];
+    p.long_rows[L] = (uint32_t)r;
+    p.long_first[L] = c0;
+    const int64_t nc = (len + kChunkNnz - 1) / kChunkNnz;
+    for (int64_t c = 0; c < nc; ++c) {
+      p.chunk_row[c0 + c] = (uint32_t)r;
+      p.chunk_begin[c0 + c] = b + c * kChunkNnz;
+    }
+  }
+  if (r == n - 1) p.long_first[pos_long[n]] = pos_chunk[n];
+}
+
+template <class Rows>
+static int build_plan(lne_ctx* ctx, Rows R, int64_t n, SpmmPlan& plan) {
+  cudaStream_t st = ctx->stream;
+  int64_t* cnt = nullptr;  // 3 count arrays + 3 position arrays (n+1 each)
+  void* tmp = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, (void**)&cnt, sizeof(int64_t) * 6 * (n + 1), "spmm plan counts"))) return rc;
+  if ((rc = dalloc(ctx, &tmp, scan_tmp_bytes(n), "spmm plan scan"))) { dfree(ctx, cnt); return rc; }
+  int64_t *is_short = cnt, *nchunk = cnt + (n + 1), *is_long = cnt + 2 * (n + 1);
+  int64_t *pos_short = cnt + 3 * (n + 1), *pos_chunk = cnt + 4 * (n + 1), *pos_long = cnt + 5 * (n + 1);
+  const unsigned g = (unsigned)((n + 255) / 256);
+  k_plan_count<<<g, 256, 0, st>>>(R, n, is_short, nchunk, is_long);
+  scan_exclusive_i64(is_short, pos_short, n, tmp, st);
+  scan_exclusive_i64(nchunk, pos_chunk, n, tmp, st);
+  scan_exclusive_i64(is_long, pos_long, n, tmp, st);
+  int64_t tot[3];
+  LNE_CUDA_TRY(cudaMemcpyAsync(&tot[0], pos_short + n, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(&tot[1], pos_chunk + n, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(&tot[2], pos_long + n, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaStreamSynchronize(st));
+  plan.n_short = tot[0];
+  plan.n_chunks = tot[1];
+  plan.n_long = tot[2];
+  const size_t bytes = sizeof(uint32_t) * (plan.n_short + plan.n_chunks + plan.n_long) +
+                       sizeof(int64_t) * (plan.n_chunks + plan.n_long + 1) + 64;
+  char* m = nullptr;
+  if ((rc = dalloc(ctx, (void**)&m, bytes, "spmm plan"))) { dfree(ctx, tmp); dfree(ctx, cnt); return rc; }
+  plan.mem = m;
+  plan.chunk_begin = (int64_t*)m;
+  plan.long_first = plan.chunk_begin + plan.n_chunks;
+  plan.short_rows = (uint32_t*)(plan.long_first + plan.n_long + 1);
+  plan.chunk_row = plan.short_rows + plan.n_short;
+  plan.long_rows = plan.chunk_row + plan.n_chunks;
+  k_plan_fill<<<g, 256, 0, st>>>(R, n, pos_short, pos_chunk, pos_long, plan);
+  dfree(ctx, tmp);
+  dfree(ctx, cnt);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+int build_plan_csr(lne_ctx* ctx, lne_csr* c) {
+  if (c->plan_ready) return LNE_OK;
+  CsrRows R{c->row_ptr, c->col, c->val};
+  int rc = build_plan(ctx, R, c->n, c->plan);
+  if (rc == LNE_OK) c->plan_ready = true;
+  return rc;
+}
+
+int build_plan_graph(lne_ctx* ctx, lne_graph* g) {
+  if (g->plan_ready) return LNE_OK;
+  GraphRows R{g->vdata, g->nbrs};
+  int rc = build_plan(ctx, R, g->n, g->plan);
+  if (rc == LNE_OK) g->plan_ready = true;
+  return rc;
+}
+
+void free_plan(SpmmPlan& p) {
+  if (p.mem) cudaFree(p.mem);
+  p = SpmmPlan();
+}
+
+// Y = alpha * acc + beta * Y on columns < d (beta == 0 does not read Y).
+struct EpiAxpby {
+  float alpha, beta;
+  float* __restrict__ Y;
+  int64_t ldy;
+  int d;
+  template <int N>
+  __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&a)[N]) const {
+    float* y = Y + r * ldy + e0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      if (e0 + i < d) y[i] = beta == 0.f ? alpha * a[i] : fmaf(alpha, a[i], beta * y[i]);
+    }
+  }
+};
+
+}  // namespace lne
+
+using namespace lne;
+
+extern "C" int lne_spmm(lne_ctx* ctx, const lne_csr* A, int x_prec, const void* X, int64_t ldx, int64_t d,
+                        float alpha, float beta, float* Y, int64_t ldy) {
+  LNE_CHECK_ARG(ctx && A && X && Y, "lne_spmm: NULL argument");
+  LNE_CHECK_ARG(d >= 1 && ldx >= d && ldy >= d, "lne_spmm: need 1 <= d <= ldx, ldy");
+  LNE_CHECK_ARG(x_prec == LNE_PREC_FP32 || x_prec == LNE_PREC_BF16, "lne_spmm: x_prec must be FP32 or BF16");
+  LNE_CHECK_ARG(ldx % 8 == 0 && ((uintptr_t)X % 16) == 0,
+                "lne_spmm: X rows must start on 16-byte boundaries (ldx a multiple of 8)");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  lne_csr* Am = const_cast<lne_csr*>(A);
+  int rc = build_plan_csr(ctx, Am);
+  if (rc) return rc;
+  CsrRows R{A->row_ptr, A->col, A->val};
+  EpiAxpby epi{alpha, beta, Y, ldy, (int)d};
+  if (x_prec == LNE_PREC_FP32)
+    rc = spmm_run<float>(ctx, R, Am->plan, (const float*)X, ldx, d, epi);
+  else
+    rc = spmm_run<__nv_bfloat16>(ctx, R, Am->plan, (const __nv_bfloat16*)X, ldx, d, epi);
+  return rc;
+}

@@ -1,0 +1,184 @@
+// Row-parallel SpMM core: Y[i,:] = epi(i, sum_j v_ij * X[c_ij, :]).
+//
+// Work is split into items so that no warp walks more than kChunkNnz
+// nonzeros: a row with at most kChunkNnz entries is one item; a longer row
+// is cut into chunks whose partial sums go to a scratch buffer and are added
+// in chunk order by a second kernel.  Every output is therefore a sum in a
+// fixed order: results are bitwise reproducible run to run.
+//
+// Within an item the warp is split into P = 32/G groups of G lanes; lane gl
+// of a group owns the 16-byte column vectors gl, gl+G, ... of the row, and
+// group g takes the nonzeros t with t % P == g.  Column ids (and values) are
+// loaded 32 at a time, one per lane, and broadcast with shuffles; the
+// gathers of kUnroll nonzeros are issued before their FMAs so that every
+// lane keeps several 16-byte loads in flight.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dense_common.cuh"
+#include "lne_internal.h"
+
+namespace lne {
+
+static constexpr unsigned kFull = 0xffffffffu;
+
+// Access to a sparse operator's rows.
+struct CsrRows {  // explicit CSR: int64 row_ptr, int32 col, float val
+  const int64_t* __restrict__ row_ptr;
+  const int32_t* __restrict__ col;
+  const float* __restrict__ val;
+  __device__ __forceinline__ int64_t begin(int64_t r) const { return __ldg(row_ptr + r); }
+  __device__ __forceinline__ int64_t end(int64_t r) const { return __ldg(row_ptr + r + 1); }
+  __device__ __forceinline__ uint32_t c(int64_t j) const { return (uint32_t)__ldg(col + j); }
+  __device__ __forceinline__ float v(int64_t j) const { return __ldg(val + j); }
+  static constexpr bool kHasVal = true;
+};
+
+struct GraphRows {  // graph adjacency: {offset, degree} per vertex, unit values
+  const Vertex* __restrict__ vdata;
+  const uint32_t* __restrict__ nbrs;
+  __device__ __forceinline__ int64_t begin(int64_t r) const { return (int64_t)__ldg(&vdata[r].off); }
+  __device__ __forceinline__ int64_t end(int64_t r) const {
+    return (int64_t)__ldg(&vdata[r].off) + (int64_t)__ldg(&vdata[r].deg);
+  }
+  __device__ __forceinline__ uint32_t c(int64_t j) const { return __ldg(nbrs + j); }
+  __device__ __forceinline__ float v(int64_t) const { return 1.0f; }
+  static constexpr bool kHasVal = false;
+};
+
+template <typename XT, int VPL>
+struct Acc {
+  static constexpr int E = Vec16<XT>::E;
+  float a[VPL][E];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int k = 0; k < VPL; ++k)
+#pragma unroll
+      for (int e = 0; e < E; ++e) a[k][e] = 0.f;
+  }
+};
+
+// Accumulate nonzeros [j0, j1) of the operator into acc (per group), then
+// reduce across the P groups so that the lanes of group 0 hold the sums.
+template <typename XT, int G, int VPL, class Rows>
+__device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64_t j1, const XT* __restrict__ X,
+                                                int64_t ldx, int C, Acc<XT, VPL>& acc) {
+  constexpr int P = 32 / G;
+  constexpr int E = Vec16<XT>::E;
+  constexpr int kUnroll = 4;
+  const int lane = threadIdx.x & 31;
+  const int grp = lane / G, gl = lane % G;
+  for (int64_t base = j0; base < j1; base += 32) {
+    const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);
+    const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;
+    const float v = Rows::kHasVal ? (lane < cnt ? R.v(base + lane) : 0.f) : 1.f;
+    for (int t0 = 0; t0 < cnt; t0 += P * kUnroll) {
+      uint32_t cc[kUnroll];
+      float vv[kUnroll];
+      float x[kUnroll][VPL][E];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        const int t = t0 + u * P + grp;
+        cc[u] = __shfl_sync(kFull, c, t & 31);
+        vv[u] = Rows::kHasVal ? __shfl_sync(kFull, v, t & 31) : 1.f;
+        const XT* xr = X + (int64_t)cc[u] * ldx;
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          const int ch = gl + G * k;
+          if (t < cnt && ch < C) {
+            Vec16<XT>::load(xr + ch * E, x[u][k]);
+          } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[u][k][e] = 0.f;
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+        for (int k = 0; k < VPL; ++k)
+#pragma unroll
+          for (int e = 0; e < E; ++e) acc.a[k][e] = fmaf(vv[u], x[u][k][e], acc.a[k][e]);
+    }
+  }
+#pragma unroll
+  for (int o = G; o < 32; o <<= 1)
+#pragma unroll
+    for (int k = 0; k < VPL; ++k)
+#pragma unroll
+      for (int e = 0; e < E; ++e) acc.a[k][e] += __shfl_xor_sync(kFull, acc.a[k][e], o);
+}
+
+// Main kernel: short rows call the epilogue directly; chunks of long rows
+// store partial sums (FP32, ld = ldp) for k_spmm_finish.
+template <typename XT, int G, int VPL, class Rows, class Epi>
+__global__ void __launch_bounds__(256, 2) k_spmm(Rows R, SpmmPlan plan, const XT* __restrict__ X, int64_t ldx, int C,
+                                              float* __restrict__ partial, int64_t ldp, int e_base, Epi epi) {
+  constexpr int E = Vec16<XT>::E;
+  const int lane = threadIdx.x & 31;
+  const int gl = lane % G;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t items = plan.n_short + plan.n_chunks;
+  for (int64_t it = warp; it < items; it += nwarps) {
+    Acc<XT, VPL> acc;
+    acc.zero();
+    if (it < plan.n_short) {
+      const uint32_t r = __ldg(plan.short_rows + it);
+      spmm_accumulate<XT, G, VPL>(R, R.begin(r), R.end(r), X, ldx, C, acc);
+      if (lane < G) {
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          const int ch = gl + G * k;
+          if (ch < C) epi(r, e_base + ch * E, acc.a[k]);
+        }
+      }
+    } else {
+      const int64_t ci = it - plan.n_short;
+      const int64_t b = __ldg(plan.chunk_begin + ci);
+      const uint32_t r = __ldg(plan.chunk_row + ci);
+      int64_t e = R.end(r);
+      const int64_t lim = b + kChunkNnz;
+      e = e < lim ? e : lim;
+      spmm_accumulate<XT, G, VPL>(R, b, e, X, ldx, C, acc);
+      if (lane < G) {
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          const int ch = gl + G * k;
+          if (ch < C) {
+            float* p = partial + ci * ldp + ch * E;
+#pragma unroll
+            for (int q = 0; q < E; q += 4)
+              *reinterpret_cast<float4*>(p + q) = make_float4(acc.a[k][q], acc.a[k][q + 1], acc.a[k][q + 2],
+                                                             acc.a[k][q + 3]);
+          }
+        }
+      }
+    }
+  }
+}
+
+// Long rows: add the chunk partials in order and apply the epilogue.
+// One warp per long row; lanes cover the row in 16-byte (4-float) vectors.
+template <class Epi>
+__global__ void k_spmm_finish(SpmmPlan plan, const float* __restrict__ partial, int64_t ldp, int cols, int e_base,
+                              Epi epi) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp; w < plan.n_long; w += nwarps) {
+    const uint32_t r = plan.long_rows[w];
+    const int64_t c0 = plan.long_first[w], c1 = plan.long_first[w + 1];
+    for (int q = lane * 4; q < cols; q += 128) {
+      float s[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int64_t ci = c0; ci < c1; ++ci) {
+        const float4 v = *reinterpret_cast<const float4*>(partial + ci * ldp + q);
+        s[0] += v.x; s[1] += v.y; s[2] += v.z; s[3] += v.w;
+      }
+      epi(r, e_base + q, s);
+    }
+  }
+}
+
+}  // namespace lne

@@ -1,0 +1,70 @@
+// Host-side launcher of the SpMM core: picks the lane layout for the row
+// width and walks column slabs of at most 128 16-byte vectors.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "lne_internal.h"
+#include "spmm_core.cuh"
+
+namespace lne {
+
+template <typename XT, int G, int VPL, class Rows, class Epi>
+static void spmm_launch(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int64_t ldx, int C, float* partial,
+                        int64_t ldp, int e_base, const Epi& epi) {
+  const int64_t items = plan.n_short + plan.n_chunks;
+  int64_t blocks = (items + 7) / 8;
+  const int64_t cap = (int64_t)ctx->num_sms * 16;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  k_spmm<XT, G, VPL, Rows, Epi><<<(unsigned)blocks, 256, 0, ctx->stream>>>(R, plan, X, ldx, C, partial, ldp, e_base,
+                                                                          epi);
+}
+
+// Runs Y-epilogue(A * X) over all rows.  X rows: ldx elements, 16-byte
+// aligned; d columns are produced (the epilogue sees element offsets).
+template <typename XT, class Rows, class Epi>
+static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int64_t ldx, int64_t d, const Epi& epi,
+                    int* launches = nullptr) {
+  constexpr int E = Vec16<XT>::E;
+  const int64_t c_total = (d + E - 1) / E;
+  float* partial = nullptr;
+  int rc;
+  int nl = 0;
+  for (int64_t c_off = 0; c_off < c_total; c_off += 128) {
+    const int C = (int)((c_total - c_off) < 128 ? (c_total - c_off) : 128);
+    const int64_t ldp = (int64_t)C * E;
+    if (plan.n_chunks > 0 && partial == nullptr) {
+      const int64_t w = (c_total < 128 ? c_total : 128) * E;
+      if ((rc = dalloc(ctx, (void**)&partial, sizeof(float) * plan.n_chunks * w, "spmm partials"))) return rc;
+    }
+    const XT* Xs = X + c_off * E;
+    const int e_base = (int)(c_off * E);
+    if (C <= 8)
+      spmm_launch<XT, 8, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+    else if (C <= 16)
+      spmm_launch<XT, 16, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+    else if (C <= 32)
+      spmm_launch<XT, 32, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+    else if (C <= 64)
+      spmm_launch<XT, 32, 2>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+    else
+      spmm_launch<XT, 32, 4>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+    ++nl;
+    if (plan.n_long > 0) {
+      int64_t blocks = (plan.n_long + 7) / 8;
+      if (blocks > (int64_t)ctx->num_sms * 8) blocks = (int64_t)ctx->num_sms * 8;
+      k_spmm_finish<Epi><<<(unsigned)blocks, 256, 0, ctx->stream>>>(plan, partial, ldp, (int)ldp, e_base, epi);
+      ++nl;
+    }
+  }
+  if (partial) dfree(ctx, partial);
+  if (launches) *launches += nl;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("spmm launch: ") + cudaGetErrorString(e));
+    return LNE_ERR_CUDA;
+  }
+  return LNE_OK;
+}
+
+}  // namespace lne

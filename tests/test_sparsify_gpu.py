@@ -125,3 +125,25 @@ def test_trunc_log_hard_cases(ctx, lib):
     ok = glibc.view(np.uint64) == cr.view(np.uint64)
     assert ok.mean() > 0.99
     assert np.array_equal(out[ok].astype(np.float32).view(np.uint32), glibc[ok].astype(np.float32).view(np.uint32))
+
+
+def test_hub_rows_use_merge_passes(ctx):
+    # a star plus a sparse Chung-Lu part: the hub's row of M has far more
+    # than 16384 entries, so it is sorted in segments and merged
+    from lightne_gb300.graphs import csr_from_edges
+    n = 60000
+    leaves = np.arange(1, n, dtype=np.int64)
+    o2, n2 = graphs.chung_lu(n, 30000, 2.1, seed=8)
+    src = np.repeat(np.arange(n), np.diff(o2))
+    keep = src < n2
+    lo = np.concatenate([np.zeros(n - 1, np.int64), src[keep]])
+    hi = np.concatenate([leaves, n2[keep].astype(np.int64)])
+    key = np.unique(lo * n + hi)
+    off, nbrs = csr_from_edges(n, key // n, key % n)
+    prm = dict(seed=31, walk_len=3, tablesz=3_000_000, negative=1, sample=0, sample_ratio=0.6, mem_ratio=1.0,
+               upper=0)
+    got, st = device_sparsify(ctx, off, nbrs, prm)
+    rl = np.diff(got[0])
+    assert rl.max() > 2 * 16384, rl.max()
+    ref, _ = port.sparsify(off, nbrs, 31, walk_len=3, tablesz=3_000_000, sample_ratio=0.6)
+    assert_csr_equal(got, ref)
