@@ -57,7 +57,8 @@ const char* lne_last_error(void);
 /* Library version string. */
 const char* lne_version(void);
 
-/* Context: device, stream (a cudaStream_t, or NULL for a private stream). */
+/* Context: device and the cudaStream_t all of its work is ordered on
+ * (NULL: the default stream). */
 int lne_ctx_create(lne_ctx** out, int device, void* stream);
 int lne_ctx_destroy(lne_ctx* ctx);
 /* Wait for all work queued on the context's stream. */
@@ -126,6 +127,86 @@ int lne_trunc_log_values(lne_ctx* ctx, const double* x, int64_t n, double* out);
  */
 int lne_spmm(lne_ctx* ctx, const lne_csr* A, int x_prec, const void* X, int64_t ldx, int64_t d, float alpha,
              float beta, float* Y, int64_t ldy);
+
+/* Parameters of the randomized SVD; names as the LightNE flags
+ * (LightNE/LightNE.cc:34-50). */
+typedef struct lne_randsvd_params {
+  int64_t rank;                 /* -rank: sketch width r (oversampled) */
+  int64_t dim;                  /* -dim: embedding dimension d <= r */
+  int32_t normalize;            /* -normalize: L2-normalise embedding rows */
+  int32_t precision;            /* LNE_PREC_FP32 or LNE_PREC_BF16 (SpMM dense operand) */
+  uint64_t seed;                /* Gaussian sketch seed (the reference's VSL seed is 777) */
+  int32_t random_project_only;  /* -random_project_only: return (A * Omega)[:, :dim] */
+  int32_t reserved;
+} lne_randsvd_params;
+
+typedef struct lne_randsvd_stats {
+  float ms_sketch, ms_qr, ms_spmm2, ms_core, ms_total; /* device time per stage */
+  int32_t jacobi_sweeps;
+  int32_t kernel_launches;
+  double spmm_nnz;
+} lne_randsvd_stats;
+
+/*
+ * Randomized SVD of A (n x n CSR, general) and the embedding
+ * emb = U[:, :dim] * sqrt(S[:dim]) (R1-R7).  d_emb: device n x dim FP32,
+ * row-major.  h_S: host float[rank] singular values of the r x r core
+ * (descending), may be NULL.  stats may be NULL.  Replaces
+ * MKLRedSVD(...).run() + compute_u_sigma_root
+ * (LightNE/mklredsvd/mklredsvd.cc:54-403, LightNE/PathEmbed.h:371-408).
+ */
+int lne_randsvd(lne_ctx* ctx, const lne_csr* A, const lne_randsvd_params* p, float* d_emb, float* h_S,
+                lne_randsvd_stats* stats);
+
+/*
+ * The Gaussian sketch generator lne_randsvd uses: rows x cols N(0,1) values
+ * of stream stream_id (0: Omega, 1: P) into device memory with leading
+ * dimension ld.  Exposed so that a checker can rebuild the same sketches
+ * (the reference's VSL SFMT19937 stream, mklredsvd.cc:141, has no
+ * counterpart without MKL).
+ */
+int lne_gaussian(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols, float* d_out,
+                 int64_t ld);
+
+/* Parameters of the spectral propagation (chebyshev_expansion). */
+typedef struct lne_propagate_params {
+  int64_t dim;        /* columns of the embedding (rank == dim in LightNE.cc:114) */
+  int32_t order;      /* -order: number of Chebyshev terms K */
+  int32_t precision;  /* LNE_PREC_FP32 or LNE_PREC_BF16 (SpMM dense operand) */
+  double mu;          /* 0.2 in LightNE.cc:114 (narrowed to float, as the reference) */
+  double s;           /* 0.5 in LightNE.cc:114 (Bessel argument, narrowed to float) */
+} lne_propagate_params;
+
+typedef struct lne_propagate_stats {
+  float ms_total;
+  int32_t kernel_launches;
+  int32_t spmm_calls;
+} lne_propagate_stats;
+
+/*
+ * Spectral propagation (P1, P2, P4): y = (A + I)(a - sum_k c_k T_k(X) a)
+ * with X = M^2/2 - I, M = I - D~^-1 (A + I) - mu I, c_k the Bessel weights.
+ * d_a (input) and d_y (output): device n x dim FP32, row-major; y must not
+ * alias a.  d_a_out (optional, may be NULL) receives a - conv, the value the
+ * reference leaves in its mutated argument.  Replaces
+ * spectral_propagation::chebyshev_expansion up to the (A+I)a product
+ * (LightNE/SpectralPropagation.h:45-221).
+ */
+int lne_propagate(lne_ctx* ctx, const lne_graph* g, const lne_propagate_params* p, const float* d_a, float* d_y,
+                  float* d_a_out, lne_propagate_stats* stats);
+
+/* The Chebyshev/Bessel weights c_0..c_{max(order,2)-1} as float, computed
+ * in extended precision and narrowed as the reference's axpy calls do
+ * (SpectralPropagation.h:129-197). */
+int lne_chebyshev_coefficients(int32_t order, double s, float* out);
+
+/*
+ * Dense embedding (P5): SVD of x (device n x dim FP32) and
+ * emb = U * sqrt(S) with rows L2-normalised (norm > 1e-5), as
+ * spectral_propagation::get_embedding_dense (LightNE/SpectralPropagation.h:16-43).
+ * h_S (host float[dim]) may be NULL.
+ */
+int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_t dim, float* d_emb, float* h_S);
 
 /* CSR accessors. */
 int lne_csr_info(const lne_csr* c, int64_t* n, int64_t* nnz);

@@ -76,6 +76,55 @@ class SparsifyStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class RandsvdParams(ctypes.Structure):
+    _fields_ = [
+        ("rank", ctypes.c_int64),
+        ("dim", ctypes.c_int64),
+        ("normalize", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+        ("random_project_only", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class RandsvdStats(ctypes.Structure):
+    _fields_ = [
+        ("ms_sketch", ctypes.c_float),
+        ("ms_qr", ctypes.c_float),
+        ("ms_spmm2", ctypes.c_float),
+        ("ms_core", ctypes.c_float),
+        ("ms_total", ctypes.c_float),
+        ("jacobi_sweeps", ctypes.c_int32),
+        ("kernel_launches", ctypes.c_int32),
+        ("spmm_nnz", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PropagateParams(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int64),
+        ("order", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("mu", ctypes.c_double),
+        ("s", ctypes.c_double),
+    ]
+
+
+class PropagateStats(ctypes.Structure):
+    _fields_ = [
+        ("ms_total", ctypes.c_float),
+        ("kernel_launches", ctypes.c_int32),
+        ("spmm_calls", ctypes.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 VP = ctypes.c_void_p
 I64 = ctypes.c_int64
 I32 = ctypes.c_int32
@@ -94,6 +143,12 @@ SIGNATURES = {
     "lne_sparsify": (ctypes.c_int, [VP, VP, ctypes.POINTER(SparsifyParams), PVP, ctypes.POINTER(SparsifyStats)]),
     "lne_trunc_log_values": (ctypes.c_int, [VP, VP, I64, VP]),
     "lne_spmm": (ctypes.c_int, [VP, VP, ctypes.c_int, VP, I64, I64, ctypes.c_float, ctypes.c_float, VP, I64]),
+    "lne_randsvd": (ctypes.c_int, [VP, VP, ctypes.POINTER(RandsvdParams), VP, VP, ctypes.POINTER(RandsvdStats)]),
+    "lne_gaussian": (ctypes.c_int, [VP, ctypes.c_uint64, ctypes.c_uint64, I64, I64, VP, I64]),
+    "lne_propagate": (ctypes.c_int, [VP, VP, ctypes.POINTER(PropagateParams), VP, VP, VP,
+                                     ctypes.POINTER(PropagateStats)]),
+    "lne_chebyshev_coefficients": (ctypes.c_int, [ctypes.c_int32, ctypes.c_double, VP]),
+    "lne_dense_embed": (ctypes.c_int, [VP, VP, I64, I64, VP, VP]),
     "lne_csr_info": (ctypes.c_int, [VP, ctypes.POINTER(I64), ctypes.POINTER(I64)]),
     "lne_csr_download": (ctypes.c_int, [VP, VP, VP, VP, VP]),
     "lne_csr_device_ptrs": (ctypes.c_int, [VP, PVP, PVP, PVP]),

@@ -12,9 +12,13 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import LneError, SparsifyParams, SparsifyStats, check
+from ._lib import (LNE_PREC_BF16, LNE_PREC_FP32, LneError, PropagateParams, PropagateStats, RandsvdParams,
+                   RandsvdStats, SparsifyParams, SparsifyStats, check)
 
-__all__ = ["Context", "Graph", "CSR", "generate_trunc_log_matrix_v2", "LneError"]
+__all__ = ["Context", "Graph", "CSR", "generate_trunc_log_matrix_v2", "randsvd",
+           "chebyshev_expansion", "get_embedding_dense", "gaussian", "chebyshev_coefficients", "LneError"]
+
+PRECISIONS = {"fp32": LNE_PREC_FP32, "bf16": LNE_PREC_BF16}
 
 
 def _ptr(a: np.ndarray) -> ctypes.c_void_p:
@@ -22,10 +26,15 @@ def _ptr(a: np.ndarray) -> ctypes.c_void_p:
 
 
 class Context:
-    """Device + stream.  ``stream`` is a raw cudaStream_t (int) or None."""
+    """Device + stream.  ``stream`` is a raw cudaStream_t (int); by default
+    the context runs on torch's current stream of ``device``, so library work
+    and torch tensor operations are ordered on one stream."""
 
     def __init__(self, device: int = 0, stream: int | None = None):
         L = _lib.load()
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream(device).cuda_stream
         h = ctypes.c_void_p()
         check(L.lne_ctx_create(ctypes.byref(h), device, ctypes.c_void_p(stream or 0)))
         self.handle = h
@@ -149,3 +158,76 @@ def generate_trunc_log_matrix_v2(ctx: Context, graph: Graph, seed: int, walk_len
     h = ctypes.c_void_p()
     check(_lib.load().lne_sparsify(ctx.handle, graph.handle, ctypes.byref(p), ctypes.byref(h), ctypes.byref(st)))
     return CSR(ctx, h), st.as_dict()
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _as_device_f32(x, device):
+    torch = _torch()
+    if isinstance(x, np.ndarray):
+        return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(f"cuda:{device}")
+    return x.to(device=f"cuda:{device}", dtype=torch.float32).contiguous()
+
+
+def gaussian(ctx: Context, seed: int, stream_id: int, rows: int, cols: int):
+    """The device Gaussian sketch (stream 0: Omega, 1: P) as a torch tensor."""
+    torch = _torch()
+    out = torch.empty(rows, cols, dtype=torch.float32, device=f"cuda:{ctx.device}")
+    check(_lib.load().lne_gaussian(ctx.handle, seed, stream_id, rows, cols, ctypes.c_void_p(out.data_ptr()), cols))
+    ctx.synchronize()
+    return out
+
+
+def randsvd(ctx: Context, A: CSR, rank: int, dim: int, normalize: bool = False, precision: str = "fp32",
+            seed: int = 777, random_project_only: bool = False):
+    """MKLRedSVD(...).run() + compute_u_sigma_root on the device
+    (LightNE/mklredsvd/mklredsvd.cc:93-403, LightNE/PathEmbed.h:371-408).
+    Returns (emb torch n x dim, S numpy[rank], stats)."""
+    torch = _torch()
+    emb = torch.empty(A.n, dim, dtype=torch.float32, device=f"cuda:{ctx.device}")
+    S = np.zeros(rank, dtype=np.float32)
+    p = RandsvdParams(rank=rank, dim=dim, normalize=int(bool(normalize)), precision=PRECISIONS[precision],
+                      seed=seed, random_project_only=int(bool(random_project_only)))
+    st = RandsvdStats()
+    check(_lib.load().lne_randsvd(ctx.handle, A.handle, ctypes.byref(p), ctypes.c_void_p(emb.data_ptr()),
+                                  _ptr(S), ctypes.byref(st)))
+    return emb, S, st.as_dict()
+
+
+def chebyshev_expansion(ctx: Context, graph: Graph, a, dim: int, order: int = 10, mu: float = 0.2,
+                        s: float = 0.5, precision: str = "fp32", return_a: bool = False):
+    """spectral_propagation::chebyshev_expansion up to (A+I)a
+    (LightNE/SpectralPropagation.h:45-221).  ``a`` is n x dim (numpy or
+    torch); returns y (torch), and a - conv when ``return_a``."""
+    torch = _torch()
+    da = _as_device_f32(a, ctx.device)
+    y = torch.empty_like(da)
+    a_out = torch.empty_like(da) if return_a else None
+    p = PropagateParams(dim=dim, order=order, precision=PRECISIONS[precision], mu=mu, s=s)
+    st = PropagateStats()
+    check(_lib.load().lne_propagate(ctx.handle, graph.handle, ctypes.byref(p), ctypes.c_void_p(da.data_ptr()),
+                                    ctypes.c_void_p(y.data_ptr()),
+                                    ctypes.c_void_p(a_out.data_ptr() if return_a else 0), ctypes.byref(st)))
+    return (y, a_out, st.as_dict()) if return_a else (y, st.as_dict())
+
+
+def get_embedding_dense(ctx: Context, x, dim: int):
+    """SVD of x (n x dim) -> U sqrt(S), rows normalised
+    (LightNE/SpectralPropagation.h:16-43).  Returns (emb torch, S numpy)."""
+    torch = _torch()
+    dx = _as_device_f32(x, ctx.device)
+    n = dx.shape[0]
+    emb = torch.empty(n, dim, dtype=torch.float32, device=f"cuda:{ctx.device}")
+    S = np.zeros(dim, dtype=np.float32)
+    check(_lib.load().lne_dense_embed(ctx.handle, ctypes.c_void_p(dx.data_ptr()), n, dim,
+                                      ctypes.c_void_p(emb.data_ptr()), _ptr(S)))
+    return emb, S
+
+
+def chebyshev_coefficients(order: int, s: float = 0.5) -> np.ndarray:
+    out = np.zeros(max(order, 2), dtype=np.float32)
+    check(_lib.load().lne_chebyshev_coefficients(order, s, _ptr(out)))
+    return out

@@ -192,17 +192,9 @@ int lne_ctx_create(lne_ctx** out, int device, void* stream) {
   LNE_CUDA_TRY(cudaSetDevice(device));
   lne_ctx* c = new lne_ctx();
   c->device = device;
-  if (stream) {
-    c->stream = (cudaStream_t)stream;
-  } else {
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) {
-      delete c;
-      set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
-      return LNE_ERR_CUDA;
-    }
-    c->own_stream = true;
-  }
+  // all work is ordered on the caller's stream (NULL: the default stream)
+  c->stream = (cudaStream_t)stream;
+  c->own_stream = false;
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   int optin = 0;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);

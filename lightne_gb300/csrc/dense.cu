@@ -1,0 +1,440 @@
+// Dense kernels of the randomized SVD (mklredsvd.cc:93-403 replaced by
+// CholeskyQR and a one-sided Jacobi core SVD) and of the dense embedding.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <string>
+
+#include "dense.h"
+#include "dense_common.cuh"
+#include "lne_math.cuh"
+
+namespace lne {
+
+// ---------------------------------------------------------------------------
+// Gaussian sketch
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gaussian_at(uint64_t base, uint64_t idx) {
+  const uint64_t x1 = hash64_2(base + 2 * idx), x2 = hash64_2(base + 2 * idx + 1);
+  const float u1 = (float)((x1 >> 40) + 1) * 5.9604644775390625e-08f;  // (0, 1]
+  const float u2 = (float)(x2 >> 40) * 5.9604644775390625e-08f;        // [0, 1)
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  return sqrtf(-2.0f * logf(u1)) * c;
+}
+
+template <typename T>
+__global__ void k_gaussian(uint64_t base, int64_t rows, int64_t cols, T* __restrict__ out, int64_t ld) {
+  const int64_t total = rows * ld;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / ld, j = t - i * ld;
+    const float z = j < cols ? gaussian_at(base, (uint64_t)(i * cols + j)) : 0.0f;
+    out[t] = (T)z;
+  }
+}
+
+static uint64_t gaussian_base(uint64_t seed, uint64_t stream_id) {
+  return hash64_2(seed ^ hash64_2(stream_id + 0x9E3779B97F4A7C15ULL));
+}
+
+static unsigned grid1d(int64_t items, int threads, int64_t cap) {
+  int64_t b = (items + threads - 1) / threads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, cap));
+}
+
+int gaussian_fill_f32(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols, float* out,
+                      int64_t ld) {
+  k_gaussian<float><<<grid1d(rows * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
+      gaussian_base(seed, stream_id), rows, cols, out, ld);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+int gaussian_fill_bf16(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
+                       __nv_bfloat16* out, int64_t ld) {
+  k_gaussian<__nv_bfloat16><<<grid1d(rows * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
+      gaussian_base(seed, stream_id), rows, cols, out, ld);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Gram: partial[b] = A_b^T B_b over row blocks of kGramRows, 64 x 64 output
+// tiles, 256 threads with 4 x 4 outputs each; then a fixed-order FP64 sum.
+// ---------------------------------------------------------------------------
+static constexpr int kGramRows = 2048;
+
+__global__ void __launch_bounds__(256) k_gram_partial(const float* __restrict__ A, int64_t lda, int c1,
+                                                      const float* __restrict__ B, int64_t ldb, int c2, int64_t n,
+                                                      float* __restrict__ partial, int tiles_j) {
+  __shared__ __align__(16) float As[32][64];
+  __shared__ __align__(16) float Bs[32][64];
+  const int ti = blockIdx.x / tiles_j, tj = blockIdx.x % tiles_j;
+  const int64_t rb = blockIdx.y;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t r0 = rb * kGramRows;
+  const int64_t r1 = std::min<int64_t>(n, r0 + kGramRows);
+  float acc[4][4] = {};
+  for (int64_t k0 = r0; k0 < r1; k0 += 32) {
+    for (int idx = tid; idx < 32 * 64; idx += 256) {
+      const int rr = idx >> 6, cc = idx & 63;
+      const int64_t row = k0 + rr;
+      const int ca = ti * 64 + cc, cb = tj * 64 + cc;
+      As[rr][cc] = (row < r1 && ca < c1) ? A[row * lda + ca] : 0.f;
+      Bs[rr][cc] = (row < r1 && cb < c2) ? B[row * ldb + cb] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      const float4 a = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+      const float4 b = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(av[p], bv[q], acc[p][q]);
+    }
+    __syncthreads();
+  }
+  float* out = partial + rb * (int64_t)c1 * c2;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int i = ti * 64 + ty * 4 + p;
+    if (i >= c1) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = tj * 64 + tx * 4 + q;
+      if (j < c2) out[(int64_t)i * c2 + j] = acc[p][q];
+    }
+  }
+}
+
+__global__ void k_gram_reduce(const float* __restrict__ partial, int64_t nb, int64_t cnt, double* __restrict__ G) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  double s = 0.0;
+  for (int64_t b = 0; b < nb; ++b) s += (double)partial[b * cnt + t];
+  G[t] = s;
+}
+
+int gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+         double* G) {
+  const int64_t nb = std::max<int64_t>(1, (n + kGramRows - 1) / kGramRows);
+  const int tiles_i = (c1 + 63) / 64, tiles_j = (c2 + 63) / 64;
+  float* partial = nullptr;
+  int rc = dalloc(ctx, (void**)&partial, sizeof(float) * nb * c1 * c2, "gram partials");
+  if (rc) return rc;
+  dim3 grid((unsigned)(tiles_i * tiles_j), (unsigned)nb);
+  k_gram_partial<<<grid, 256, 0, ctx->stream>>>(A, lda, c1, B, ldb, c2, n, partial, tiles_j);
+  const int64_t cnt = (int64_t)c1 * c2;
+  k_gram_reduce<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, cnt, G);
+  dfree(ctx, partial);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Tall GEMM: Out = In * W, 128 x 64 output tiles, 256 threads, 8 x 4 each.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gemm_tall(const float* __restrict__ In, int64_t ldi, int k,
+                                                   const float* __restrict__ W, int c2, int64_t n,
+                                                   float* __restrict__ Out, int64_t ldo,
+                                                   __nv_bfloat16* __restrict__ OutB) {
+  __shared__ __align__(16) float As[16][128 + 4];
+  __shared__ __align__(16) float Ws[16][64];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t row0 = (int64_t)blockIdx.x * 128;
+  const int col0 = blockIdx.y * 64;
+  float acc[8][4] = {};
+  for (int k0 = 0; k0 < k; k0 += 16) {
+    for (int idx = tid; idx < 128 * 16; idx += 256) {
+      const int rr = idx >> 4, kk = idx & 15;
+      const int64_t row = row0 + rr;
+      As[kk][rr] = (row < n && k0 + kk < k) ? In[row * ldi + k0 + kk] : 0.f;
+    }
+    for (int idx = tid; idx < 16 * 64; idx += 256) {
+      const int kk = idx >> 6, cc = idx & 63;
+      Ws[kk][cc] = (k0 + kk < k && col0 + cc < c2) ? W[(int64_t)(k0 + kk) * c2 + col0 + cc] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 8]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][ty * 8 + 4]);
+      const float4 b = *reinterpret_cast<const float4*>(&Ws[kk][tx * 4]);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int p = 0; p < 8; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(av[p], bv[q], acc[p][q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const int64_t row = row0 + ty * 8 + p;
+    if (row >= n) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = col0 + tx * 4 + q;
+      if (c < ldo) {
+        const float v = c < c2 ? acc[p][q] : 0.f;
+        Out[row * ldo + c] = v;
+        if (OutB) OutB[row * ldo + c] = __float2bfloat16_rn(v);
+      }
+    }
+  }
+}
+
+int gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
+              int64_t ldo, __nv_bfloat16* OutB) {
+  if (n <= 0) return LNE_OK;
+  dim3 grid((unsigned)((n + 127) / 128), (unsigned)((ldo + 63) / 64));
+  k_gemm_tall<<<grid, 256, 0, ctx->stream>>>(In, ldi, k, W, c2, n, Out, ldo, OutB);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 Cholesky (right-looking, one block) and W = L^-T in FP32.
+// ---------------------------------------------------------------------------
+__global__ void k_cholesky(double* __restrict__ G, int r, double shift, int* __restrict__ status) {
+  __shared__ double dk;
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  for (int i = threadIdx.x; i < r; i += blockDim.x) G[(int64_t)i * r + i] += shift;
+  __syncthreads();
+  for (int k = 0; k < r; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = G[(int64_t)k * r + k];
+      if (!(d > 0.0) || !isfinite(d)) {
+        bad = 1;
+        dk = 1.0;
+      } else {
+        dk = sqrt(d);
+      }
+      G[(int64_t)k * r + k] = dk;
+    }
+    __syncthreads();
+    if (bad) break;
+    const double piv = dk;
+    for (int i = k + 1 + threadIdx.x; i < r; i += blockDim.x) G[(int64_t)i * r + k] /= piv;
+    __syncthreads();
+    const int m = r - k - 1;
+    for (int64_t t = threadIdx.x; t < (int64_t)m * m; t += blockDim.x) {
+      const int i = k + 1 + (int)(t / m), j = k + 1 + (int)(t % m);
+      if (j <= i) G[(int64_t)i * r + j] -= G[(int64_t)i * r + k] * G[(int64_t)j * r + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *status = bad;
+}
+
+// X = L^-1 by forward substitution, one column per thread; W[i][j] = X[j][i].
+__global__ void k_tri_inv_t(const double* __restrict__ L, int r, float* __restrict__ W, double* __restrict__ X) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= r) return;
+  for (int i = 0; i < r; ++i) {
+    double x;
+    if (i < j) {
+      x = 0.0;
+    } else if (i == j) {
+      x = 1.0 / L[(int64_t)j * r + j];
+    } else {
+      double s = 0.0;
+      for (int k = j; k < i; ++k) s += L[(int64_t)i * r + k] * X[(int64_t)k * r + j];
+      x = -s / L[(int64_t)i * r + i];
+    }
+    X[(int64_t)i * r + j] = x;
+    W[(int64_t)j * r + i] = (float)x;
+  }
+}
+
+int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W) {
+  double* X = nullptr;
+  int* status = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, (void**)&X, sizeof(double) * r * r + 16, "triangular inverse"))) return rc;
+  status = (int*)(X + (int64_t)r * r);
+  k_cholesky<<<1, 1024, 0, ctx->stream>>>(G, r, shift, status);
+  k_tri_inv_t<<<(r + 127) / 128, 128, 0, ctx->stream>>>(G, r, W, X);
+  int h = 0;
+  LNE_CUDA_TRY(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, X);
+  LNE_CUDA_TRY(cudaGetLastError());
+  if (h) {
+    set_error("Cholesky of the Gram matrix failed (matrix not numerically positive definite)");
+    return LNE_ERR_NUMERIC;
+  }
+  return LNE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// One-sided Jacobi SVD (Hestenes), FP64, one block.  Columns of the working
+// copy Wc (column-major) are rotated pairwise in round-robin order until
+// every pair is orthogonal to 1e-15 relative; singular values are the column
+// norms, left singular vectors the normalised columns.
+// ---------------------------------------------------------------------------
+__global__ void k_jacobi(const double* __restrict__ C, int r, double* __restrict__ Wc, double* __restrict__ U,
+                         double* __restrict__ S, int* __restrict__ sweeps_out, int max_sweeps) {
+  __shared__ int rotated;
+  __shared__ int order[1024];
+  __shared__ double norms[1024];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t t = threadIdx.x; t < (int64_t)r * r; t += blockDim.x) {
+    const int i = (int)(t / r), j = (int)(t % r);
+    Wc[(int64_t)j * r + i] = C[t];
+  }
+  __syncthreads();
+  const int rp = (r + 1) & ~1;  // even number of players (index r is a dummy when r is odd)
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) rotated = 0;
+    __syncthreads();
+    for (int s = 0; s < rp - 1; ++s) {
+      for (int pk = warp; pk < rp / 2; pk += nw) {
+        int p, q;
+        if (pk == 0) {
+          p = rp - 1;
+          q = s;
+        } else {
+          p = (s + pk) % (rp - 1);
+          q = (s - pk + rp - 1) % (rp - 1);
+        }
+        if (p >= r || q >= r) continue;
+        if (p > q) { const int t = p; p = q; q = t; }
+        double* wp = Wc + (int64_t)p * r;
+        double* wq = Wc + (int64_t)q * r;
+        double a = 0.0, b = 0.0, g = 0.0;
+        for (int i = lane; i < r; i += 32) {
+          const double x = wp[i], y = wq[i];
+          a = fma(x, x, a);
+          b = fma(y, y, b);
+          g = fma(x, y, g);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          a += __shfl_xor_sync(0xffffffffu, a, o);
+          b += __shfl_xor_sync(0xffffffffu, b, o);
+          g += __shfl_xor_sync(0xffffffffu, g, o);
+        }
+        if (fabs(g) > 1e-15 * sqrt(a * b) && g != 0.0) {
+          const double zeta = (b - a) / (2.0 * g);
+          const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+          for (int i = lane; i < r; i += 32) {
+            const double x = wp[i], y = wq[i];
+            wp[i] = c * x - sn * y;
+            wq[i] = sn * x + c * y;
+          }
+          if (lane == 0) rotated = 1;
+        }
+      }
+      __syncthreads();
+    }
+    if (!rotated) break;
+    __syncthreads();
+  }
+  // norms and descending order
+  for (int j = threadIdx.x; j < r; j += blockDim.x) {
+    double s2 = 0.0;
+    for (int i = 0; i < r; ++i) s2 = fma(Wc[(int64_t)j * r + i], Wc[(int64_t)j * r + i], s2);
+    norms[j] = sqrt(s2);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < r; j += blockDim.x) {
+    int rank = 0;
+    for (int k = 0; k < r; ++k) rank += (norms[k] > norms[j]) || (norms[k] == norms[j] && k < j);
+    order[rank] = j;
+  }
+  __syncthreads();
+  for (int64_t t = threadIdx.x; t < (int64_t)r * r; t += blockDim.x) {
+    const int i = (int)(t / r), jn = (int)(t % r);
+    const int j = order[jn];
+    const double nrm = norms[j];
+    U[t] = nrm > 0.0 ? Wc[(int64_t)j * r + i] / nrm : 0.0;
+  }
+  for (int jn = threadIdx.x; jn < r; jn += blockDim.x) S[jn] = norms[order[jn]];
+  if (threadIdx.x == 0) *sweeps_out = sweep + 1;
+}
+
+int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out) {
+  if (r > 1024) {
+    set_error("jacobi_svd: rank above 1024 is not supported");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  double* Wc = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, (void**)&Wc, sizeof(double) * r * r + 16, "jacobi work"))) return rc;
+  int* d_sw = (int*)(Wc + (int64_t)r * r);
+  k_jacobi<<<1, 1024, 0, ctx->stream>>>(C, r, Wc, U, S, d_sw, 60);
+  int h = 0;
+  LNE_CUDA_TRY(cudaMemcpyAsync(&h, d_sw, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, Wc);
+  LNE_CUDA_TRY(cudaGetLastError());
+  if (sweeps_out) *sweeps_out = h;
+  return LNE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------
+__global__ void k_to_bf16(const float* __restrict__ X, int64_t total, __nv_bfloat16* __restrict__ Y) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+    Y[t] = __float2bfloat16_rn(X[t]);
+}
+
+int to_bf16(lne_ctx* ctx, const float* X, int64_t n, int64_t ld, __nv_bfloat16* Y) {
+  k_to_bf16<<<grid1d(n * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(X, n * ld, Y);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+// One warp per row: norm in FP32 (as cblas_snrm2 on FP32 data), scale by
+// 1/norm when norm > eps.
+__global__ void k_normalize_rows(float* __restrict__ X, int64_t n, int d, int64_t ld, float eps) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    float* x = X + r * ld;
+    float s = 0.f;
+    for (int j = lane; j < d; j += 32) s = fmaf(x[j], x[j], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const float nrm = sqrtf(s);
+    if (nrm > eps) {
+      const float inv = (float)(1.0 / (double)nrm);
+      for (int j = lane; j < d; j += 32) x[j] *= inv;
+    }
+  }
+}
+
+int normalize_rows(lne_ctx* ctx, float* X, int64_t n, int d, int64_t ld, float eps) {
+  k_normalize_rows<<<grid1d(n * 32, 256, (int64_t)ctx->num_sms * 16), 256, 0, ctx->stream>>>(X, n, d, ld, eps);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+__global__ void k_trace(const double* G, int r, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < r; ++i) s += G[(int64_t)i * r + i];
+    *out = s;
+  }
+}
+
+int trace_host(lne_ctx* ctx, const double* G, int r, double* out) {
+  double* d = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, (void**)&d, sizeof(double), "trace"))) return rc;
+  k_trace<<<1, 32, 0, ctx->stream>>>(G, r, d);
+  LNE_CUDA_TRY(cudaMemcpyAsync(out, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, d);
+  return LNE_OK;
+}
+
+}  // namespace lne

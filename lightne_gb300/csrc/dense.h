@@ -1,0 +1,53 @@
+// Dense building blocks of the randomized SVD and of the dense embedding
+// (host-side launchers; all work on ctx->stream).
+//
+// Tall matrices are row-major n x ld (ld = pad_ld(cols), 16-byte rows,
+// padding columns kept at zero).  Small r x r matrices are row-major FP64.
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "lne_internal.h"
+
+namespace lne {
+
+// N(0,1) entries from a counter-based generator: entry (i, j) of stream
+// `stream_id` is a Box-Muller transform of two 53-bit uniforms hashed from
+// (seed, stream_id, i, j).  Independent of the launch shape.
+int gaussian_fill_f32(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols, float* out,
+                      int64_t ld);
+int gaussian_fill_bf16(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
+                       __nv_bfloat16* out, int64_t ld);
+
+// G (c1 x c2, FP64, row-major, ldg = c2) = A^T B for A (n x c1, lda),
+// B (n x c2, ldb).  FP32 products summed per 2048-row block, blocks summed
+// in FP64 in block order (reproducible).
+int gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+         double* G);
+
+// Out (n x c2, ldo) = In (n x k, ldi) * W (k x c2, FP32 row-major, ldw = c2).
+// Optional BF16 copy of Out (ldb = ldo).  Columns c2..ldo-1 of Out are zeroed.
+int gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
+              int64_t ldo, __nv_bfloat16* OutB);
+
+// Cholesky G + shift*I = L L^T (FP64, in place on a device r x r buffer) and
+// W = L^-T as FP32 (r x r row-major, upper triangular).  Returns
+// LNE_ERR_NUMERIC when a pivot is not positive.
+int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W);
+
+// One-sided Jacobi SVD of C (r x r, FP64 row-major, device; overwritten):
+// U (r x r FP64, columns = left singular vectors, sorted by singular value,
+// descending), S (r, FP64).
+int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out);
+
+// Copies an FP32 tall matrix into a BF16 copy (same ld).
+int to_bf16(lne_ctx* ctx, const float* X, int64_t n, int64_t ld, __nv_bfloat16* Y);
+
+// Row-wise L2 normalisation of an n x d FP32 matrix (rows with norm <= eps
+// are left unchanged), as PathEmbed.h:390-405.
+int normalize_rows(lne_ctx* ctx, float* X, int64_t n, int d, int64_t ld, float eps);
+
+// Trace of a device FP64 r x r matrix, read back to the host (synchronises).
+int trace_host(lne_ctx* ctx, const double* G, int r, double* out);
+
+}  // namespace lne

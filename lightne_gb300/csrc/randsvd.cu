@@ -1,0 +1,302 @@
+// Randomized SVD of the sparsifier matrix and the U * sqrt(Sigma) embedding.
+//
+// Reference: mkl_redsvd::MKLRedSVD<FP>::run (LightNE/mklredsvd/mklredsvd.cc:93-403)
+// and path_embed::compute_u_sigma_root (LightNE/PathEmbed.h:371-408):
+//   Y = A * Omega, Q = qr(Y), B = A * Q, Z = qr(B * P), C = Z^T B,
+//   C = U_C S V^T, matU = Z * U_C, emb[:, j] = sqrt(S_j) * matU[:, j], j < dim.
+// Orthonormalisation is CholeskyQR (a shifted pass, then two plain passes)
+// instead of Householder geqrf+orgqr; R has a positive diagonal, so Q is the
+// unique thin-QR factor with that sign convention.  The core SVD is a
+// one-sided FP64 Jacobi.  The Gaussian sketches come from a counter-based
+// generator (MKL's SFMT19937 stream cannot be reproduced without MKL).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "dense.h"
+#include "dense_common.cuh"
+#include "lne_internal.h"
+#include "spmm_core.cuh"
+#include "spmm_dispatch.cuh"
+
+namespace lne {
+
+namespace {
+
+struct Buf {
+  lne_ctx* ctx;
+  std::vector<void*> ptrs;
+  explicit Buf(lne_ctx* c) : ctx(c) {}
+  template <typename T>
+  int get(T** out, size_t count, const char* what) {
+    void* p = nullptr;
+    int rc = dalloc(ctx, &p, sizeof(T) * (count > 0 ? count : 1), what);
+    if (rc == LNE_OK) ptrs.push_back(p);
+    *out = (T*)p;
+    return rc;
+  }
+  ~Buf() {
+    for (void* p : ptrs) dfree(ctx, p);
+  }
+};
+
+// Y = A * X with FP32 output (overwrites Y), X FP32 or BF16.
+struct EpiStore {
+  float* __restrict__ Y;
+  int64_t ldy;
+  int d;
+  template <int N>
+  __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&a)[N]) const {
+    float* y = Y + r * ldy + e0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (e0 + i < d) y[i] = a[i];
+  }
+};
+
+__global__ void k_scale_cols(const double* __restrict__ U, const double* __restrict__ S, int r, int dim,
+                             float* __restrict__ W) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= r * dim) return;
+  const int i = t / dim, j = t % dim;
+  // compute_u_sigma_root takes sqrt of the float singular value
+  W[t] = (float)U[(int64_t)i * r + j] * sqrtf((float)S[j]);
+}
+
+__global__ void k_copy_cols(const float* __restrict__ X, int64_t ldx, int64_t n, int dim, float* __restrict__ E) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n * dim; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / dim;
+    const int j = (int)(t - i * dim);
+    E[t] = X[i * ldx + j];
+  }
+}
+
+}  // namespace
+
+// In-place CholeskyQR on X (n x ld FP32, r columns) using tmp as the ping-pong
+// partner; the result ends in X.  Xb (optional) receives a BF16 copy.
+static int cholqr3(lne_ctx* ctx, float* X, float* tmp, int64_t n, int64_t ld, int r, __nv_bfloat16* Xb,
+                   int* launches) {
+  Buf B(ctx);
+  double* G = nullptr;
+  float* W = nullptr;
+  int rc;
+  if ((rc = B.get(&G, (size_t)r * r, "gram")) || (rc = B.get(&W, (size_t)r * r, "R^-1"))) return rc;
+  float* src = X;
+  float* dst = tmp;
+  const double u32 = 5.9604644775390625e-08;
+  for (int pass = 0; pass < 3; ++pass) {
+    double shift = 0.0;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+      if ((rc = gram(ctx, src, ld, r, src, ld, r, n, G))) return rc;
+      *launches += 2;
+      if (pass == 0 || attempt > 0) {
+        double tr = 0.0;
+        if ((rc = trace_host(ctx, G, r, &tr))) return rc;
+        *launches += 1;
+        shift = (pass == 0 && attempt == 0 ? 64.0 : 64.0 * pow(10.0, attempt)) * u32 * tr;
+      }
+      rc = cholesky_inv(ctx, G, r, shift, W);
+      *launches += 2;
+      if (rc == LNE_OK) break;
+      if (rc != LNE_ERR_NUMERIC || attempt == 5) return rc;
+    }
+    const bool last = pass == 2;
+    if ((rc = gemm_tall(ctx, src, ld, r, W, r, n, dst, ld, last ? Xb : nullptr))) return rc;
+    *launches += 1;
+    float* t = src;
+    src = dst;
+    dst = t;
+  }
+  // three passes: the result is in tmp; move it to X
+  LNE_CUDA_TRY(cudaMemcpyAsync(X, src, sizeof(float) * n * ld, cudaMemcpyDeviceToDevice, ctx->stream));
+  return LNE_OK;
+}
+
+template <typename XT>
+static int spmm_store(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ld, int d, float* Y, int* launches) {
+  CsrRows R{A->row_ptr, A->col, A->val};
+  EpiStore epi{Y, ld, d};
+  return spmm_run<XT>(ctx, R, A->plan, X, ld, d, epi, launches);
+}
+
+}  // namespace lne
+
+using namespace lne;
+
+extern "C" int lne_gaussian(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
+                            float* d_out, int64_t ld) {
+  LNE_CHECK_ARG(ctx && d_out && rows >= 0 && cols >= 0 && ld >= cols, "lne_gaussian: bad argument");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  return gaussian_fill_f32(ctx, seed, stream_id, rows, cols, d_out, ld);
+}
+
+extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_params* p, float* d_emb,
+                           float* h_S, lne_randsvd_stats* stats) {
+  LNE_CHECK_ARG(ctx && Acsr && p && d_emb, "lne_randsvd: NULL argument");
+  LNE_CHECK_ARG(p->rank >= 1 && p->dim >= 1 && p->dim <= p->rank, "lne_randsvd: need 1 <= dim <= rank");
+  LNE_CHECK_ARG(p->rank <= Acsr->n, "lne_randsvd: rank above n");
+  LNE_CHECK_ARG(p->precision == LNE_PREC_FP32 || p->precision == LNE_PREC_BF16, "lne_randsvd: bad precision");
+  if (p->rank > 1024) {
+    set_error("lne_randsvd: rank above 1024 is not supported by the one-block Jacobi core");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  lne_csr* A = const_cast<lne_csr*>(Acsr);
+  const int64_t n = A->n;
+  const int r = (int)p->rank, dim = (int)p->dim;
+  const int64_t ld = pad_ld(r);
+  const bool bf16 = p->precision == LNE_PREC_BF16;
+  cudaStream_t st = ctx->stream;
+  int launches = 0;
+  int rc = build_plan_csr(ctx, A);
+  if (rc) return rc;
+
+  cudaEvent_t ev[6];
+  for (auto& e : ev) cudaEventCreate(&e);
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() { for (int i = 0; i < 6; ++i) cudaEventDestroy(e[i]); }
+  } evg{ev};
+
+  Buf B(ctx);
+  float *Y = nullptr, *T = nullptr, *Bm = nullptr, *P = nullptr, *Wf = nullptr;
+  __nv_bfloat16* Xb = nullptr;
+  double *C = nullptr, *U = nullptr, *S = nullptr;
+  if ((rc = B.get(&Y, (size_t)n * ld, "Y")) || (rc = B.get(&T, (size_t)n * ld, "QR scratch")) ||
+      (bf16 && (rc = B.get(&Xb, (size_t)n * ld, "BF16 operand"))))
+    return rc;
+
+  cudaEventRecord(ev[0], st);
+  // Y = A * Omega
+  if (bf16) {
+    if ((rc = gaussian_fill_bf16(ctx, p->seed, 0, n, r, Xb, ld))) return rc;
+    if ((rc = spmm_store<__nv_bfloat16>(ctx, A, Xb, ld, (int)ld, Y, &launches))) return rc;
+  } else {
+    if ((rc = gaussian_fill_f32(ctx, p->seed, 0, n, r, T, ld))) return rc;
+    if ((rc = spmm_store<float>(ctx, A, T, ld, (int)ld, Y, &launches))) return rc;
+  }
+  launches += 1;
+  cudaEventRecord(ev[1], st);
+
+  if (p->random_project_only) {
+    // matU = Y, S = NULL: emb = Y[:, :dim] (PathEmbed.h:380 uses sigma = 1)
+    k_copy_cols<<<(unsigned)std::min<int64_t>((n * dim + 255) / 256, (int64_t)ctx->num_sms * 32), 256, 0, st>>>(
+        Y, ld, n, dim, d_emb);
+    launches += 1;
+    if (p->normalize && (rc = normalize_rows(ctx, d_emb, n, dim, dim, 1e-5f))) return rc;
+    if (h_S)
+      for (int i = 0; i < r; ++i) h_S[i] = 1.0f;
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (stats) {
+      memset(stats, 0, sizeof(*stats));
+      cudaEventElapsedTime(&stats->ms_sketch, ev[0], ev[1]);
+      stats->kernel_launches = launches + (p->normalize ? 1 : 0);
+    }
+    return LNE_OK;
+  }
+
+  // Q = qr(Y)
+  if ((rc = cholqr3(ctx, Y, T, n, ld, r, bf16 ? Xb : nullptr, &launches))) return rc;
+  cudaEventRecord(ev[2], st);
+  // B = A * Q
+  if ((rc = B.get(&Bm, (size_t)n * ld, "B"))) return rc;
+  if (bf16)
+    rc = spmm_store<__nv_bfloat16>(ctx, A, Xb, ld, (int)ld, Bm, &launches);
+  else
+    rc = spmm_store<float>(ctx, A, Y, ld, (int)ld, Bm, &launches);
+  if (rc) return rc;
+  cudaEventRecord(ev[3], st);
+  // Z = qr(B * P); Y holds Z from here on
+  if ((rc = B.get(&P, (size_t)r * r, "P"))) return rc;
+  if ((rc = gaussian_fill_f32(ctx, p->seed, 1, r, r, P, r))) return rc;
+  if ((rc = gemm_tall(ctx, Bm, ld, r, P, r, n, Y, ld, nullptr))) return rc;
+  launches += 2;
+  if ((rc = cholqr3(ctx, Y, T, n, ld, r, nullptr, &launches))) return rc;
+  cudaEventRecord(ev[4], st);
+  // C = Z^T B, C = U_C S V^T
+  if ((rc = B.get(&C, (size_t)r * r, "C")) || (rc = B.get(&U, (size_t)r * r, "U_C")) ||
+      (rc = B.get(&S, (size_t)r, "S")))
+    return rc;
+  if ((rc = gram(ctx, Y, ld, r, Bm, ld, r, n, C))) return rc;
+  int sweeps = 0;
+  if ((rc = jacobi_svd(ctx, C, r, U, S, &sweeps))) return rc;
+  launches += 3;
+  // emb = Z * (U_C[:, :dim] * diag(sqrt(S[:dim])))
+  if ((rc = B.get(&Wf, (size_t)r * dim, "U sqrt(S)"))) return rc;
+  k_scale_cols<<<(r * dim + 255) / 256, 256, 0, st>>>(U, S, r, dim, Wf);
+  if ((rc = gemm_tall(ctx, Y, ld, r, Wf, dim, n, d_emb, dim, nullptr))) return rc;
+  launches += 2;
+  if (p->normalize) {
+    if ((rc = normalize_rows(ctx, d_emb, n, dim, dim, 1e-5f))) return rc;
+    launches += 1;
+  }
+  cudaEventRecord(ev[5], st);
+  if (h_S) {
+    std::vector<double> hs(r);
+    LNE_CUDA_TRY(cudaMemcpyAsync(hs.data(), S, sizeof(double) * r, cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int i = 0; i < r; ++i) h_S[i] = (float)hs[i];
+  }
+  LNE_CUDA_TRY(cudaEventSynchronize(ev[5]));
+  LNE_CUDA_TRY(cudaGetLastError());
+  if (stats) {
+    cudaEventElapsedTime(&stats->ms_sketch, ev[0], ev[1]);
+    cudaEventElapsedTime(&stats->ms_qr, ev[1], ev[2]);
+    cudaEventElapsedTime(&stats->ms_spmm2, ev[2], ev[3]);
+    cudaEventElapsedTime(&stats->ms_core, ev[3], ev[5]);
+    cudaEventElapsedTime(&stats->ms_total, ev[0], ev[5]);
+    stats->jacobi_sweeps = sweeps;
+    stats->kernel_launches = launches;
+    stats->spmm_nnz = (double)A->nnz;
+  }
+  return LNE_OK;
+}
+
+extern "C" int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_t dim, float* d_emb, float* h_S) {
+  LNE_CHECK_ARG(ctx && d_x && d_emb && n >= 1 && dim >= 1 && dim <= n, "lne_dense_embed: bad argument");
+  if (dim > 1024) {
+    set_error("lne_dense_embed: dim above 1024 is not supported by the one-block Jacobi core");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const int d = (int)dim;
+  const int64_t ld = pad_ld(d);
+  Buf B(ctx);
+  float *X = nullptr, *Q = nullptr, *T = nullptr, *W = nullptr;
+  double *C = nullptr, *U = nullptr, *S = nullptr;
+  int rc, launches = 0;
+  if ((rc = B.get(&X, (size_t)n * ld, "X")) || (rc = B.get(&Q, (size_t)n * ld, "Q")) ||
+      (rc = B.get(&T, (size_t)n * ld, "QR scratch")) || (rc = B.get(&C, (size_t)d * d, "R")) ||
+      (rc = B.get(&U, (size_t)d * d, "U_R")) || (rc = B.get(&S, (size_t)d, "S")) ||
+      (rc = B.get(&W, (size_t)d * d, "U sqrt(S)")))
+    return rc;
+  // padded copy (the pad columns are zero)
+  LNE_CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(float) * n * ld, st));
+  LNE_CUDA_TRY(cudaMemcpy2DAsync(X, sizeof(float) * ld, d_x, sizeof(float) * d, sizeof(float) * d, n,
+                                 cudaMemcpyDeviceToDevice, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(Q, X, sizeof(float) * n * ld, cudaMemcpyDeviceToDevice, st));
+  // X = Q R with Q from CholeskyQR; R = Q^T X; R = U_R S V^T; U = Q U_R
+  if ((rc = cholqr3(ctx, Q, T, n, ld, d, nullptr, &launches))) return rc;
+  if ((rc = gram(ctx, Q, ld, d, X, ld, d, n, C))) return rc;
+  int sweeps = 0;
+  if ((rc = jacobi_svd(ctx, C, d, U, S, &sweeps))) return rc;
+  k_scale_cols<<<(d * d + 255) / 256, 256, 0, st>>>(U, S, d, d, W);
+  if ((rc = gemm_tall(ctx, Q, ld, d, W, d, n, d_emb, d, nullptr))) return rc;
+  // get_embedding_dense normalises unconditionally (SpectralPropagation.h:40)
+  if ((rc = normalize_rows(ctx, d_emb, n, d, d, 1e-5f))) return rc;
+  if (h_S) {
+    std::vector<double> hs(d);
+    LNE_CUDA_TRY(cudaMemcpyAsync(hs.data(), S, sizeof(double) * d, cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int i = 0; i < d; ++i) h_S[i] = (float)hs[i];
+  }
+  LNE_CUDA_TRY(cudaStreamSynchronize(st));
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}

@@ -39,3 +39,12 @@ def test_version_and_error_without_device(lib):
     assert isinstance(lib.lne_last_error(), bytes)
     # NULL out pointer is rejected before any device work
     assert lib.lne_ctx_create(None, 0, None) != 0
+
+
+def test_chebyshev_coefficients_match_scipy(lib):
+    import numpy as np
+    import scipy.special as ss
+    from lightne_gb300.api import chebyshev_coefficients
+    c = chebyshev_coefficients(10, 0.5)
+    ref = [ss.iv(0, 0.5), -2 * ss.iv(1, 0.5)] + [(-2 if k & 1 else 2) * ss.iv(k, 0.5) for k in range(2, 10)]
+    assert np.array_equal(c, np.array(ref, dtype=np.float32))

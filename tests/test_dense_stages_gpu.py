@@ -1,0 +1,98 @@
+"""Randomized SVD, spectral propagation and dense embedding on the device
+against the FP64 oracle (oracle/linalg_oracle.py) with the same Gaussian
+sketches.  Tolerances: FP32 form <= 1e-4 relative embedding error after
+Procrustes; BF16 form <= 2e-2 (BF16 operands carry 2^-9 relative rounding)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from lightne_gb300 import graphs
+from lightne_gb300.api import (CSR, Graph, chebyshev_expansion, gaussian, generate_trunc_log_matrix_v2,
+                               get_embedding_dense, randsvd)
+from oracle import linalg_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def netsmf_matrix(ctx):
+    off, nbrs = graphs.chung_lu(3000, 30000, 2.1, seed=21)
+    g = Graph.from_numpy(ctx, off, nbrs)
+    csr, _ = generate_trunc_log_matrix_v2(ctx, g, 5, walk_len=10, table_size=3_000_000, sample_ratio=1.0)
+    rp, col, val = csr.download()
+    yield csr, sp.csr_matrix((val.astype(np.float64), col, rp), shape=(3000, 3000)), (off, nbrs)
+    csr.free()
+    g.free()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-4), ("bf16", 2e-2)])
+@pytest.mark.parametrize("normalize", [False, True])
+def test_randsvd_matches_fp64(ctx, netsmf_matrix, precision, tol, normalize):
+    csr, A, _ = netsmf_matrix
+    rank, dim, seed = 48, 32, 777
+    emb, S, st = randsvd(ctx, csr, rank, dim, normalize=normalize, precision=precision, seed=seed)
+    om = gaussian(ctx, seed, 0, A.shape[0], rank)
+    if precision == "bf16":
+        om = om.to(torch.bfloat16).float()
+    P = gaussian(ctx, seed, 1, rank, rank)
+    ref, Sref = lo.randsvd(A, om.double().cpu().numpy(), P.double().cpu().numpy(), dim, normalize=normalize)
+    e = emb.double().cpu().numpy()
+    assert np.isfinite(e).all()
+    err = lo.procrustes_rel_error(e, ref)
+    assert err < tol, err
+    assert lo.rel_sv_error(S[:dim], Sref[:dim]) < tol
+    assert st["jacobi_sweeps"] > 0
+
+
+def test_random_project_only(ctx, netsmf_matrix):
+    csr, A, _ = netsmf_matrix
+    emb, S, _ = randsvd(ctx, csr, 40, 24, random_project_only=True, seed=9)
+    om = gaussian(ctx, 9, 0, A.shape[0], 40).double().cpu().numpy()
+    ref, _ = lo.randsvd(A, om, None, 24, random_project_only=True)
+    np.testing.assert_allclose(emb.double().cpu().numpy(), ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("bf16", 1.5e-2)])
+@pytest.mark.parametrize("order,dim", [(10, 128), (10, 20), (2, 16), (3, 16)])
+def test_propagate_matches_fp64(ctx, netsmf_matrix, precision, tol, order, dim):
+    _, _, (off, nbrs) = netsmf_matrix
+    g = Graph.from_numpy(ctx, off, nbrs)
+    a = np.random.default_rng(3).standard_normal((off.size - 1, dim)).astype(np.float32)
+    y, a2, _ = chebyshev_expansion(ctx, g, a, dim, order=order, precision=precision, return_a=True)
+    yref, a2ref = lo.propagate(off, nbrs, a, order=order)
+    y = y.double().cpu().numpy()
+    rel = np.linalg.norm(y - yref) / np.linalg.norm(yref)
+    assert rel < tol, rel
+    rel2 = np.linalg.norm(a2.double().cpu().numpy() - a2ref) / np.linalg.norm(a2ref)
+    assert rel2 < tol, rel2
+    g.free()
+
+
+def test_propagate_long_rows(ctx):
+    # a star: the hub's adjacency row exceeds the SpMM chunk (2048 entries)
+    off, nbrs = graphs.star_graph(9000)
+    g = Graph.from_numpy(ctx, off, nbrs)
+    a = np.random.default_rng(4).standard_normal((9000, 24)).astype(np.float32)
+    y, _ = chebyshev_expansion(ctx, g, a, 24, order=10)
+    yref, _ = lo.propagate(off, nbrs, a, order=10)
+    rel = np.linalg.norm(y.double().cpu().numpy() - yref) / np.linalg.norm(yref)
+    assert rel < 1e-5, rel
+    g.free()
+
+
+@pytest.mark.parametrize("dim", [16, 64, 128])
+def test_dense_embed_matches_fp64(ctx, dim):
+    rng = np.random.default_rng(dim)
+    n = 5000
+    U, _ = np.linalg.qr(rng.standard_normal((n, dim)))
+    V, _ = np.linalg.qr(rng.standard_normal((dim, dim)))
+    s = np.logspace(0, -2.5, dim)
+    x = (U * s) @ V.T
+    emb, S = get_embedding_dense(ctx, x.astype(np.float32), dim)
+    ref, Sref = lo.dense_embed(x.astype(np.float32))
+    err = lo.procrustes_rel_error(emb.double().cpu().numpy(), ref)
+    assert err < 1e-4, err
+    assert lo.rel_sv_error(S, Sref) < 1e-4
+    nr = np.linalg.norm(emb.double().cpu().numpy(), axis=1)
+    np.testing.assert_allclose(nr, 1.0, rtol=1e-5)
