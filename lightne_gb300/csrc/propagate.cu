@@ -64,16 +64,25 @@ __global__ void k_op_coef(const Vertex* __restrict__ vd, int64_t n, float mu, fl
   coef[i] = make_float2((float)(1.0 - (double)mu - inv), (float)(-inv));
 }
 
-// Loads E elements of row r of a dense operand (FP32 or BF16) as floats.
+// Loads N elements (N a multiple of 4, e0 a multiple of 4) of row r of a
+// dense operand as floats: 16-byte loads for FP32, 8-byte loads for BF16
+// (so an e0 that is 4 mod 8 stays aligned).
 template <typename T, int N>
 __device__ __forceinline__ void load_row(const T* __restrict__ X, int64_t ld, int64_t r, int e0, float (&o)[N]) {
   const T* p = X + r * ld + e0;
+  if constexpr (sizeof(T) == 4) {
 #pragma unroll
-  for (int i = 0; i < N; i += Vec16<T>::E) {
-    float v[Vec16<T>::E];
-    Vec16<T>::load(p + i, v);
+    for (int i = 0; i < N; i += 4) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(p + i));
+      o[i] = v.x; o[i + 1] = v.y; o[i + 2] = v.z; o[i + 3] = v.w;
+    }
+  } else {
 #pragma unroll
-    for (int q = 0; q < Vec16<T>::E && i + q < N; ++q) o[i + q] = v[q];
+    for (int i = 0; i < N; i += 4) {
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(p + i));
+      o[i] = __uint_as_float(v.x << 16); o[i + 1] = __uint_as_float(v.x & 0xffff0000u);
+      o[i + 2] = __uint_as_float(v.y << 16); o[i + 3] = __uint_as_float(v.y & 0xffff0000u);
+    }
   }
 }
 template <int N>
