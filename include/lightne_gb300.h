@@ -161,7 +161,8 @@ int lne_randsvd(lne_ctx* ctx, const lne_csr* A, const lne_randsvd_params* p, flo
 /*
  * The Gaussian sketch generator lne_randsvd uses: rows x cols N(0,1) values
  * of stream stream_id (0: Omega, 1: P) into device memory with leading
- * dimension ld.  Exposed so that a checker can rebuild the same sketches
+ * dimension ld.  Values are rounded to BF16-representable floats, so the
+ * FP32 and BF16 forms share one sketch.  Exposed so that a checker can rebuild the same sketches
  * (the reference's VSL SFMT19937 stream, mklredsvd.cc:141, has no
  * counterpart without MKL).
  */

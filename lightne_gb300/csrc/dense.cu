@@ -22,7 +22,9 @@ __device__ __forceinline__ float gaussian_at(uint64_t base, uint64_t idx) {
   const float u2 = (float)(x2 >> 40) * 5.9604644775390625e-08f;        // [0, 1)
   float s, c;
   sincospif(2.0f * u2, &s, &c);
-  return sqrtf(-2.0f * logf(u1)) * c;
+  // rounded to a BF16-representable value, so that the FP32 and BF16 forms
+  // of the randomized SVD use the same sketch
+  return __bfloat162float(__float2bfloat16_rn(sqrtf(-2.0f * logf(u1)) * c));
 }
 
 template <typename T>

@@ -32,6 +32,19 @@ import scipy.sparse as sp
 import scipy.special as ss
 
 
+def spmm64(A: sp.csr_matrix, X: np.ndarray) -> np.ndarray:
+    """A @ X in FP64.  Uses torch's multi-threaded CPU CSR product when torch
+    is importable (same FP64 arithmetic, faster on large matrices)."""
+    try:
+        import torch
+    except ImportError:
+        return A @ X
+    At = torch.sparse_csr_tensor(torch.from_numpy(A.indptr.astype(np.int64)),
+                                 torch.from_numpy(A.indices.astype(np.int64)),
+                                 torch.from_numpy(A.data.astype(np.float64)), size=A.shape)
+    return torch.sparse.mm(At, torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64))).numpy()
+
+
 def qr_pos(Y: np.ndarray) -> np.ndarray:
     """Thin Q of Y with diag(R) > 0 (the CholeskyQR factor)."""
     Q, R = np.linalg.qr(Y, mode="reduced")
@@ -56,11 +69,11 @@ def randsvd(A: sp.csr_matrix, omega: np.ndarray, P: np.ndarray, dim: int, normal
             random_project_only: bool = False):
     """MKLRedSVD::run + compute_u_sigma_root in FP64.  Returns (emb, S)."""
     A = A.astype(np.float64)
-    Y = A @ omega
+    Y = spmm64(A, omega)
     if random_project_only:
         return u_sigma_root(Y, None, dim, normalize), None
     Q = qr_pos(Y)
-    B = A @ Q
+    B = spmm64(A, Q)
     Z = qr_pos(B @ P)
     C = Z.T @ B
     Uc, S, _ = np.linalg.svd(C)
@@ -97,20 +110,20 @@ def propagate(offsets: np.ndarray, nbrs: np.ndarray, a: np.ndarray, order: int =
     diag, off = operator_values(deg, mu)
     rows = np.repeat(np.arange(n), deg)
     Adj = sp.csr_matrix((np.ones(nbrs.size), nbrs.astype(np.int64), offsets), shape=(n, n))
-    M = sp.diags(diag) + sp.diags(off) @ Adj
+    M = (sp.diags(diag) + sp.diags(off) @ Adj).tocsr()
     c = chebyshev_coefficients(order, s)
     a = a.astype(np.float64)
     Lx0 = a.copy()
-    tmp = M @ a
-    Lx1 = 0.5 * (M @ tmp) - a
+    tmp = spmm64(M, a)
+    Lx1 = 0.5 * spmm64(M, tmp) - a
     conv = c[0] * Lx0 + c[1] * Lx1
     for k in range(2, order):
-        tmp = M @ Lx1
-        Lx2 = M @ tmp - Lx0 - 2.0 * Lx1
+        tmp = spmm64(M, Lx1)
+        Lx2 = spmm64(M, tmp) - Lx0 - 2.0 * Lx1
         conv = conv + c[k] * Lx2
         Lx0, Lx1 = Lx1, Lx2
     a2 = a - conv
-    y = a2 + Adj @ a2
+    y = a2 + spmm64(Adj, a2)
     del rows
     return y, a2
 
