@@ -284,8 +284,17 @@ def run_ours(args, ws, rank, local):
     barrier(ws)
     with ClockSampler(local) as clk:
         ms_bf, st_bf, out_bf, emb_bf = time_form(ctx, g, w, "bf16", seed, args.steps, args.warmup, stream, flush)
-        ms_fp, st_fp, out_fp, emb_fp = time_form(ctx, g, w, "fp32", seed, args.steps, args.warmup, stream, flush)
+        if args.quick:
+            ms_fp, st_fp = ms_bf, st_bf
+        else:
+            ms_fp, st_fp, out_fp, emb_fp = time_form(ctx, g, w, "fp32", seed, args.steps, args.warmup, stream,
+                                                     flush)
     barrier(ws)
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"quick": True, "ms_per_step_bf16": ms_bf, "stages": st_bf[-1]}))
+        ctx.close()
+        return
     ms_bf = allmax(ws, ms_bf)
     ms_fp = allmax(ws, ms_fp)
     samples = st_bf[-1]["sparsify"]["samples_emitted"]
@@ -424,6 +433,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="BF16 form only, no e2e / CPU legs (for profiling)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

@@ -65,6 +65,15 @@ int lne_ctx_destroy(lne_ctx* ctx);
 int lne_ctx_synchronize(lne_ctx* ctx);
 
 /*
+ * Device memory helpers for callers that do not link the CUDA runtime
+ * (stream-ordered on the context's stream; copies synchronise).
+ */
+int lne_device_alloc(lne_ctx* ctx, int64_t bytes, void** out);
+int lne_device_free(lne_ctx* ctx, void* p);
+int lne_copy_to_host(lne_ctx* ctx, void* host_dst, const void* dev_src, int64_t bytes);
+int lne_copy_to_device(lne_ctx* ctx, void* dev_dst, const void* host_src, int64_t bytes);
+
+/*
  * Graph: symmetric CSR, offsets int64[n+1] (offsets[n] = number of directed
  * entries), neighbours int32[offsets[n]], in the order of the AdjacencyGraph
  * file (the walk depends on it).  Host pointers; the graph is copied to the
@@ -134,7 +143,9 @@ typedef struct lne_randsvd_params {
   int64_t rank;                 /* -rank: sketch width r (oversampled) */
   int64_t dim;                  /* -dim: embedding dimension d <= r */
   int32_t normalize;            /* -normalize: L2-normalise embedding rows */
-  int32_t precision;            /* LNE_PREC_FP32 or LNE_PREC_BF16 (SpMM dense operand) */
+  int32_t precision;            /* LNE_PREC_BF16: the sketch product A * Omega reads a BF16
+                                   Omega (exact: the sketch is BF16-representable); the product
+                                   A * Q reads FP32 Q in both forms */
   uint64_t seed;                /* Gaussian sketch seed (the reference's VSL seed is 777) */
   int32_t random_project_only;  /* -random_project_only: return (A * Omega)[:, :dim] */
   int32_t reserved;
@@ -200,6 +211,19 @@ int lne_propagate(lne_ctx* ctx, const lne_graph* g, const lne_propagate_params* 
  * in extended precision and narrowed as the reference's axpy calls do
  * (SpectralPropagation.h:129-197). */
 int lne_chebyshev_coefficients(int32_t order, double s, float* out);
+
+/*
+ * Adjoint of lne_propagate (P3; no counterpart in the reference): for
+ * y = (A + I)(a - sum_k c_k(s) T_k(X(mu)) a) and an output gradient g
+ * (device n x dim), d_ga = dL/da (device n x dim, may be NULL), *h_dmu =
+ * dL/dmu and *h_ds = dL/ds (host, may be NULL; they need d_a).  Uses
+ * M^T = D~ M D~^-1, so dL/da = h - D~ sum_k c_k T_k(X) D~^-1 h with
+ * h = (A + I) g; dL/ds = -sum_k c_k'(s) <h, T_k a>; dL/dmu from the forward
+ * tangent T'_1 = -M a, T'_{k+1} = 2 X T'_k - T'_{k-1} - 2 M T_k.
+ * The derivatives are of the real-valued map (mu, s not rounded to float).
+ */
+int lne_propagate_adjoint(lne_ctx* ctx, const lne_graph* g, const lne_propagate_params* p, const float* d_a,
+                          const float* d_gy, float* d_ga, double* h_dmu, double* h_ds, lne_propagate_stats* stats);
 
 /*
  * Dense embedding (P5): SVD of x (device n x dim FP32) and

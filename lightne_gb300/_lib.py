@@ -137,6 +137,10 @@ SIGNATURES = {
     "lne_ctx_create": (ctypes.c_int, [PVP, ctypes.c_int, VP]),
     "lne_ctx_destroy": (ctypes.c_int, [VP]),
     "lne_ctx_synchronize": (ctypes.c_int, [VP]),
+    "lne_device_alloc": (ctypes.c_int, [VP, I64, PVP]),
+    "lne_device_free": (ctypes.c_int, [VP, VP]),
+    "lne_copy_to_host": (ctypes.c_int, [VP, VP, VP, I64]),
+    "lne_copy_to_device": (ctypes.c_int, [VP, VP, VP, I64]),
     "lne_graph_upload": (ctypes.c_int, [VP, I64, VP, VP, PVP]),
     "lne_graph_upload_device": (ctypes.c_int, [VP, I64, VP, VP, PVP]),
     "lne_graph_free": (ctypes.c_int, [VP]),
@@ -147,6 +151,9 @@ SIGNATURES = {
     "lne_gaussian": (ctypes.c_int, [VP, ctypes.c_uint64, ctypes.c_uint64, I64, I64, VP, I64]),
     "lne_propagate": (ctypes.c_int, [VP, VP, ctypes.POINTER(PropagateParams), VP, VP, VP,
                                      ctypes.POINTER(PropagateStats)]),
+    "lne_propagate_adjoint": (ctypes.c_int, [VP, VP, ctypes.POINTER(PropagateParams), VP, VP, VP,
+                                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                             ctypes.POINTER(PropagateStats)]),
     "lne_chebyshev_coefficients": (ctypes.c_int, [ctypes.c_int32, ctypes.c_double, VP]),
     "lne_dense_embed": (ctypes.c_int, [VP, VP, I64, I64, VP, VP]),
     "lne_csr_info": (ctypes.c_int, [VP, ctypes.POINTER(I64), ctypes.POINTER(I64)]),

@@ -16,7 +16,7 @@ from ._lib import (LNE_PREC_BF16, LNE_PREC_FP32, LneError, PropagateParams, Prop
                    RandsvdStats, SparsifyParams, SparsifyStats, check)
 
 __all__ = ["Context", "Graph", "CSR", "generate_trunc_log_matrix_v2", "randsvd",
-           "chebyshev_expansion", "get_embedding_dense", "gaussian", "chebyshev_coefficients", "LneError"]
+           "chebyshev_expansion", "get_embedding_dense", "gaussian", "chebyshev_coefficients", "propagate_adjoint", "ChebyshevPropagation", "LneError"]
 
 PRECISIONS = {"fp32": LNE_PREC_FP32, "bf16": LNE_PREC_BF16}
 
@@ -231,3 +231,68 @@ def chebyshev_coefficients(order: int, s: float = 0.5) -> np.ndarray:
     out = np.zeros(max(order, 2), dtype=np.float32)
     check(_lib.load().lne_chebyshev_coefficients(order, s, _ptr(out)))
     return out
+
+
+def propagate_adjoint(ctx: Context, graph: Graph, a, gy, dim: int, order: int = 10, mu: float = 0.2,
+                      s: float = 0.5, precision: str = "fp32", need_params: bool = True):
+    """Adjoint of :func:`chebyshev_expansion`: returns (dL/da torch, dL/dmu,
+    dL/ds) for the output gradient ``gy`` (no counterpart in the reference)."""
+    torch = _torch()
+    da = _as_device_f32(a, ctx.device)
+    dg = _as_device_f32(gy, ctx.device)
+    ga = torch.empty_like(dg)
+    dmu = ctypes.c_double(0.0)
+    ds = ctypes.c_double(0.0)
+    p = PropagateParams(dim=dim, order=order, precision=PRECISIONS[precision], mu=mu, s=s)
+    st = PropagateStats()
+    check(_lib.load().lne_propagate_adjoint(
+        ctx.handle, graph.handle, ctypes.byref(p), ctypes.c_void_p(da.data_ptr()), ctypes.c_void_p(dg.data_ptr()),
+        ctypes.c_void_p(ga.data_ptr()), ctypes.byref(dmu) if need_params else None,
+        ctypes.byref(ds) if need_params else None, ctypes.byref(st)))
+    return ga, dmu.value, ds.value
+
+
+def _make_autograd_function():
+    torch = _torch()
+
+    class _ChebyshevPropagation(torch.autograd.Function):
+        """y = (A + I)(a - sum_k c_k(s) T_k(X(mu)) a) on the device, with the
+        hand-written adjoint (lne_propagate_adjoint) as its backward."""
+
+        @staticmethod
+        def forward(fctx, a, mu, s, lctx, graph, order, precision):
+            a = a.contiguous().float()
+            y, _ = chebyshev_expansion(lctx, graph, a, a.shape[1], order=order, mu=float(mu), s=float(s),
+                                       precision=precision)
+            fctx.save_for_backward(a)
+            fctx.lctx, fctx.graph, fctx.order, fctx.precision = lctx, graph, order, precision
+            fctx.mu, fctx.s = float(mu), float(s)
+            fctx.need_mu = torch.is_tensor(mu) and mu.requires_grad
+            fctx.need_s = torch.is_tensor(s) and s.requires_grad
+            return y
+
+        @staticmethod
+        def backward(fctx, gy):
+            (a,) = fctx.saved_tensors
+            need = fctx.need_mu or fctx.need_s
+            ga, dmu, ds = propagate_adjoint(fctx.lctx, fctx.graph, a, gy.contiguous(), a.shape[1],
+                                            order=fctx.order, mu=fctx.mu, s=fctx.s, precision=fctx.precision,
+                                            need_params=need)
+            gmu = torch.tensor(dmu, dtype=torch.float32, device=a.device) if fctx.need_mu else None
+            gs = torch.tensor(ds, dtype=torch.float32, device=a.device) if fctx.need_s else None
+            return ga, gmu, gs, None, None, None, None
+
+    return _ChebyshevPropagation
+
+
+_AUTOGRAD = None
+
+
+def ChebyshevPropagation(a, mu, s, lctx: Context, graph: Graph, order: int = 10, precision: str = "fp32"):
+    """Differentiable spectral propagation (``torch.autograd.Function``):
+    gradients flow to ``a`` and to ``mu`` / ``s`` when they are tensors that
+    require grad."""
+    global _AUTOGRAD
+    if _AUTOGRAD is None:
+        _AUTOGRAD = _make_autograd_function()
+    return _AUTOGRAD.apply(a, mu, s, lctx, graph, order, precision)

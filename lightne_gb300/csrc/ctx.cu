@@ -1,5 +1,6 @@
 // Context, errors, graph upload, CSR handles and the device scan.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -213,6 +214,25 @@ int lne_ctx_create(lne_ctx** out, int device, void* stream) {
     return LNE_ERR_ALLOC;
   }
   cudaMemset(c->d_flags, 0, sizeof(int) * kFlagWords);
+  {
+    // log(1 + j/128) and 1/(1 + j/128) as double-floats, from long double
+    LogTable T;
+    for (int j = 0; j < 128; ++j) {
+      const long double cj = 1.0L + (long double)j / 128.0L, lg = logl(cj), inv = 1.0L / cj;
+      T.log_hi[j] = (float)lg;
+      T.log_lo[j] = (float)(lg - (long double)T.log_hi[j]);
+      T.inv_hi[j] = (float)inv;
+      T.inv_lo[j] = (float)(inv - (long double)T.inv_hi[j]);
+    }
+    if (cudaMalloc(&c->log_table, sizeof(LogTable)) != cudaSuccess ||
+        cudaMemcpy(c->log_table, &T, sizeof(LogTable), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(c->d_flags);
+      delete c;
+      set_error("lne_ctx_create: cannot set up the log table");
+      return LNE_ERR_ALLOC;
+    }
+  }
   *out = c;
   clear_error();
   return LNE_OK;
@@ -223,6 +243,7 @@ int lne_ctx_destroy(lne_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->d_flags);
+  cudaFree(ctx->log_table);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return LNE_OK;
@@ -348,6 +369,32 @@ int lne_graph_upload(lne_ctx* ctx, int64_t n, const int64_t* offsets, const int3
 int lne_graph_upload_device(lne_ctx* ctx, int64_t n, const int64_t* d_offsets, const int32_t* d_nbrs,
                             lne_graph** out) {
   return graph_upload_impl(ctx, n, d_offsets, d_nbrs, true, out);
+}
+
+int lne_device_alloc(lne_ctx* ctx, int64_t bytes, void** out) {
+  LNE_CHECK_ARG(ctx && out && bytes >= 0, "lne_device_alloc: bad argument");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  return dalloc(ctx, out, (size_t)bytes, "lne_device_alloc");
+}
+
+int lne_device_free(lne_ctx* ctx, void* p) {
+  LNE_CHECK_ARG(ctx != nullptr, "lne_device_free: ctx is NULL");
+  dfree(ctx, p);
+  return LNE_OK;
+}
+
+int lne_copy_to_host(lne_ctx* ctx, void* host_dst, const void* dev_src, int64_t bytes) {
+  LNE_CHECK_ARG(ctx && host_dst && dev_src && bytes >= 0, "lne_copy_to_host: bad argument");
+  LNE_CUDA_TRY(cudaMemcpyAsync(host_dst, dev_src, (size_t)bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return LNE_OK;
+}
+
+int lne_copy_to_device(lne_ctx* ctx, void* dev_dst, const void* host_src, int64_t bytes) {
+  LNE_CHECK_ARG(ctx && dev_dst && host_src && bytes >= 0, "lne_copy_to_device: bad argument");
+  LNE_CUDA_TRY(cudaMemcpyAsync(dev_dst, host_src, (size_t)bytes, cudaMemcpyHostToDevice, ctx->stream));
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return LNE_OK;
 }
 
 int lne_csr_info(const lne_csr* c, int64_t* n, int64_t* nnz) {

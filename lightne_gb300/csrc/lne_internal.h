@@ -54,6 +54,7 @@ struct lne_ctx {
   int* d_flags = nullptr;       // device int32[kFlagWords]
   int num_sms = 0;
   size_t smem_optin = 0;
+  void* log_table = nullptr;    // device lne::LogTable (double-float log(c_j), 1/c_j)
 };
 
 struct lne_graph {

@@ -56,12 +56,14 @@ void chebyshev_coeffs(int order, double s, std::vector<float>& c) {
 
 namespace {
 
-__global__ void k_op_coef(const Vertex* __restrict__ vd, int64_t n, float mu, float2* __restrict__ coef) {
+// Per-row operator data: x = diagonal m_i, y = off-diagonal o_i (the floats
+// the reference stores), z = d~_i = deg + 1, w = 1 / d~_i.
+__global__ void k_op_coef(const Vertex* __restrict__ vd, int64_t n, float mu, float4* __restrict__ coef) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float dt = (float)(vd[i].deg + 1u);
   const double inv = 1.0 / (double)dt;
-  coef[i] = make_float2((float)(1.0 - (double)mu - inv), (float)(-inv));
+  coef[i] = make_float4((float)(1.0 - (double)mu - inv), (float)(-inv), dt, (float)inv);
 }
 
 // Loads N elements (N a multiple of 4, e0 a multiple of 4) of row r of a
@@ -108,17 +110,18 @@ __device__ __forceinline__ void store_bf16(__nv_bfloat16* __restrict__ X, int64_
   for (int i = 0; i < N; i += 2) *reinterpret_cast<__nv_bfloat162*>(p + i) = __floats2bfloat162_rn(o[i], o[i + 1]);
 }
 
-// tmp = M x: out = m_i x_i + o_i acc (operand x of type XT).
+// tmp = M x: out = m_i x_i + o_i acc (operand x of type XT); FP32 and/or
+// BF16 outputs.
 template <typename XT>
 struct EpiApplyM {
-  const float2* __restrict__ coef;
+  const float4* __restrict__ coef;
   const XT* __restrict__ X;  // the operand (diagonal term)
   int64_t ld;
-  float* __restrict__ out_f;           // FP32 output (FP32 form) or null
-  __nv_bfloat16* __restrict__ out_b;   // BF16 output (BF16 form) or null
+  float* __restrict__ out_f;
+  __nv_bfloat16* __restrict__ out_b;
   template <int N>
   __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&a)[N]) const {
-    const float2 c = __ldg(coef + r);
+    const float4 c = __ldg(coef + r);
     float x[N], y[N];
     load_row<XT, N>(X, ld, r, e0, x);
 #pragma unroll
@@ -128,23 +131,40 @@ struct EpiApplyM {
   }
 };
 
-// First order: Lx1 = 0.5 M tmp - a;  conv = c0 a + c1 Lx1;  optionally the
-// final a - conv when the filter has order <= 2.
+// Final vector of a filter: fin = base - (scale_dt ? d~_i : 1) * conv.
+struct FinalOut {
+  const float* __restrict__ base;  // null: not the final step
+  bool scale_dt;
+  float* __restrict__ out;
+  __nv_bfloat16* __restrict__ outb;
+  template <int N>
+  __device__ __forceinline__ void apply(int64_t r, int e0, int64_t ld, const float4 c, const float (&cv)[N]) const {
+    float b[N], f[N];
+    load_f32<N>(base, ld, r, e0, b);
+    const float sc = scale_dt ? c.z : 1.0f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) f[i] = fmaf(-sc, cv[i], b[i]);
+    store_f32<N>(out, ld, r, e0, f);
+    if (outb) store_bf16<N>(outb, ld, r, e0, f);
+  }
+};
+
+// First order: Lx1 = 0.5 M tmp - x;  conv = c0 x + c1 Lx1 (conv may be null:
+// the tangent pass keeps no sum);  or the final vector when order <= 2.
 template <typename XT>
 struct EpiFirst {
-  const float2* __restrict__ coef;
+  const float4* __restrict__ coef;
   const XT* __restrict__ T;        // tmp (operand)
-  const float* __restrict__ A;     // a (FP32)
+  const float* __restrict__ A;     // x (FP32)
   float* __restrict__ L1;          // Lx1 FP32
   __nv_bfloat16* __restrict__ L1b; // Lx1 BF16 copy (BF16 form) or null
   float* __restrict__ conv;
-  float* __restrict__ afin;        // a - conv, or null
-  __nv_bfloat16* __restrict__ afinb;
+  FinalOut fin;
   int64_t ld;
   float c0, c1;
   template <int N>
   __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&acc)[N]) const {
-    const float2 c = __ldg(coef + r);
+    const float4 c = __ldg(coef + r);
     float t[N], a[N], l1[N], cv[N];
     load_row<XT, N>(T, ld, r, e0, t);
     load_f32<N>(A, ld, r, e0, a);
@@ -156,58 +176,66 @@ struct EpiFirst {
     }
     store_f32<N>(L1, ld, r, e0, l1);
     if (L1b) store_bf16<N>(L1b, ld, r, e0, l1);
-    if (afin) {
-#pragma unroll
-      for (int i = 0; i < N; ++i) cv[i] = a[i] - cv[i];
-      store_f32<N>(afin, ld, r, e0, cv);
-      if (afinb) store_bf16<N>(afinb, ld, r, e0, cv);
-    } else {
+    if (fin.base)
+      fin.apply<N>(r, e0, ld, c, cv);
+    else if (conv)
       store_f32<N>(conv, ld, r, e0, cv);
-    }
   }
 };
 
-// Order k >= 2: Lx2 = M tmp - Lx0 - 2 Lx1;  conv += ck Lx2;  optionally
-// a - conv on the last order.
+// Order k >= 2: Lx2 = M tmp - Lx0 - 2 Lx1 [- 2 extra];  conv += ck Lx2 (conv
+// may be null);  or the final vector on the last order.  L0 == null means a
+// zero Lx0; `extra` (FP32, may be null) is the tangent pass's M T_k term.
 template <typename XT>
 struct EpiStep {
-  const float2* __restrict__ coef;
+  const float4* __restrict__ coef;
   const XT* __restrict__ T;
   const float* __restrict__ L0;
   const float* __restrict__ L1;
+  const float* __restrict__ extra;
   float* __restrict__ L2;
   __nv_bfloat16* __restrict__ L2b;
   float* __restrict__ conv;
-  const float* __restrict__ A;
-  float* __restrict__ afin;
-  __nv_bfloat16* __restrict__ afinb;
+  FinalOut fin;
   int64_t ld;
   float ck;
   template <int N>
   __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&acc)[N]) const {
-    const float2 c = __ldg(coef + r);
+    const float4 c = __ldg(coef + r);
     float t[N], l0[N], l1[N], l2[N], cv[N];
     load_row<XT, N>(T, ld, r, e0, t);
-    load_f32<N>(L0, ld, r, e0, l0);
+    if (L0) {
+      load_f32<N>(L0, ld, r, e0, l0);
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) l0[i] = 0.0f;
+    }
     load_f32<N>(L1, ld, r, e0, l1);
-    load_f32<N>(conv, ld, r, e0, cv);
+    if (conv) {
+      load_f32<N>(conv, ld, r, e0, cv);
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) cv[i] = 0.0f;
+    }
+    float ex[N];
+    if (extra) {
+      load_f32<N>(extra, ld, r, e0, ex);
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) ex[i] = 0.0f;
+    }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       const float mt = fmaf(c.x, t[i], c.y * acc[i]);
-      l2[i] = fmaf(-2.0f, l1[i], mt - l0[i]);
+      l2[i] = fmaf(-2.0f, ex[i], fmaf(-2.0f, l1[i], mt - l0[i]));
       cv[i] = fmaf(ck, l2[i], cv[i]);
     }
-    if (!afin) {
+    if (fin.base) {
+      fin.apply<N>(r, e0, ld, c, cv);
+    } else {
       store_f32<N>(L2, ld, r, e0, l2);
       if (L2b) store_bf16<N>(L2b, ld, r, e0, l2);
-      store_f32<N>(conv, ld, r, e0, cv);
-    } else {
-      float a[N];
-      load_f32<N>(A, ld, r, e0, a);
-#pragma unroll
-      for (int i = 0; i < N; ++i) a[i] -= cv[i];
-      store_f32<N>(afin, ld, r, e0, a);
-      if (afinb) store_bf16<N>(afinb, ld, r, e0, a);
+      if (conv) store_f32<N>(conv, ld, r, e0, cv);
     }
   }
 };
@@ -232,6 +260,31 @@ struct EpiAPlusI {
   }
 };
 
+// Adjoint start: h = (A + I) g;  b = h / d~_i (FP32 and BF16 copy).
+template <typename XT>
+struct EpiAdjInit {
+  const float4* __restrict__ coef;
+  const XT* __restrict__ G;
+  int64_t ld;
+  float* __restrict__ H;
+  float* __restrict__ Bf;
+  __nv_bfloat16* __restrict__ Bb;
+  template <int N>
+  __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&acc)[N]) const {
+    const float4 c = __ldg(coef + r);
+    float gr[N], h[N], b[N];
+    load_row<XT, N>(G, ld, r, e0, gr);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      h[i] = gr[i] + acc[i];
+      b[i] = h[i] * c.w;
+    }
+    store_f32<N>(H, ld, r, e0, h);
+    store_f32<N>(Bf, ld, r, e0, b);
+    if (Bb) store_bf16<N>(Bb, ld, r, e0, b);
+  }
+};
+
 __global__ void k_pad_copy(const float* __restrict__ src, int64_t n, int d, float* __restrict__ dst, int64_t ld,
                            __nv_bfloat16* __restrict__ dstb) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n * ld; t += (int64_t)gridDim.x * blockDim.x) {
@@ -247,6 +300,36 @@ __global__ void k_unpad_copy(const float* __restrict__ src, int64_t ld, int64_t 
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n * d; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t / d;
     dst[t] = src[i * ld + (t - i * d)];
+  }
+}
+
+// y = alpha x (FP32) and its BF16 copy.
+__global__ void k_scale_copy(const float* __restrict__ x, int64_t total, float alpha, float* __restrict__ y,
+                             __nv_bfloat16* __restrict__ yb) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const float v = alpha * x[t];
+    y[t] = v;
+    if (yb) yb[t] = __float2bfloat16_rn(v);
+  }
+}
+
+// <h, x> partial sums: FP32 within a thread, FP64 across threads, one
+// value per block (summed in block order on the host).
+static constexpr int kDotBlocks = 1024;
+__global__ void k_dot_partial(const float* __restrict__ h, const float* __restrict__ x, int64_t total,
+                              double* __restrict__ out) {
+  float s = 0.0f;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+    s = fmaf(h[t], x[t], s);
+  double d = (double)s;
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+  __shared__ double ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += ws[i];
+    out[blockIdx.x] = t;
   }
 }
 
@@ -267,6 +350,86 @@ struct Bufs {
   }
 };
 
+// Shared state of one filter evaluation.
+template <typename XT>
+struct Filter {
+  static constexpr bool kBF16 = sizeof(XT) == 2;
+  lne_ctx* ctx;
+  lne_graph* g;
+  GraphRows R;
+  int64_t n, ld;
+  const float4* coef;
+  int* launches;
+  Bufs* B;
+  size_t sz() const { return (size_t)n * ld; }
+
+  // operand view of an FP32 vector with an optional BF16 copy
+  const XT* op(const float* f, const __nv_bfloat16* b) const { return kBF16 ? (const XT*)b : (const XT*)f; }
+
+  int apply_m(const XT* X, float* out_f, __nv_bfloat16* out_b) {
+    EpiApplyM<XT> epi{coef, X, ld, out_f, out_b};
+    return spmm_run<XT>(ctx, R, g->plan, X, ld, ld, epi, launches);
+  }
+
+  // The Chebyshev filter on x (FP32 xf, operand copy xb): fin = base -
+  // scale * sum_k c_k T_k(X) x written to finf / finb.
+  int run(const float* xf, const __nv_bfloat16* xb, int order, const std::vector<float>& c, const float* base,
+          bool scale_dt, float* finf, __nv_bfloat16* finb) {
+    int rc;
+    float *conv = nullptr, *Tf = nullptr;
+    __nv_bfloat16* Tb = nullptr;
+    float* ring[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16* ringb[3] = {nullptr, nullptr, nullptr};
+    const int nring = order > 2 ? 3 : 1;
+    if ((rc = B->get(&conv, sz(), "conv"))) return rc;
+    for (int i = 0; i < nring; ++i) {
+      if ((rc = B->get(&ring[i], sz(), "Chebyshev vector"))) return rc;
+      if (kBF16 && (rc = B->get(&ringb[i], sz(), "Chebyshev vector bf16"))) return rc;
+    }
+    if (kBF16) {
+      if ((rc = B->get(&Tb, sz(), "tmp bf16"))) return rc;
+    } else if ((rc = B->get(&Tf, sz(), "tmp"))) {
+      return rc;
+    }
+    const XT* X0 = op(xf, xb);
+    const XT* Tx = kBF16 ? (const XT*)Tb : (const XT*)Tf;
+    if ((rc = apply_m(X0, kBF16 ? nullptr : Tf, kBF16 ? Tb : nullptr))) return rc;  // tmp = M x
+    const bool first_is_last = order <= 2;
+    {
+      FinalOut fo{first_is_last ? base : nullptr, scale_dt, finf, finb};
+      EpiFirst<XT> epi{coef, Tx, xf, ring[0], ringb[0], conv, fo, ld, c[0], c[1]};
+      if ((rc = spmm_run<XT>(ctx, R, g->plan, Tx, ld, ld, epi, launches))) return rc;
+    }
+    const float* l0 = xf;
+    int j1 = 0;
+    for (int k = 2; k < order; ++k) {
+      const int j2 = (j1 + 1) % 3;
+      if ((rc = apply_m(op(ring[j1], ringb[j1]), kBF16 ? nullptr : Tf, kBF16 ? Tb : nullptr))) return rc;
+      const bool last = k == order - 1;
+      FinalOut fo{last ? base : nullptr, scale_dt, finf, finb};
+      EpiStep<XT> epi{coef, Tx, l0, ring[j1], nullptr, ring[j2], ringb[j2], conv, fo, ld, c[k]};
+      if ((rc = spmm_run<XT>(ctx, R, g->plan, Tx, ld, ld, epi, launches))) return rc;
+      l0 = ring[j1];
+      j1 = j2;
+    }
+    return LNE_OK;
+  }
+};
+
+template <typename XT>
+int setup_filter(lne_ctx* ctx, lne_graph* g, const lne_propagate_params* p, Bufs& B, int* launches, Filter<XT>& F,
+                 float4** coef_out) {
+  const int64_t n = g->n;
+  float4* coef = nullptr;
+  int rc;
+  if ((rc = B.get(&coef, n, "operator coefficients"))) return rc;
+  k_op_coef<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(g->vdata, n, (float)p->mu, coef);
+  *launches += 1;
+  F = Filter<XT>{ctx, g, GraphRows{g->vdata, g->nbrs}, n, pad_ld(p->dim), coef, launches, &B};
+  *coef_out = coef;
+  return LNE_OK;
+}
+
 template <typename XT>
 int propagate_impl(lne_ctx* ctx, lne_graph* g, const lne_propagate_params* p, const float* d_a, float* d_y,
                    float* d_a_out, lne_propagate_stats* stats) {
@@ -274,81 +437,33 @@ int propagate_impl(lne_ctx* ctx, lne_graph* g, const lne_propagate_params* p, co
   const int64_t n = g->n;
   const int d = (int)p->dim;
   const int64_t ld = pad_ld(d);
-  const int order = p->order;
   cudaStream_t st = ctx->stream;
   int launches = 0;
   std::vector<float> c;
-  chebyshev_coeffs(order, p->s, c);
+  chebyshev_coeffs(p->order, p->s, c);
   Bufs B(ctx);
-  float2* coef = nullptr;
-  float *A = nullptr, *conv = nullptr, *Tf = nullptr, *Af = nullptr;
-  float* ring[3] = {nullptr, nullptr, nullptr};            // Chebyshev vectors, FP32
-  __nv_bfloat16* ringb[3] = {nullptr, nullptr, nullptr};   // their BF16 copies (BF16 form)
-  __nv_bfloat16 *Ab = nullptr, *Tb = nullptr, *Afb = nullptr;
-  const size_t sz = (size_t)n * ld;
-  const int nring = order > 2 ? 3 : 1;
+  Filter<XT> F;
+  float4* coef = nullptr;
   int rc;
-  if ((rc = B.get(&coef, n, "operator coefficients")) || (rc = B.get(&A, sz, "a")) ||
-      (rc = B.get(&conv, sz, "conv")) || (rc = B.get(&Af, sz, "a - conv")))
-    return rc;
-  for (int i = 0; i < nring; ++i)
-    if ((rc = B.get(&ring[i], sz, "Chebyshev vector"))) return rc;
-  if (kBF16) {
-    if ((rc = B.get(&Ab, sz, "a bf16")) || (rc = B.get(&Tb, sz, "tmp bf16")) || (rc = B.get(&Afb, sz, "a - conv bf16")))
-      return rc;
-    for (int i = 0; i < nring; ++i)
-      if ((rc = B.get(&ringb[i], sz, "Chebyshev vector bf16"))) return rc;
-  } else {
-    if ((rc = B.get(&Tf, sz, "tmp"))) return rc;
-  }
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
   cudaEventRecord(ev0, st);
-  k_op_coef<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g->vdata, n, (float)p->mu, coef);
+  if ((rc = setup_filter<XT>(ctx, g, p, B, &launches, F, &coef))) return rc;
+  float *A = nullptr, *Af = nullptr;
+  __nv_bfloat16 *Ab = nullptr, *Afb = nullptr;
+  const size_t sz = (size_t)n * ld;
+  if ((rc = B.get(&A, sz, "a")) || (rc = B.get(&Af, sz, "a - conv"))) return rc;
+  if (kBF16 && ((rc = B.get(&Ab, sz, "a bf16")) || (rc = B.get(&Afb, sz, "a - conv bf16")))) return rc;
   const unsigned pg = (unsigned)std::min<int64_t>((n * ld + 255) / 256, (int64_t)ctx->num_sms * 32);
   k_pad_copy<<<pg, 256, 0, st>>>(d_a, n, d, A, ld, Ab);
-  launches += 2;
-  GraphRows R{g->vdata, g->nbrs};
-  const XT* Xa = kBF16 ? (const XT*)Ab : (const XT*)A;
-  XT* Tx = kBF16 ? (XT*)Tb : (XT*)Tf;
-  // tmp = M a
+  launches += 1;
+  // a - conv, then y = (A + I)(a - conv)
+  if ((rc = F.run(A, Ab, p->order, c, A, false, Af, Afb))) return rc;
   {
-    EpiApplyM<XT> epi{coef, Xa, ld, kBF16 ? nullptr : Tf, kBF16 ? Tb : nullptr};
-    if ((rc = spmm_run<XT>(ctx, R, g->plan, Xa, ld, ld, epi, &launches))) return rc;
-  }
-  // Lx1 = 0.5 M tmp - a; conv = c0 a + c1 Lx1 (and a - conv when order <= 2)
-  const bool first_is_last = order <= 2;
-  {
-    EpiFirst<XT> epi{coef, Tx, A, ring[0], ringb[0], conv, first_is_last ? Af : nullptr,
-                     first_is_last ? Afb : nullptr, ld, c[0], c[1]};
-    if ((rc = spmm_run<XT>(ctx, R, g->plan, Tx, ld, ld, epi, &launches))) return rc;
-  }
-  // Lx0 = a (never overwritten), Lx1 = ring[0]; each order writes Lx2 into
-  // the ring slot that holds neither Lx0 nor Lx1.
-  const float* l0 = A;
-  int j1 = 0;
-  for (int k = 2; k < order; ++k) {
-    const int j2 = (j1 + 1) % 3;
-    const XT* X1 = kBF16 ? (const XT*)ringb[j1] : (const XT*)ring[j1];
-    {
-      EpiApplyM<XT> epi{coef, X1, ld, kBF16 ? nullptr : Tf, kBF16 ? Tb : nullptr};
-      if ((rc = spmm_run<XT>(ctx, R, g->plan, X1, ld, ld, epi, &launches))) return rc;
-    }
-    const bool last = k == order - 1;
-    {
-      EpiStep<XT> epi{coef, Tx, l0, ring[j1], ring[j2], ringb[j2], conv, A, last ? Af : nullptr,
-                      last ? Afb : nullptr, ld, c[k]};
-      if ((rc = spmm_run<XT>(ctx, R, g->plan, Tx, ld, ld, epi, &launches))) return rc;
-    }
-    l0 = ring[j1];
-    j1 = j2;
-  }
-  // y = (A + I)(a - conv)
-  {
-    const XT* Xf = kBF16 ? (const XT*)Afb : (const XT*)Af;
+    const XT* Xf = F.op(Af, Afb);
     EpiAPlusI<XT> epi{Xf, ld, d_y, d, d};
-    if ((rc = spmm_run<XT>(ctx, R, g->plan, Xf, ld, ld, epi, &launches))) return rc;
+    if ((rc = spmm_run<XT>(ctx, F.R, g->plan, Xf, ld, ld, epi, &launches))) return rc;
   }
   if (d_a_out) {
     k_unpad_copy<<<pg, 256, 0, st>>>(Af, ld, n, d, d_a_out);
@@ -361,7 +476,156 @@ int propagate_impl(lne_ctx* ctx, lne_graph* g, const lne_propagate_params* p, co
     memset(stats, 0, sizeof(*stats));
     cudaEventElapsedTime(&stats->ms_total, ev0, ev1);
     stats->kernel_launches = launches;
-    stats->spmm_calls = 2 * (order > 2 ? order - 1 : 1) + 1;
+    stats->spmm_calls = 2 * (p->order > 2 ? p->order - 1 : 1) + 1;
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  return LNE_OK;
+}
+
+// Derivatives of the reference's weights with respect to s:
+// c_0 = I0(s), c_k = 2 (-1)^k I_k(s);  I0' = I1, I_k' = (I_{k-1} + I_{k+1}) / 2.
+void chebyshev_coeffs_ds(int order, double s, std::vector<double>& dc) {
+  const double sf = (double)(float)s;
+  dc.assign(order > 2 ? order : 2, 0.0);
+  dc[0] = bessel_i(1, sf);
+  for (int k = 1; k < (int)dc.size(); ++k)
+    dc[k] = ((k & 1) ? -1.0 : 1.0) * (bessel_i(k - 1, sf) + bessel_i(k + 1, sf));
+}
+
+template <typename XT>
+int adjoint_impl(lne_ctx* ctx, lne_graph* g, const lne_propagate_params* p, const float* d_a, const float* d_gy,
+                 float* d_ga, double* h_dmu, double* h_ds, lne_propagate_stats* stats) {
+  constexpr bool kBF16 = sizeof(XT) == 2;
+  const int64_t n = g->n;
+  const int d = (int)p->dim;
+  const int64_t ld = pad_ld(d);
+  const int order = p->order;
+  cudaStream_t st = ctx->stream;
+  int launches = 0;
+  std::vector<float> c;
+  chebyshev_coeffs(order, p->s, c);
+  Bufs B(ctx);
+  Filter<XT> F;
+  float4* coef = nullptr;
+  int rc;
+  cudaEvent_t ev0, ev1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  cudaEventRecord(ev0, st);
+  if ((rc = setup_filter<XT>(ctx, g, p, B, &launches, F, &coef))) return rc;
+  const size_t sz = (size_t)n * ld;
+  const int64_t total = (int64_t)sz;
+  float *G = nullptr, *H = nullptr, *Bf = nullptr, *GA = nullptr;
+  __nv_bfloat16 *Gb = nullptr, *Bb = nullptr;
+  if ((rc = B.get(&G, sz, "g")) || (rc = B.get(&H, sz, "h")) || (rc = B.get(&Bf, sz, "b")) ||
+      (rc = B.get(&GA, sz, "grad a")))
+    return rc;
+  if (kBF16 && ((rc = B.get(&Gb, sz, "g bf16")) || (rc = B.get(&Bb, sz, "b bf16")))) return rc;
+  const unsigned pg = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 32);
+  k_pad_copy<<<pg, 256, 0, st>>>(d_gy, n, d, G, ld, Gb);
+  launches += 1;
+  // h = (A + I) g, b = D~^-1 h
+  {
+    const XT* Gx = F.op(G, Gb);
+    EpiAdjInit<XT> epi{coef, Gx, ld, H, Bf, Bb};
+    if ((rc = spmm_run<XT>(ctx, F.R, g->plan, Gx, ld, ld, epi, &launches))) return rc;
+  }
+  // grad a = h - D~ sum_k c_k T_k(X) b      (M^T = D~ M D~^-1)
+  if ((rc = F.run(Bf, Bb, order, c, H, true, GA, nullptr))) return rc;
+  if (d_ga) {
+    k_unpad_copy<<<pg, 256, 0, st>>>(GA, ld, n, d, d_ga);
+    launches += 1;
+  }
+  if (h_dmu || h_ds) {
+    // Forward pass on a with the mu-tangent:  T'_1 = -M a,
+    // T'_{k+1} = M(M T'_k) - 2 T'_k - T'_{k-1} - 2 M T_k;  dots with h.
+    const int K = order > 2 ? order : 2;
+    double* partial = nullptr;
+    if ((rc = B.get(&partial, (size_t)2 * K * kDotBlocks, "dot partials"))) return rc;
+    LNE_CUDA_TRY(cudaMemsetAsync(partial, 0, sizeof(double) * 2 * K * kDotBlocks, st));
+    auto dot = [&](int slot, const float* x) {
+      k_dot_partial<<<kDotBlocks, 256, 0, st>>>(H, x, total, partial + (int64_t)slot * kDotBlocks);
+      launches += 1;
+    };
+    float *A = nullptr, *Tm = nullptr;  // a, and M T_k (FP32, kept for the tangent)
+    __nv_bfloat16 *Ab = nullptr, *Tmb = nullptr;
+    float* T[3];
+    float* Tp[3];
+    __nv_bfloat16* Tb[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16* Tpb[3] = {nullptr, nullptr, nullptr};
+    float* Tpm = nullptr;  // M T'_k
+    __nv_bfloat16* Tpmb = nullptr;
+    if ((rc = B.get(&A, sz, "a")) || (rc = B.get(&Tm, sz, "M T")) || (rc = B.get(&Tpm, sz, "M T'"))) return rc;
+    for (int i = 0; i < 3; ++i)
+      if ((rc = B.get(&T[i], sz, "T")) || (rc = B.get(&Tp[i], sz, "T'"))) return rc;
+    if (kBF16) {
+      if ((rc = B.get(&Ab, sz, "a bf16")) || (rc = B.get(&Tmb, sz, "M T bf16")) || (rc = B.get(&Tpmb, sz, "M T' bf16")))
+        return rc;
+      for (int i = 0; i < 3; ++i)
+        if ((rc = B.get(&Tb[i], sz, "T bf16")) || (rc = B.get(&Tpb[i], sz, "T' bf16"))) return rc;
+    }
+    k_pad_copy<<<pg, 256, 0, st>>>(d_a, n, d, A, ld, Ab);
+    launches += 1;
+    dot(0, A);  // <h, T_0>
+    // tmp = M a;  T_1 = 0.5 M tmp - a;  T'_1 = -tmp
+    if ((rc = F.apply_m(F.op(A, Ab), Tm, Tmb))) return rc;
+    {
+      FinalOut fo{nullptr, false, nullptr, nullptr};
+      EpiFirst<XT> epi{coef, F.op(Tm, Tmb), A, T[0], Tb[0], nullptr, fo, ld, 0.0f, 0.0f};
+      if ((rc = spmm_run<XT>(ctx, F.R, g->plan, F.op(Tm, Tmb), ld, ld, epi, &launches))) return rc;
+    }
+    k_scale_copy<<<pg, 256, 0, st>>>(Tm, total, -1.0f, Tp[0], Tpb[0]);
+    launches += 1;
+    dot(1, T[0]);
+    dot(K + 1, Tp[0]);
+    const float* t0 = A;      // T_{k-1}
+    const float* tp0 = nullptr;  // T'_{k-1} (T'_0 = 0)
+    int j1 = 0;
+    for (int k = 1; k + 1 < order; ++k) {
+      const int j2 = (j1 + 1) % 3;
+      // tmp = M T_k; T_{k+1} = M tmp - 2 T_k - T_{k-1}
+      if ((rc = F.apply_m(F.op(T[j1], Tb[j1]), Tm, Tmb))) return rc;
+      {
+        FinalOut fo{nullptr, false, nullptr, nullptr};
+        EpiStep<XT> epi{coef, F.op(Tm, Tmb), t0, T[j1], nullptr, T[j2], Tb[j2], nullptr, fo, ld, 0.0f};
+        if ((rc = spmm_run<XT>(ctx, F.R, g->plan, F.op(Tm, Tmb), ld, ld, epi, &launches))) return rc;
+      }
+      // tmp' = M T'_k; T'_{k+1} = M tmp' - 2 T'_k - T'_{k-1} - 2 M T_k
+      if ((rc = F.apply_m(F.op(Tp[j1], Tpb[j1]), Tpm, Tpmb))) return rc;
+      {
+        FinalOut fo{nullptr, false, nullptr, nullptr};
+        EpiStep<XT> epi{coef, F.op(Tpm, Tpmb), tp0, Tp[j1], Tm, Tp[j2], Tpb[j2], nullptr, fo, ld, 0.0f};
+        if ((rc = spmm_run<XT>(ctx, F.R, g->plan, F.op(Tpm, Tpmb), ld, ld, epi, &launches))) return rc;
+      }
+      dot(k + 1, T[j2]);
+      dot(K + k + 1, Tp[j2]);
+      t0 = T[j1];
+      tp0 = Tp[j1];
+      j1 = j2;
+    }
+    std::vector<double> hp((size_t)2 * K * kDotBlocks);
+    LNE_CUDA_TRY(cudaMemcpyAsync(hp.data(), partial, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    std::vector<double> dots(2 * K, 0.0);
+    for (int sidx = 0; sidx < 2 * K; ++sidx)
+      for (int b = 0; b < kDotBlocks; ++b) dots[sidx] += hp[(size_t)sidx * kDotBlocks + b];
+    std::vector<double> dc;
+    chebyshev_coeffs_ds(order, p->s, dc);
+    // only the terms the forward filter uses: k < max(order, 2)
+    double gs = 0.0, gmu = 0.0;
+    for (int k = 0; k < K; ++k) gs -= dc[k] * dots[k];
+    for (int k = 1; k < K; ++k) gmu -= (double)c[k] * dots[K + k];
+    if (h_ds) *h_ds = gs;
+    if (h_dmu) *h_dmu = gmu;
+  }
+  cudaEventRecord(ev1, st);
+  LNE_CUDA_TRY(cudaEventSynchronize(ev1));
+  LNE_CUDA_TRY(cudaGetLastError());
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    cudaEventElapsedTime(&stats->ms_total, ev0, ev1);
+    stats->kernel_launches = launches;
   }
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
@@ -385,6 +649,23 @@ extern "C" int lne_propagate(lne_ctx* ctx, const lne_graph* g, const lne_propaga
   if (rc) return rc;
   if (p->precision == LNE_PREC_BF16) return propagate_impl<__nv_bfloat16>(ctx, gm, p, d_a, d_y, d_a_out, stats);
   return propagate_impl<float>(ctx, gm, p, d_a, d_y, d_a_out, stats);
+}
+
+extern "C" int lne_propagate_adjoint(lne_ctx* ctx, const lne_graph* g, const lne_propagate_params* p,
+                                     const float* d_a, const float* d_gy, float* d_ga, double* h_dmu, double* h_ds,
+                                     lne_propagate_stats* stats) {
+  LNE_CHECK_ARG(ctx && g && p && d_gy, "lne_propagate_adjoint: NULL argument");
+  LNE_CHECK_ARG(d_a || (!h_dmu && !h_ds), "lne_propagate_adjoint: the parameter gradients need a");
+  LNE_CHECK_ARG(p->dim >= 1 && p->order >= 0, "lne_propagate_adjoint: bad dim/order");
+  LNE_CHECK_ARG(p->precision == LNE_PREC_FP32 || p->precision == LNE_PREC_BF16,
+                "lne_propagate_adjoint: bad precision");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  lne_graph* gm = const_cast<lne_graph*>(g);
+  int rc = build_plan_graph(ctx, gm);
+  if (rc) return rc;
+  if (p->precision == LNE_PREC_BF16)
+    return adjoint_impl<__nv_bfloat16>(ctx, gm, p, d_a, d_gy, d_ga, h_dmu, h_ds, stats);
+  return adjoint_impl<float>(ctx, gm, p, d_a, d_gy, d_ga, h_dmu, h_ds, stats);
 }
 
 extern "C" int lne_chebyshev_coefficients(int32_t order, double s, float* out) {

@@ -8,7 +8,9 @@
 // instead of Householder geqrf+orgqr; R has a positive diagonal, so Q is the
 // unique thin-QR factor with that sign convention.  The core SVD is a
 // one-sided FP64 Jacobi.  The Gaussian sketches come from a counter-based
-// generator (MKL's SFMT19937 stream cannot be reproduced without MKL).
+// generator (MKL's SFMT19937 stream cannot be reproduced without MKL); its
+// values are BF16-representable, so in the BF16 form the product A * Omega
+// reads a BF16 sketch with no loss.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -201,14 +203,13 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
   }
 
   // Q = qr(Y)
-  if ((rc = cholqr3(ctx, Y, T, n, ld, r, bf16 ? Xb : nullptr, &launches))) return rc;
+  if ((rc = cholqr3(ctx, Y, T, n, ld, r, nullptr, &launches))) return rc;
   cudaEventRecord(ev[2], st);
-  // B = A * Q
+  // B = A * Q.  Q is not BF16-representable (unlike the sketch), and a BF16
+  // copy of it costs about 1e-3 relative embedding error, so this product
+  // reads the FP32 Q in both forms.
   if ((rc = B.get(&Bm, (size_t)n * ld, "B"))) return rc;
-  if (bf16)
-    rc = spmm_store<__nv_bfloat16>(ctx, A, Xb, ld, (int)ld, Bm, &launches);
-  else
-    rc = spmm_store<float>(ctx, A, Y, ld, (int)ld, Bm, &launches);
+  rc = spmm_store<float>(ctx, A, Y, ld, (int)ld, Bm, &launches);
   if (rc) return rc;
   cudaEventRecord(ev[3], st);
   // Z = qr(B * P); Y holds Z from here on

@@ -32,6 +32,7 @@ static constexpr unsigned long long kEmptyKey = ~0ULL;
 // requested size) a linear-probe run this long only occurs in a table that
 // is essentially full, so the status is the same and the wait is bounded.
 static constexpr uint32_t kMaxProbes = 1u << 16;
+static constexpr unsigned kFullMask = 0xffffffffu;
 
 struct SampleArgs {
   uint64_t seed;
@@ -76,86 +77,141 @@ __device__ __forceinline__ bool table_insert_add(Slot* __restrict__ T, uint64_t 
   return false;
 }
 
-// One thread per directed CSR entry (u, v): LightNE/PathEmbed.h:128-171.
-// The per-edge generator state is a chain (every draw advances it), so the
-// samples of one edge are sequential; the loop below is a flat state machine
-// that advances one walk step per iteration so the lanes of a warp stay in
-// step regardless of each sample's walk length.
+// Path sampler, one thread per directed CSR entry (u, v), over the entries
+// [e0, e1): LightNE/PathEmbed.h:128-171.  The per-edge generator state is a
+// chain (every draw advances it), so the samples of one edge are sequential;
+// the loop is a flat state machine that advances one walk step per
+// iteration so the lanes of a warp stay in step whatever each sample's walk
+// length.  Emitted pair keys (and weights with -sample 1) are staged per
+// warp in shared memory and written to the sample buffer 32 at a time, so
+// the walk never waits on the pair table; k_insert adds them to the table.
+static constexpr int kWalkThreads = 256;
+static constexpr int kQueue = 64;  // staged keys per warp
+
 template <bool SAMPLE>
-__global__ void __launch_bounds__(256) k_sample(const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs,
-                                                const uint32_t* __restrict__ src, int64_t m_dir, SampleArgs a,
-                                                Slot* __restrict__ table, int* flags,
-                                                unsigned long long* __restrict__ emitted_total) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long emitted = 0;
-  if (e < m_dir) {
-    const uint32_t u = __ldg(src + e), v = __ldg(nbrs + e);
-    uint64_t s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
-    uint64_t todo = a.exp_rv;
-    if (a.use_frac) {
-      todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
-    }
-    double p = 1.0, ipw = 1.0;
+__global__ void __launch_bounds__(kWalkThreads) k_walk(const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs,
+                                                      const uint32_t* __restrict__ src, int64_t e0, int64_t e1,
+                                                      SampleArgs a, unsigned long long* __restrict__ out_keys,
+                                                      double* __restrict__ out_w,
+                                                      unsigned long long* __restrict__ out_count, uint64_t out_cap,
+                                                      int* flags) {
+  __shared__ unsigned long long qk[kWalkThreads / 32][kQueue];
+  __shared__ double qw[SAMPLE ? kWalkThreads / 32 : 1][SAMPLE ? kQueue : 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t e = e0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool active = e < e1;
+  uint32_t u = 0, v = 0, cur = 0, x = 0, left1 = 0, left2 = 0;
+  uint64_t s = 0, todo = 0;
+  double p = 1.0, ipw = 1.0;
+  int phase = 0;  // 0: start a sample, 1: walking from u, 2: walking from v
+  if (active) {
+    u = __ldg(src + e);
+    v = __ldg(nbrs + e);
+    s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
+    todo = a.exp_rv;
+    if (a.use_frac) todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
     if (SAMPLE) {
       const double du = (double)__ldg(&vd[u].deg), dv = (double)__ldg(&vd[v].deg);
       p = __dmul_rn(__dadd_rn(__ddiv_rn(1.0, du), __ddiv_rn(1.0, dv)), a.logn);
       p = p < 1.0 ? p : 1.0;
       ipw = __ddiv_rn(1.0, p);
     }
-    uint32_t cur = u, x = 0, left1 = 0, left2 = 0;
-    int phase = 0;  // 0: start a sample, 1: walking from u, 2: walking from v
-    uint32_t since_check = 0;
-    while (true) {
+  }
+  int qlen = 0;  // warp-uniform
+  while (__any_sync(kFullMask, active)) {
+    bool emit = false;
+    unsigned long long key = 0;
+    if (active) {
       if (phase == 0) {
-        if (todo == 0) break;
-        if (++since_check == 32) {
-          since_check = 0;
-          if (table_full(flags)) break;
+        if (todo == 0) {
+          active = false;
+        } else {
+          --todo;
+          bool take = true;
+          if (SAMPLE) take = map_uint64(rng_draw(s)) < p;
+          if (take) {
+            const uint64_t r = rng_draw(s) % a.walk_len + 1;
+            const uint64_t k = rng_draw(s) % r + 1;
+            left1 = (uint32_t)(k - 1);
+            left2 = (uint32_t)(r - k);
+            cur = u;
+            phase = 1;
+          }
         }
-        --todo;
-        if (SAMPLE) {
-          const double eff = map_uint64(rng_draw(s));
-          if (!(eff < p)) continue;
+      }
+      if (active && phase != 0) {
+        if (phase == 1 && left1 == 0) {
+          x = cur;
+          cur = v;
+          phase = 2;
         }
-        const uint64_t r = rng_draw(s) % a.walk_len + 1;
-        const uint64_t k = rng_draw(s) % r + 1;
-        left1 = (uint32_t)(k - 1);
-        left2 = (uint32_t)(r - k);
-        cur = u;
-        phase = 1;
+        if (phase == 2 && left2 == 0) {
+          const uint32_t lo = x < cur ? x : cur, hi = x < cur ? cur : x;
+          key = ((uint64_t)lo << 32) + (uint64_t)hi;
+          emit = true;
+          phase = 0;
+        } else {
+          const uint4 raw = __ldg(reinterpret_cast<const uint4*>(vd + cur));
+          if (raw.y == 0) {
+            active = false;  // unreachable for a validated (symmetric) graph
+          } else {
+            const uint32_t idx = gm_mod(rng_draw(s), raw.y, ((uint64_t)raw.w << 32) | raw.z);
+            cur = __ldg(nbrs + raw.x + idx);
+            if (phase == 1) --left1; else --left2;
+          }
+        }
       }
-      if (phase == 1 && left1 == 0) {
-        x = cur;
-        cur = v;
-        phase = 2;
+    }
+    // stage this iteration's keys in the warp queue
+    const unsigned em = __ballot_sync(kFullMask, emit);
+    if (emit) {
+      const int pos = qlen + __popc(em & ((1u << lane) - 1));
+      qk[wid][pos] = key;
+      if (SAMPLE) qw[wid][pos] = ipw;
+    }
+    qlen += __popc(em);
+    __syncwarp();
+    if (qlen >= 32) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(out_count, 32ULL);
+      base = __shfl_sync(kFullMask, base, 0);
+      if (base + 32 <= out_cap) {
+        out_keys[base + lane] = qk[wid][lane];
+        if (SAMPLE) out_w[base + lane] = qw[wid][lane];
+      } else if (lane == 0) {
+        atomicExch(flags + kFlagSortOverflow, 1);
       }
-      if (phase == 2 && left2 == 0) {
-        const uint32_t lo = x < cur ? x : cur, hi = x < cur ? cur : x;
-        if (!table_insert_add<SAMPLE>(table, a.mask, ((uint64_t)lo << 32) + (uint64_t)hi, ipw, flags)) break;
-        ++emitted;
-        phase = 0;
-        continue;
+      __syncwarp();
+      if (lane < qlen - 32) {
+        qk[wid][lane] = qk[wid][32 + lane];
+        if (SAMPLE) qw[wid][lane] = qw[wid][32 + lane];
       }
-      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(vd + cur));
-      const uint32_t doff = raw.x, ddeg = raw.y;
-      const uint64_t dmagic = ((uint64_t)raw.w << 32) | raw.z;
-      if (ddeg == 0) break;  // unreachable for a validated (symmetric) graph
-      const uint32_t idx = gm_mod(rng_draw(s), ddeg, dmagic);
-      cur = __ldg(nbrs + doff + idx);
-      if (phase == 1)
-        --left1;
-      else
-        --left2;
+      qlen -= 32;
+      __syncwarp();
     }
   }
-  // block total of emitted samples
-  for (int o = 16; o > 0; o >>= 1) emitted += __shfl_down_sync(0xffffffffu, emitted, o);
-  __shared__ unsigned long long bsum;
-  if (threadIdx.x == 0) bsum = 0;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0 && emitted) atomicAdd(&bsum, emitted);
-  __syncthreads();
-  if (threadIdx.x == 0 && bsum) atomicAdd(emitted_total, bsum);
+  if (qlen > 0) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(out_count, (unsigned long long)qlen);
+    base = __shfl_sync(kFullMask, base, 0);
+    if (lane < qlen) {
+      if (base + lane < out_cap) {
+        out_keys[base + lane] = qk[wid][lane];
+        if (SAMPLE) out_w[base + lane] = qw[wid][lane];
+      } else {
+        atomicExch(flags + kFlagSortOverflow, 1);
+      }
+    }
+  }
+}
+
+// Adds every staged key to the pair table (par_table::insert_add).
+template <bool WEIGHTED>
+__global__ void k_insert(const unsigned long long* __restrict__ keys, const double* __restrict__ w, uint64_t count,
+                         Slot* __restrict__ table, uint64_t mask, int* flags) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (!table_insert_add<WEIGHTED>(table, mask, keys[i], WEIGHTED ? w[i] : 1.0, flags)) return;
+  }
 }
 
 // Sum of weights and number of occupied slots (PathEmbed.h:175-188).  Counts
@@ -224,23 +280,51 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 // Trunc-log map (PathEmbed.h:203-218) fused with the per-row counts of the
 // CSR build (PathEmbed.h:226-288).  Kept slots get the float bits of the
 // log value in `val`; dropped slots become empty.
+//
+// Counts (-sample 0): adj = ((w * factor) / d_u) / d_v is reproduced
+// exactly by integer arithmetic (the reference's three double roundings),
+// adj > 1 decides the keep test exactly, and log(adj) is evaluated in
+// double-float; only values whose narrowing to float the double-float
+// result cannot decide go through FP64 (trunc_log_value).  Weights
+// (-sample 1) take the FP64 path throughout.
 template <bool WEIGHTED>
-__global__ void k_trunclog(Slot* __restrict__ T, uint64_t cap, const Vertex* __restrict__ vd, double factor,
-                           int upper, unsigned long long* __restrict__ rowcnt,
-                           unsigned long long* __restrict__ kept_total) {
+__global__ void __launch_bounds__(256) k_trunclog(Slot* __restrict__ T, uint64_t cap, const Vertex* __restrict__ vd,
+                                                  double factor, int upper, const LogTable* __restrict__ ltab,
+                                                  unsigned long long* __restrict__ rowcnt,
+                                                  unsigned long long* __restrict__ kept_total) {
+  __shared__ LogTable tab;
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+    tab.log_hi[i] = ltab->log_hi[i];
+    tab.log_lo[i] = ltab->log_lo[i];
+    tab.inv_hi[i] = ltab->inv_hi[i];
+    tab.inv_lo[i] = ltab->inv_lo[i];
+  }
+  __syncthreads();
+  const XDouble xf = xd_from_double(factor);
   unsigned long long kept = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
     const unsigned long long key = T[i].key;
     if (key == kEmptyKey) continue;
     const uint32_t u = (uint32_t)(key >> 32), v = (uint32_t)key;
-    const double du = (double)__ldg(&vd[u].deg), dv = (double)__ldg(&vd[v].deg);
+    const uint4 ru = __ldg(reinterpret_cast<const uint4*>(vd + u));
+    const uint4 rv = __ldg(reinterpret_cast<const uint4*>(vd + v));
     const unsigned long long raw = T[i].val;
-    double w = WEIGHTED ? __longlong_as_double((long long)raw) : __ull2double_rn(raw);
-    if (u == v) w = __dmul_rn(w, 2.0);
-    const double adj = __ddiv_rn(__ddiv_rn(__dmul_rn(w, factor), du), dv);
-    const double L = trunc_log_value(adj);
-    if (L > 0.0) {
-      const float f = __double2float_rn(L);
+    float f = 0.0f;
+    bool keep;
+    if (WEIGHTED) {
+      double w = __longlong_as_double((long long)raw);
+      if (u == v) w = __dmul_rn(w, 2.0);
+      const double adj = __ddiv_rn(__ddiv_rn(__dmul_rn(w, factor), (double)ru.y), (double)rv.y);
+      const double L = trunc_log_value(adj);
+      keep = L > 0.0;
+      if (keep) f = __double2float_rn(L);
+    } else {
+      const XDouble adj = trunc_log_adj(raw, u == v, xf, ru.y, ((uint64_t)ru.w << 32) | ru.z, rv.y,
+                                        ((uint64_t)rv.w << 32) | rv.z);
+      keep = adj.e > -52 || (adj.e == -52 && adj.m > (1ull << 52));  // adj > 1  <=>  log(adj) > 0
+      if (keep && !float_of_log_fast(log_df(adj, tab), &f)) f = __double2float_rn(trunc_log_value(xd_to_double(adj)));
+    }
+    if (keep) {
       T[i].val = (unsigned long long)__float_as_uint(f);
       atomicAdd(&rowcnt[u], 1ULL);
       if (!upper && u != v) atomicAdd(&rowcnt[v], 1ULL);
@@ -552,12 +636,44 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   a.use_frac = frac > 0.0000000001 ? 1 : 0;
 
   cudaEventRecord(ev.e[0], st);
-  const unsigned sblocks = (unsigned)((m_dir + 255) / 256);
-  if (p->sample)
-    k_sample<true><<<sblocks, 256, 0, st>>>(g->vdata, g->nbrs, g->src, m_dir, a, table, ctx->d_flags, counters);
-  else
-    k_sample<false><<<sblocks, 256, 0, st>>>(g->vdata, g->nbrs, g->src, m_dir, a, table, ctx->d_flags, counters);
+  // Sample buffer: at most exp_rv + 1 samples per directed entry; the edge
+  // range is processed in batches that fit the buffer.
+  const uint64_t per_edge = (uint64_t)exp_rv + 1;
+  const uint64_t want_keys = per_edge * (uint64_t)m_dir;
+  const uint64_t max_keys = (uint64_t)1 << 30;  // 8 GiB of keys per batch
+  const uint64_t buf_keys = want_keys < max_keys ? want_keys : max_keys;
+  const int64_t edges_per_batch = (int64_t)std::max<uint64_t>(1, buf_keys / per_edge);
+  unsigned long long* keys = nullptr;
+  double* wts = nullptr;
+  if ((rc = S.get((void**)&keys, sizeof(unsigned long long) * buf_keys, "sample buffer"))) return rc;
+  if (p->sample && (rc = S.get((void**)&wts, sizeof(double) * buf_keys, "sample weights"))) return rc;
+  int launches_sample = 0;
+  unsigned long long emitted_total = 0;
+  for (int64_t eb = 0; eb < m_dir; eb += edges_per_batch) {
+    const int64_t ee = std::min<int64_t>(m_dir, eb + edges_per_batch);
+    LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 8, st));
+    const unsigned wblocks = (unsigned)((ee - eb + kWalkThreads - 1) / kWalkThreads);
+    if (p->sample)
+      k_walk<true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts, counters,
+                                                     buf_keys, ctx->d_flags);
+    else
+      k_walk<false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts, counters,
+                                                      buf_keys, ctx->d_flags);
+    unsigned long long got = 0;
+    LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (got > buf_keys) got = buf_keys;  // overflow is flagged and reported below
+    const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 32);
+    if (p->sample)
+      k_insert<true><<<iblocks, 256, 0, st>>>(keys, wts, got, table, cap - 1, ctx->d_flags);
+    else
+      k_insert<false><<<iblocks, 256, 0, st>>>(keys, wts, got, table, cap - 1, ctx->d_flags);
+    emitted_total += got;
+    launches_sample += 2;
+  }
   LNE_CUDA_TRY(cudaGetLastError());
+  S.release(keys);
+  if (wts) S.release(wts);
   cudaEventRecord(ev.e[1], st);
 
   const unsigned tgrid = grid_for((int64_t)cap, 256, (int64_t)ctx->num_sms * 16);
@@ -568,6 +684,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     k_table_sum<false><<<sgrid, 256, 0, st>>>(table, cap, counters + 1, counters + 2, wsum);
   k_sum_blocks<<<1, 32, 0, st>>>(wsum, sgrid, wsum + sum_blocks);
   unsigned long long h_cnt[3] = {0, 0, 0};
+  LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 8, st));
   double h_w = 0.0;
   int h_flags[kFlagWords];
   LNE_CUDA_TRY(cudaMemcpyAsync(h_cnt, counters, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
@@ -575,6 +692,11 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   LNE_CUDA_TRY(cudaMemcpyAsync(h_flags, ctx->d_flags, sizeof(h_flags), cudaMemcpyDeviceToHost, st));
   LNE_CUDA_TRY(cudaStreamSynchronize(st));
   LNE_CUDA_TRY(cudaGetLastError());
+  h_cnt[0] = emitted_total;
+  if (h_flags[kFlagSortOverflow]) {
+    set_error("lne_sparsify: sample buffer overflow (internal sizing error)");
+    return LNE_ERR_UNSUPPORTED;
+  }
   if (h_flags[kFlagTableFull]) {
     char buf[256];
     snprintf(buf, sizeof(buf),
@@ -597,9 +719,11 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   if ((rc = S.get(&scan_tmp, scan_tmp_bytes(n), "scan scratch"))) { dfree(ctx, row_ptr); return rc; }
   LNE_CUDA_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(unsigned long long) * n, st));
   if (p->sample)
-    k_trunclog<true><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper, rowcnt, counters + 3);
+    k_trunclog<true><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper,
+                                            (const LogTable*)ctx->log_table, rowcnt, counters + 3);
   else
-    k_trunclog<false><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper, rowcnt, counters + 3);
+    k_trunclog<false><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper,
+                                             (const LogTable*)ctx->log_table, rowcnt, counters + 3);
   cudaEventRecord(ev.e[2], st);
   scan_exclusive_i64((const int64_t*)rowcnt, row_ptr, n, scan_tmp, st);
   int64_t nnz = 0;
@@ -635,7 +759,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     return rc;
   }
   LNE_CUDA_TRY(cudaMemsetAsync(cls_cnt, 0, sizeof(unsigned long long) * 16, st));
-  int launches = 15;  // 9 before this point, 6 sort launches below
+  int launches = 13 + launches_sample;  // 7 + walk/insert before this point, 6 sort launches below
   k_classify_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(row_ptr, n, packed, col, val, cls_cnt, cls_rows, n,
                                                                segs);
   const int64_t sms = ctx->num_sms;

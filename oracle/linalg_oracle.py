@@ -81,18 +81,21 @@ def randsvd(A: sp.csr_matrix, omega: np.ndarray, P: np.ndarray, dim: int, normal
     return u_sigma_root(matU, S, dim, normalize), S
 
 
-def operator_values(deg: np.ndarray, mu: float):
+def operator_values(deg: np.ndarray, mu: float, narrow: bool = True):
     """Per-row diagonal and off-diagonal values of M as the reference stores
-    them (floats computed in double, SpectralPropagation.h:62-72)."""
+    them (floats computed in double, SpectralPropagation.h:62-72); with
+    narrow=False the exact real-valued operator (for derivatives)."""
+    dt = (deg + 1).astype(np.float64)
+    if not narrow:
+        return 1.0 - mu - 1.0 / dt, -1.0 / dt
     mu_f = float(np.float32(mu))
-    dt = (deg + 1).astype(np.float32).astype(np.float64)
     diag = (1.0 - mu_f - 1.0 / dt).astype(np.float32).astype(np.float64)
     off = (-1.0 / dt).astype(np.float32).astype(np.float64)
     return diag, off
 
 
 def chebyshev_coefficients(order: int, s: float, narrow: bool = True) -> np.ndarray:
-    s_f = float(np.float32(s))
+    s_f = float(np.float32(s)) if narrow else float(s)
     c = np.zeros(max(order, 2))
     c[0] = ss.iv(0, s_f)
     c[1] = -2.0 * ss.iv(1, s_f)
@@ -102,16 +105,17 @@ def chebyshev_coefficients(order: int, s: float, narrow: bool = True) -> np.ndar
 
 
 def propagate(offsets: np.ndarray, nbrs: np.ndarray, a: np.ndarray, order: int = 10, mu: float = 0.2,
-              s: float = 0.5):
-    """chebyshev_expansion up to tmp = (A + I)(a - conv), in FP64.
-    Returns (y, a - conv)."""
+              s: float = 0.5, narrow: bool = True):
+    """chebyshev_expansion up to tmp = (A + I)(a - conv), in FP64.  With
+    narrow=False mu, s, M and the weights are not rounded to float (the
+    real-valued map, for finite differences).  Returns (y, a - conv)."""
     n = offsets.size - 1
     deg = np.diff(offsets)
-    diag, off = operator_values(deg, mu)
+    diag, off = operator_values(deg, mu, narrow)
     rows = np.repeat(np.arange(n), deg)
     Adj = sp.csr_matrix((np.ones(nbrs.size), nbrs.astype(np.int64), offsets), shape=(n, n))
     M = (sp.diags(diag) + sp.diags(off) @ Adj).tocsr()
-    c = chebyshev_coefficients(order, s)
+    c = chebyshev_coefficients(order, s, narrow)
     a = a.astype(np.float64)
     Lx0 = a.copy()
     tmp = spmm64(M, a)
