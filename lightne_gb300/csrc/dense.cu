@@ -276,29 +276,43 @@ int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W) {
 }
 
 // ---------------------------------------------------------------------------
-// One-sided Jacobi SVD (Hestenes), FP64, one block.  Columns of the working
-// copy Wc (column-major) are rotated pairwise in round-robin order until
-// every pair is orthogonal to 1e-15 relative; singular values are the column
-// norms, left singular vectors the normalised columns.
+// One-sided Jacobi SVD (Hestenes), FP64.  Columns of the working copy Wc
+// (column-major, in global memory / L2) are rotated pairwise in round-robin
+// order until every pair is orthogonal to 1e-15 relative; singular values
+// are the column norms, left singular vectors the normalised columns.
+//
+// The sweeps run on one thread-block cluster (16 CTAs where the device
+// allows that size, else 8): each warp of the cluster takes pairs of the
+// current round-robin step, and a cluster barrier (release/acquire at
+// cluster scope) separates the steps.  Columns are read with ld.global.cg
+// so that no CTA sees a stale L1 line of a column another CTA rotated.
+// FP64 runs at 1/68 of the FP32 rate on this part, so one SM would spend
+// about 30 ms on a 138 x 138 core; 16 SMs share the work.
 // ---------------------------------------------------------------------------
-__global__ void k_jacobi(const double* __restrict__ C, int r, double* __restrict__ Wc, double* __restrict__ U,
-                         double* __restrict__ S, int* __restrict__ sweeps_out, int max_sweeps) {
-  __shared__ int rotated;
-  __shared__ int order[1024];
-  __shared__ double norms[1024];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int64_t t = threadIdx.x; t < (int64_t)r * r; t += blockDim.x) {
+__global__ void k_jacobi_init(const double* __restrict__ C, int r, double* __restrict__ Wc,
+                              int* __restrict__ rotated, int max_sweeps) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)r * r;
+       t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t / r), j = (int)(t % r);
     Wc[(int64_t)j * r + i] = C[t];
   }
-  __syncthreads();
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < max_sweeps; t += gridDim.x * blockDim.x) rotated[t] = 0;
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict__ Wc, int* __restrict__ rotated,
+                                                       int max_sweeps, int* __restrict__ sweeps_out) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;  // the grid is one cluster
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int rp = (r + 1) & ~1;  // even number of players (index r is a dummy when r is odd)
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
-    if (threadIdx.x == 0) rotated = 0;
-    __syncthreads();
     for (int s = 0; s < rp - 1; ++s) {
-      for (int pk = warp; pk < rp / 2; pk += nw) {
+      for (int pk = gw; pk < rp / 2; pk += nwarps) {
         int p, q;
         if (pk == 0) {
           p = rp - 1;
@@ -313,7 +327,7 @@ __global__ void k_jacobi(const double* __restrict__ C, int r, double* __restrict
         double* wq = Wc + (int64_t)q * r;
         double a = 0.0, b = 0.0, g = 0.0;
         for (int i = lane; i < r; i += 32) {
-          const double x = wp[i], y = wq[i];
+          const double x = __ldcg(wp + i), y = __ldcg(wq + i);
           a = fma(x, x, a);
           b = fma(y, y, b);
           g = fma(x, y, g);
@@ -328,19 +342,24 @@ __global__ void k_jacobi(const double* __restrict__ C, int r, double* __restrict
           const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
           const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
           for (int i = lane; i < r; i += 32) {
-            const double x = wp[i], y = wq[i];
+            const double x = __ldcg(wp + i), y = __ldcg(wq + i);
             wp[i] = c * x - sn * y;
             wq[i] = sn * x + c * y;
           }
-          if (lane == 0) rotated = 1;
+          if (lane == 0) rotated[sweep] = 1;
         }
       }
-      __syncthreads();
+      cluster_barrier();
     }
-    if (!rotated) break;
-    __syncthreads();
+    if (__ldcg(rotated + sweep) == 0) break;
   }
-  // norms and descending order
+  if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep + 1;
+}
+
+__global__ void k_jacobi_finish(int r, const double* __restrict__ Wc, double* __restrict__ U,
+                                double* __restrict__ S) {
+  __shared__ int order[1024];
+  __shared__ double norms[1024];
   for (int j = threadIdx.x; j < r; j += blockDim.x) {
     double s2 = 0.0;
     for (int i = 0; i < r; ++i) s2 = fma(Wc[(int64_t)j * r + i], Wc[(int64_t)j * r + i], s2);
@@ -360,7 +379,6 @@ __global__ void k_jacobi(const double* __restrict__ C, int r, double* __restrict
     U[t] = nrm > 0.0 ? Wc[(int64_t)j * r + i] / nrm : 0.0;
   }
   for (int jn = threadIdx.x; jn < r; jn += blockDim.x) S[jn] = norms[order[jn]];
-  if (threadIdx.x == 0) *sweeps_out = sweep + 1;
 }
 
 int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out) {
@@ -368,11 +386,49 @@ int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps
     set_error("jacobi_svd: rank above 1024 is not supported");
     return LNE_ERR_UNSUPPORTED;
   }
+  const int kMaxSweeps = 60;
   double* Wc = nullptr;
   int rc;
-  if ((rc = dalloc(ctx, (void**)&Wc, sizeof(double) * r * r + 16, "jacobi work"))) return rc;
-  int* d_sw = (int*)(Wc + (int64_t)r * r);
-  k_jacobi<<<1, 1024, 0, ctx->stream>>>(C, r, Wc, U, S, d_sw, 60);
+  if ((rc = dalloc(ctx, (void**)&Wc, sizeof(double) * r * r + sizeof(int) * (kMaxSweeps + 4), "jacobi work")))
+    return rc;
+  int* rotated = (int*)(Wc + (int64_t)r * r);
+  int* d_sw = rotated + kMaxSweeps;
+  k_jacobi_init<<<64, 256, 0, ctx->stream>>>(C, r, Wc, rotated, kMaxSweeps);
+  // one cluster: 16 CTAs if the device accepts that (non-portable) size
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = ctx->stream;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaErrorUnknown;
+  for (int cl : {16, 8}) {
+    if (cl == 16 && cudaFuncSetAttribute(k_jacobi_sweeps, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                        cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cfg.gridDim = dim3(cl, 1, 1);
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_jacobi_sweeps, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      continue;
+    }
+    e = cudaLaunchKernelEx(&cfg, k_jacobi_sweeps, r, Wc, rotated, kMaxSweeps, d_sw);
+    if (e == cudaSuccess) break;
+    cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    dfree(ctx, Wc);
+    set_error(std::string("jacobi_svd: cluster launch failed: ") + cudaGetErrorString(e));
+    return LNE_ERR_CUDA;
+  }
+  k_jacobi_finish<<<1, 1024, 0, ctx->stream>>>(r, Wc, U, S);
   int h = 0;
   LNE_CUDA_TRY(cudaMemcpyAsync(&h, d_sw, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

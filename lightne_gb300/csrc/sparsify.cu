@@ -36,7 +36,8 @@ static constexpr unsigned kFullMask = 0xffffffffu;
 
 struct SampleArgs {
   uint64_t seed;
-  uint64_t walk_len;
+  uint64_t walk_len;      // T (< 2^31)
+  uint64_t walk_magic;    // Granlund-Montgomery multiplier of T
   uint64_t exp_rv;
   double frac;
   double logn;
@@ -58,7 +59,7 @@ __global__ void k_table_init(Slot* __restrict__ T, uint64_t cap) {
 // key; a stale EMPTY is resolved by the compare-and-swap.
 template <bool WEIGHTED>
 __device__ __forceinline__ bool table_insert_add(Slot* __restrict__ T, uint64_t mask, uint64_t key,
-                                                 double w, int* flags) {
+                                                 double w, int* flags, unsigned long long cnt = 1ULL) {
   uint64_t h = hash64_2(key) & mask;
   for (uint32_t p = 0; p < kMaxProbes; ++p) {
     unsigned long long k = __ldcg(&T[h].key);
@@ -67,7 +68,7 @@ __device__ __forceinline__ bool table_insert_add(Slot* __restrict__ T, uint64_t 
       if (WEIGHTED)
         atomicAdd(reinterpret_cast<double*>(&T[h].val), w);
       else
-        atomicAdd(&T[h].val, 1ULL);
+        atomicAdd(&T[h].val, cnt);
       return true;
     }
     h = (h + 1) & mask;
@@ -79,17 +80,24 @@ __device__ __forceinline__ bool table_insert_add(Slot* __restrict__ T, uint64_t 
 
 // Path sampler, one thread per directed CSR entry (u, v), over the entries
 // [e0, e1): LightNE/PathEmbed.h:128-171.  The per-edge generator state is a
-// chain (every draw advances it), so the samples of one edge are sequential;
-// the loop is a flat state machine that advances one walk step per
-// iteration so the lanes of a warp stay in step whatever each sample's walk
-// length.  Emitted pair keys (and weights with -sample 1) are staged per
+// chain (every draw advances it), so the samples of one edge are sequential.
+// Every loop iteration makes exactly one draw (rand + next) and reduces it
+// modulo the divisor of the current phase with that divisor's
+// Granlund-Montgomery multiplier:
+//   [eff test (-sample 1)] -> r = rand % T + 1 -> k = rand % r + 1 ->
+//   k-1 steps from u, then r-k steps from v (rand % degree each)
+// so the lanes of a warp execute the same instructions whatever phase each
+// lane is in.  Emitted pair keys (and weights with -sample 1) are staged per
 // warp in shared memory and written to the sample buffer 32 at a time, so
 // the walk never waits on the pair table; k_insert adds them to the table.
 static constexpr int kWalkThreads = 256;
-static constexpr int kQueue = 64;  // staged keys per warp
+static constexpr int kQueue = 64;    // staged keys per warp
+static constexpr int kMaxRMagic = 64;  // multipliers of r = 1..64 kept in shared memory
+
+enum WalkPhase : int { kPhEff = 0, kPhR = 1, kPhK = 2, kPhW1 = 3, kPhW2 = 4 };
 
 template <bool SAMPLE>
-__global__ void __launch_bounds__(kWalkThreads) k_walk(const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs,
+__global__ void __launch_bounds__(kWalkThreads, 6) k_walk(const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs,
                                                       const uint32_t* __restrict__ src, int64_t e0, int64_t e1,
                                                       SampleArgs a, unsigned long long* __restrict__ out_keys,
                                                       double* __restrict__ out_w,
@@ -97,68 +105,120 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(const Vertex* __restrict_
                                                       int* flags) {
   __shared__ unsigned long long qk[kWalkThreads / 32][kQueue];
   __shared__ double qw[SAMPLE ? kWalkThreads / 32 : 1][SAMPLE ? kQueue : 1];
+  __shared__ unsigned long long rmag[kMaxRMagic + 1];
+  for (int i = threadIdx.x; i <= kMaxRMagic; i += blockDim.x) rmag[i] = gm_magic(i > 0 ? (uint32_t)i : 1u);
+  __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t e = e0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool active = e < e1;
-  uint32_t u = 0, v = 0, cur = 0, x = 0, left1 = 0, left2 = 0;
+  uint32_t u = 0, v = 0, cur = 0, x = 0, left1 = 0, left2 = 0, r = 0;
+  uint32_t cur_off = 0, div = 1;
+  uint64_t mag = 1;
+  uint4 vu = make_uint4(0, 1, 1, 0), vv = make_uint4(0, 1, 1, 0);
   uint64_t s = 0, todo = 0;
   double p = 1.0, ipw = 1.0;
-  int phase = 0;  // 0: start a sample, 1: walking from u, 2: walking from v
+  int phase = SAMPLE ? kPhEff : kPhR;
   if (active) {
     u = __ldg(src + e);
     v = __ldg(nbrs + e);
+    vu = __ldg(reinterpret_cast<const uint4*>(vd + u));
+    vv = __ldg(reinterpret_cast<const uint4*>(vd + v));
     s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
     todo = a.exp_rv;
     if (a.use_frac) todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
     if (SAMPLE) {
-      const double du = (double)__ldg(&vd[u].deg), dv = (double)__ldg(&vd[v].deg);
-      p = __dmul_rn(__dadd_rn(__ddiv_rn(1.0, du), __ddiv_rn(1.0, dv)), a.logn);
+      p = __dmul_rn(__dadd_rn(__ddiv_rn(1.0, (double)vu.y), __ddiv_rn(1.0, (double)vv.y)), a.logn);
       p = p < 1.0 ? p : 1.0;
       ipw = __ddiv_rn(1.0, p);
     }
+    active = todo > 0;
+    div = (uint32_t)a.walk_len;
+    mag = a.walk_magic;
   }
   int qlen = 0;  // warp-uniform
   while (__any_sync(kFullMask, active)) {
     bool emit = false;
     unsigned long long key = 0;
     if (active) {
-      if (phase == 0) {
-        if (todo == 0) {
-          active = false;
+      const uint64_t rnd = rng_draw(s);
+      bool sample_done = false;
+      if (SAMPLE && phase == kPhEff) {
+        if (map_uint64(rnd) < p) {
+          phase = kPhR;
+          div = (uint32_t)a.walk_len;
+          mag = a.walk_magic;
         } else {
-          --todo;
-          bool take = true;
-          if (SAMPLE) take = map_uint64(rng_draw(s)) < p;
-          if (take) {
-            const uint64_t r = rng_draw(s) % a.walk_len + 1;
-            const uint64_t k = rng_draw(s) % r + 1;
-            left1 = (uint32_t)(k - 1);
-            left2 = (uint32_t)(r - k);
-            cur = u;
-            phase = 1;
+          sample_done = true;
+        }
+      } else {
+        const uint32_t m = gm_mod(rnd, div, mag);
+        if (phase == kPhR) {
+          r = m + 1;
+          phase = kPhK;
+          div = r;
+          mag = r <= kMaxRMagic ? rmag[r] : gm_magic(r);
+        } else {
+          uint32_t nxt = 0;
+          bool to_v = false, end_walk = false;
+          if (phase == kPhK) {
+            const uint32_t k = m + 1;
+            left1 = k - 1;
+            left2 = r - k;
+            if (left1 > 0) {
+              phase = kPhW1;
+              cur = u;
+              cur_off = vu.x;
+              div = vu.y;
+              mag = ((uint64_t)vu.w << 32) | vu.z;
+            } else {
+              x = u;
+              to_v = true;
+            }
+          } else {
+            nxt = __ldg(nbrs + cur_off + m);
+            cur = nxt;
+            if (phase == kPhW1) {
+              if (--left1 == 0) {
+                x = cur;
+                to_v = true;
+              }
+            } else if (--left2 == 0) {
+              end_walk = true;
+            }
+            if (!to_v && !end_walk) {
+              const uint4 rw = __ldg(reinterpret_cast<const uint4*>(vd + cur));
+              cur_off = rw.x;
+              div = rw.y;
+              mag = ((uint64_t)rw.w << 32) | rw.z;
+              if (div == 0) active = false;  // unreachable for a validated (symmetric) graph
+            }
+          }
+          if (to_v) {
+            cur = v;
+            if (left2 > 0) {
+              phase = kPhW2;
+              cur_off = vv.x;
+              div = vv.y;
+              mag = ((uint64_t)vv.w << 32) | vv.z;
+            } else {
+              end_walk = true;
+            }
+          }
+          if (end_walk) {
+            const uint32_t lo = x < cur ? x : cur, hi = x < cur ? cur : x;
+            key = ((uint64_t)lo << 32) + (uint64_t)hi;
+            emit = true;
+            sample_done = true;
           }
         }
       }
-      if (active && phase != 0) {
-        if (phase == 1 && left1 == 0) {
-          x = cur;
-          cur = v;
-          phase = 2;
-        }
-        if (phase == 2 && left2 == 0) {
-          const uint32_t lo = x < cur ? x : cur, hi = x < cur ? cur : x;
-          key = ((uint64_t)lo << 32) + (uint64_t)hi;
-          emit = true;
-          phase = 0;
+      if (sample_done) {
+        if (--todo == 0) {
+          active = false;
         } else {
-          const uint4 raw = __ldg(reinterpret_cast<const uint4*>(vd + cur));
-          if (raw.y == 0) {
-            active = false;  // unreachable for a validated (symmetric) graph
-          } else {
-            const uint32_t idx = gm_mod(rng_draw(s), raw.y, ((uint64_t)raw.w << 32) | raw.z);
-            cur = __ldg(nbrs + raw.x + idx);
-            if (phase == 1) --left1; else --left2;
-          }
+          phase = SAMPLE ? kPhEff : kPhR;
+          div = (uint32_t)a.walk_len;
+          mag = a.walk_magic;
         }
       }
     }
@@ -205,12 +265,25 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(const Vertex* __restrict_
   }
 }
 
-// Adds every staged key to the pair table (par_table::insert_add).
+// Adds every staged key to the pair table (par_table::insert_add).  For
+// counts, the lanes of a warp that hold the same key are merged first
+// (match.any) and one of them adds their number: hub pairs recur often.
 template <bool WEIGHTED>
 __global__ void k_insert(const unsigned long long* __restrict__ keys, const double* __restrict__ w, uint64_t count,
                          Slot* __restrict__ table, uint64_t mask, int* flags) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
-    if (!table_insert_add<WEIGHTED>(table, mask, keys[i], WEIGHTED ? w[i] : 1.0, flags)) return;
+  const int lane = threadIdx.x & 31;
+  const uint64_t nwarp = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t wb = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wb < count; wb += nwarp * 32) {
+    const uint64_t i = wb + lane;
+    const bool have = i < count;
+    const unsigned long long key = have ? keys[i] : kEmptyKey;
+    if (WEIGHTED) {
+      if (have && !table_insert_add<true>(table, mask, key, w[i], flags)) return;
+    } else {
+      const unsigned same = __match_any_sync(kFullMask, key);
+      const bool leader = have && (__ffs(same) - 1) == lane;
+      if (leader && !table_insert_add<false>(table, mask, key, 1.0, flags, (unsigned long long)__popc(same))) return;
+    }
   }
 }
 
@@ -591,7 +664,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
                             lne_sparsify_stats* stats) {
   LNE_CHECK_ARG(ctx && g && p && out, "lne_sparsify: NULL argument");
   *out = nullptr;
-  LNE_CHECK_ARG(p->walk_len >= 1, "lne_sparsify: walk_len must be >= 1");
+  LNE_CHECK_ARG(p->walk_len >= 1 && p->walk_len < (int64_t)1 << 31, "lne_sparsify: walk_len must be in [1, 2^31)");
   LNE_CHECK_ARG(p->negative >= 1, "lne_sparsify: negative must be >= 1");
   LNE_CHECK_ARG(p->table_size >= 0, "lne_sparsify: table_size must be >= 0");
   LNE_CHECK_ARG(g->m_dir >= 1, "lne_sparsify: the graph has no edges");
@@ -629,6 +702,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   SampleArgs a;
   a.seed = p->seed;
   a.walk_len = (uint64_t)p->walk_len;
+  a.walk_magic = gm_magic((uint32_t)p->walk_len);
   a.exp_rv = (uint64_t)exp_rv;
   a.frac = frac;
   a.logn = logn;

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 def bessel_i_series(k, s, terms=30):
     out = torch.zeros((), dtype=torch.float64)
     for m in range(terms):
-        out = out + (s / 2) ** (2 * m + k) / (math.factorial(m) * math.factorial(m + k))
+        out = out + (s / 2) ** (2 * m + k) / float(math.factorial(m) * math.factorial(m + k))
     return out
 
 

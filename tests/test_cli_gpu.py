@@ -40,7 +40,9 @@ def test_cli_matches_library(ctx, lib):
     assert np.array_equal(e_cli, emb.cpu().numpy())
     assert np.array_equal(p_cli, pro_lib.cpu().numpy())
     norms = np.linalg.norm(p_cli, axis=1)
-    np.testing.assert_allclose(norms, 1.0, rtol=1e-5)
+    live = norms > 1e-5  # isolated vertices keep a zero row, as in the reference
+    assert live.sum() > 1500
+    np.testing.assert_allclose(norms[live], 1.0, rtol=1e-5)
     csr.free()
     g.free()
 
