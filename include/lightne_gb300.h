@@ -233,6 +233,20 @@ int lne_propagate_adjoint(lne_ctx* ctx, const lne_graph* g, const lne_propagate_
  */
 int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_t dim, float* d_emb, float* h_S);
 
+/*
+ * Dense building blocks of the randomized SVD (device pointers, FP32 in):
+ * G (c1 x c2, FP64 row-major) = A^T B for A (n x c1, lda) and B (n x c2, ldb)
+ * [the Gram of CholeskyQR, mklredsvd.cc:262 via util.cc:40-79, and C = Z^T B,
+ * mklredsvd.cc:330-345]; Out (n x c2, ldo) = In (n x k, ldi) W (k x c2
+ * row-major) [the cblas_sgemm calls of mklredsvd.cc:297-312 and :382-397].
+ * Up to 256 columns they run on the tcgen05 tensor core with split TF32
+ * operands (FP32-level accuracy); columns c2..ldo-1 of Out are zeroed.
+ */
+int lne_gram(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, const float* B, int64_t ldb, int64_t c2,
+             int64_t n, double* G);
+int lne_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int64_t k, const float* W, int64_t c2, int64_t n,
+                  float* Out, int64_t ldo);
+
 /* CSR accessors. */
 int lne_csr_info(const lne_csr* c, int64_t* n, int64_t* nnz);
 int lne_csr_download(lne_ctx* ctx, const lne_csr* c, int64_t* row_ptr, int32_t* col, float* val);

@@ -156,6 +156,8 @@ SIGNATURES = {
                                              ctypes.POINTER(PropagateStats)]),
     "lne_chebyshev_coefficients": (ctypes.c_int, [ctypes.c_int32, ctypes.c_double, VP]),
     "lne_dense_embed": (ctypes.c_int, [VP, VP, I64, I64, VP, VP]),
+    "lne_gram": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, I64, VP]),
+    "lne_gemm_tall": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, VP, I64]),
     "lne_csr_info": (ctypes.c_int, [VP, ctypes.POINTER(I64), ctypes.POINTER(I64)]),
     "lne_csr_download": (ctypes.c_int, [VP, VP, VP, VP, VP]),
     "lne_csr_device_ptrs": (ctypes.c_int, [VP, PVP, PVP, PVP]),

@@ -123,6 +123,7 @@ __global__ void k_gram_reduce(const float* __restrict__ partial, int64_t nb, int
 
 int gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
          double* G) {
+  if (tc_supported(c2)) return tc_gram(ctx, A, lda, c1, B, ldb, c2, n, G);
   const int64_t nb = std::max<int64_t>(1, (n + kGramRows - 1) / kGramRows);
   const int tiles_i = (c1 + 63) / 64, tiles_j = (c2 + 63) / 64;
   float* partial = nullptr;
@@ -194,6 +195,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const float* __restrict__ In,
 int gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
               int64_t ldo, __nv_bfloat16* OutB) {
   if (n <= 0) return LNE_OK;
+  if (tc_supported((int)std::max<int64_t>(c2, ldo))) return tc_gemm_tall(ctx, In, ldi, k, W, c2, n, Out, ldo, OutB);
   dim3 grid((unsigned)((n + 127) / 128), (unsigned)((ldo + 63) / 64));
   k_gemm_tall<<<grid, 256, 0, ctx->stream>>>(In, ldi, k, W, c2, n, Out, ldo, OutB);
   LNE_CUDA_TRY(cudaGetLastError());
@@ -496,3 +498,33 @@ int trace_host(lne_ctx* ctx, const double* G, int r, double* out) {
 }
 
 }  // namespace lne
+
+using namespace lne;
+
+extern "C" int lne_gram(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, const float* B, int64_t ldb,
+                        int64_t c2, int64_t n, double* G) {
+  LNE_CHECK_ARG(ctx && A && B && G && n >= 0 && c1 >= 1 && c2 >= 1 && lda >= c1 && ldb >= c2,
+                "lne_gram: bad argument");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  int rc = gram(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G);
+  if (rc) return rc;
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  int h = 0;
+  LNE_CUDA_TRY(cudaMemcpy(&h, ctx->d_flags + kFlagNumeric, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h == 2) { set_error("lne_gram: tensor-core wait timed out"); return LNE_ERR_CUDA; }
+  return LNE_OK;
+}
+
+extern "C" int lne_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int64_t k, const float* W, int64_t c2,
+                             int64_t n, float* Out, int64_t ldo) {
+  LNE_CHECK_ARG(ctx && In && W && Out && n >= 0 && k >= 1 && c2 >= 1 && ldi >= k && ldo >= c2,
+                "lne_gemm_tall: bad argument");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  int rc = gemm_tall(ctx, In, ldi, (int)k, W, (int)c2, n, Out, ldo, nullptr);
+  if (rc) return rc;
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  int h = 0;
+  LNE_CUDA_TRY(cudaMemcpy(&h, ctx->d_flags + kFlagNumeric, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h == 2) { set_error("lne_gemm_tall: tensor-core wait timed out"); return LNE_ERR_CUDA; }
+  return LNE_OK;
+}

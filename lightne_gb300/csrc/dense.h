@@ -40,6 +40,14 @@ int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W);
 // descending), S (r, FP64).
 int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out);
 
+// tcgen05 tensor-core versions (3xTF32, FP32-level accuracy) of gram and
+// gemm_tall for up to 256 columns; gram/gemm_tall use them when they apply.
+bool tc_supported(int c2);
+int tc_gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+            double* G);
+int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
+                 int64_t ldo, __nv_bfloat16* OutB);
+
 // Copies an FP32 tall matrix into a BF16 copy (same ld).
 int to_bf16(lne_ctx* ctx, const float* X, int64_t n, int64_t ld, __nv_bfloat16* Y);
 
