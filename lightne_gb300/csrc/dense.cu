@@ -506,6 +506,7 @@ extern "C" int lne_gram(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, c
   LNE_CHECK_ARG(ctx && A && B && G && n >= 0 && c1 >= 1 && c2 >= 1 && lda >= c1 && ldb >= c2,
                 "lne_gram: bad argument");
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, ctx->stream));
   int rc = gram(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G);
   if (rc) return rc;
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -520,6 +521,7 @@ extern "C" int lne_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int64_t
   LNE_CHECK_ARG(ctx && In && W && Out && n >= 0 && k >= 1 && c2 >= 1 && ldi >= k && ldo >= c2,
                 "lne_gemm_tall: bad argument");
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, ctx->stream));
   int rc = gemm_tall(ctx, In, ldi, (int)k, W, (int)c2, n, Out, ldo, nullptr);
   if (rc) return rc;
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

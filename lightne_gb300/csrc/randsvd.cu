@@ -148,6 +148,7 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
     return LNE_ERR_UNSUPPORTED;
   }
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, ctx->stream));
   lne_csr* A = const_cast<lne_csr*>(Acsr);
   const int64_t n = A->n;
   const int r = (int)p->rank, dim = (int)p->dim;
@@ -245,6 +246,14 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
   }
   LNE_CUDA_TRY(cudaEventSynchronize(ev[5]));
   LNE_CUDA_TRY(cudaGetLastError());
+  {
+    int hf = 0;
+    LNE_CUDA_TRY(cudaMemcpy(&hf, ctx->d_flags + kFlagNumeric, sizeof(int), cudaMemcpyDeviceToHost));
+    if (hf == 2) {
+      set_error("lne_randsvd: a tensor-core wait timed out");
+      return LNE_ERR_CUDA;
+    }
+  }
   if (stats) {
     cudaEventElapsedTime(&stats->ms_sketch, ev[0], ev[1]);
     cudaEventElapsedTime(&stats->ms_qr, ev[1], ev[2]);
@@ -266,6 +275,7 @@ extern "C" int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_
   }
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
+  LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, st));
   const int d = (int)dim;
   const int64_t ld = pad_ld(d);
   Buf B(ctx);
@@ -299,5 +309,11 @@ extern "C" int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_
   }
   LNE_CUDA_TRY(cudaStreamSynchronize(st));
   LNE_CUDA_TRY(cudaGetLastError());
+  int hf = 0;
+  LNE_CUDA_TRY(cudaMemcpy(&hf, ctx->d_flags + kFlagNumeric, sizeof(int), cudaMemcpyDeviceToHost));
+  if (hf == 2) {
+    set_error("lne_dense_embed: a tensor-core wait timed out");
+    return LNE_ERR_CUDA;
+  }
   return LNE_OK;
 }

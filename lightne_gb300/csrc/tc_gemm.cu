@@ -31,7 +31,7 @@ constexpr uint32_t kTileB = 256 * kKc * 4;  // bytes of one B part, sized for N 
 constexpr uint32_t kStageBytes = 2 * kTileA + 2 * kTileB;
 constexpr uint32_t kSmemBytes = kStages * kStageBytes + 64;
 constexpr uint32_t kTmemCols = 256;
-constexpr uint32_t kWaitLimit = 1u << 26;
+constexpr long long kWaitCycles = 2000000000LL;  // about one second
 
 struct StageBufs {
   uint8_t* a_hi;
@@ -88,13 +88,13 @@ struct TcShared {
 // Shared K-loop: stage(c, bufs) fills stage buffers for K slice c.
 template <class StageFn>
 __device__ __forceinline__ bool tc_kloop(uint8_t* smem, TcShared* sh, uint32_t tmem, uint32_t idesc, int nchunks,
-                                         StageFn stage) {
+                                         const volatile int* abort, StageFn stage) {
   bool ok = true;
   for (int c = 0; c < nchunks; ++c) {
     const int st = c % kStages;
     if (c >= kStages) {
       const uint32_t parity = (uint32_t)((c / kStages - 1) & 1);
-      if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[st]), parity, kWaitLimit)) ok = false;
+      if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[st]), parity, kWaitCycles, abort)) ok = false;
     }
     const StageBufs b = stage_bufs(smem, st);
     stage(c, b);
@@ -111,7 +111,7 @@ __device__ __forceinline__ bool tc_kloop(uint8_t* smem, TcShared* sh, uint32_t t
   if (nchunks > 0) {
     const int last = nchunks - 1;
     const uint32_t parity = (uint32_t)((last / kStages) & 1);
-    if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[last % kStages]), parity, kWaitLimit)) ok = false;
+    if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[last % kStages]), parity, kWaitCycles, abort)) ok = false;
   }
   // block-uniform verdict: the epilogue's tcgen05.ld is warp-synchronous
   ok = __syncthreads_and(ok ? 1 : 0) != 0;
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm_tall(const float* __rest
   const int t = threadIdx.x;
   const int nchunks = (K + kKc - 1) / kKc;
   const uint32_t idesc = tc::idesc_tf32(128, nmma);
-  const bool ok = tc_kloop(smem, sh, tmem, idesc, nchunks, [&](int c, const StageBufs& b) {
+  const bool ok = tc_kloop(smem, sh, tmem, idesc, nchunks, flags + kFlagNumeric, [&](int c, const StageBufs& b) {
     const int k0 = c * kKc;
     // A: row t of the tile = In row m0 + t
     {
@@ -171,8 +171,13 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm_tall(const float* __rest
     }
   });
   if (!ok) {
+    // record the timeout; give the MMAs in flight one more bounded wait
+    // before the TMEM they write is released
     if (t == 0) atomicExch(flags + kFlagNumeric, 2);
-    tc::mbar_wait(tc::smem_addr(&sh->mbar[0]), 0, kWaitLimit);
+    const int last = nchunks - 1;
+    if (last >= 0)
+      tc::mbar_wait(tc::smem_addr(&sh->mbar[last % kStages]), (uint32_t)((last / kStages) & 1), kWaitCycles,
+                    flags + kFlagTimeoutGuard);
   } else {
     const int w = t >> 5, lane = t & 31;
     const int64_t row = m0 + 32 * w + lane;
@@ -213,7 +218,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gram(const float* __restrict_
   const int nchunks = (int)((r1 - r0 + kKc - 1) / kKc);
   const uint32_t idesc = tc::idesc_tf32(128, nmma);
   const int ca = mt * 128 + t;
-  const bool ok = tc_kloop(smem, sh, tmem, idesc, nchunks, [&](int c, const StageBufs& b) {
+  const bool ok = tc_kloop(smem, sh, tmem, idesc, nchunks, flags + kFlagNumeric, [&](int c, const StageBufs& b) {
     const int64_t k0 = r0 + (int64_t)c * kKc;
     {
       float v[kKc];
@@ -229,8 +234,13 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gram(const float* __restrict_
     }
   });
   if (!ok) {
+    // record the timeout; give the MMAs in flight one more bounded wait
+    // before the TMEM they write is released
     if (t == 0) atomicExch(flags + kFlagNumeric, 2);
-    tc::mbar_wait(tc::smem_addr(&sh->mbar[0]), 0, kWaitLimit);
+    const int last = nchunks - 1;
+    if (last >= 0)
+      tc::mbar_wait(tc::smem_addr(&sh->mbar[last % kStages]), (uint32_t)((last / kStages) & 1), kWaitCycles,
+                    flags + kFlagTimeoutGuard);
   } else {
     const int w = t >> 5, lane = t & 31;
     const int i = mt * 128 + 32 * w + lane;

@@ -102,9 +102,12 @@ __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 // Waits for the phase with the given parity to complete; gives up after
-// `limit` polls and returns false (the caller records the timeout).
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t limit) {
-  for (uint32_t i = 0; i < limit; ++i) {
+// `max_cycles` SM clock cycles (or at once when *abort is set) and returns
+// false so that the caller can record the timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long max_cycles,
+                                          const volatile int* abort) {
+  const long long t0 = clock64();
+  for (;;) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred P1;\n\t"
@@ -114,8 +117,8 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32
         : "r"(mbar), "r"(parity)
         : "memory");
     if (done) return true;
+    if (*abort != 0 || clock64() - t0 > max_cycles) return false;
   }
-  return false;
 }
 
 // FP32 -> TF32 (round to nearest, ties away), as a float bit pattern.
