@@ -61,6 +61,9 @@ const char* lne_version(void);
  * (NULL: the default stream). */
 int lne_ctx_create(lne_ctx** out, int device, void* stream);
 int lne_ctx_destroy(lne_ctx* ctx);
+/* L2 tuning: the bytes of L2 one column panel of an SpMM
+ * dense operand may occupy (default 64 MiB; 0 disables column panels). */
+int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes);
 /* Wait for all work queued on the context's stream. */
 int lne_ctx_synchronize(lne_ctx* ctx);
 

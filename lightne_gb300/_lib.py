@@ -137,6 +137,7 @@ SIGNATURES = {
     "lne_ctx_create": (ctypes.c_int, [PVP, ctypes.c_int, VP]),
     "lne_ctx_destroy": (ctypes.c_int, [VP]),
     "lne_ctx_synchronize": (ctypes.c_int, [VP]),
+    "lne_ctx_set_spmm_panel_bytes": (ctypes.c_int, [VP, I64]),
     "lne_device_alloc": (ctypes.c_int, [VP, I64, PVP]),
     "lne_device_free": (ctypes.c_int, [VP, VP]),
     "lne_copy_to_host": (ctypes.c_int, [VP, VP, VP, I64]),

@@ -249,6 +249,12 @@ int lne_ctx_destroy(lne_ctx* ctx) {
   return LNE_OK;
 }
 
+int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes) {
+  LNE_CHECK_ARG(ctx != nullptr && bytes >= 0, "lne_ctx_set_spmm_panel_bytes: bad argument");
+  ctx->spmm_panel_bytes = bytes;
+  return LNE_OK;
+}
+
 int lne_ctx_synchronize(lne_ctx* ctx) {
   LNE_CHECK_ARG(ctx != nullptr, "lne_ctx_synchronize: ctx is NULL");
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -444,6 +450,7 @@ int lne_csr_wrap_device(lne_ctx* ctx, int64_t n, int64_t nnz, const int64_t* d_r
 int lne_csr_free(lne_csr* c) {
   if (!c) return LNE_OK;
   free_plan(c->plan);
+  free_panels(c);
   if (c->owned) {
     cudaFree(c->row_ptr);
     cudaFree(c->col);

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 #include "../../include/lightne_gb300.h"
 
@@ -56,6 +57,8 @@ struct lne_ctx {
   int num_sms = 0;
   size_t smem_optin = 0;
   void* log_table = nullptr;    // device lne::LogTable (double-float log(c_j), 1/c_j)
+  // L2 bytes a column panel of the SpMM dense operand may take (0: no panels)
+  int64_t spmm_panel_bytes = 64ll << 20;
 };
 
 struct lne_graph {
@@ -80,6 +83,13 @@ struct lne_csr {
   cudaStream_t stream = nullptr;
   lne::SpmmPlan plan;
   bool plan_ready = false;
+  // column panels for the cache-blocked SpMM (built on first use for a
+  // given panel width): seg[r * (npanels + 1) + p] = first entry of row r
+  // with column >= p * panel_width, relative to row_ptr[r]
+  int64_t panel_width = 0;
+  int npanels = 0;
+  int32_t* seg = nullptr;
+  std::vector<lne::SpmmPlan> panel_plans;
 };
 
 #define LNE_CUDA_TRY(expr)                                                           \
@@ -116,5 +126,8 @@ void scan_exclusive_i64(const int64_t* counts, int64_t* out, int64_t n, void* tm
 int build_plan_csr(lne_ctx* ctx, lne_csr* c);
 int build_plan_graph(lne_ctx* ctx, lne_graph* g);
 void free_plan(SpmmPlan& p);
+// Column panels of width pw for the cache-blocked SpMM (synchronises).
+int build_panels(lne_ctx* ctx, lne_csr* c, int64_t pw);
+void free_panels(lne_csr* c);
 
 }  // namespace lne

@@ -46,17 +46,19 @@ struct Buf {
   }
 };
 
-// Y = A * X with FP32 output (overwrites Y), X FP32 or BF16.
+// Y = A * X with FP32 output, X FP32 or BF16; `add` accumulates the later
+// column panels of the cache-blocked SpMM.
 struct EpiStore {
   float* __restrict__ Y;
   int64_t ldy;
   int d;
+  bool add;
   template <int N>
   __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&a)[N]) const {
     float* y = Y + r * ldy + e0;
 #pragma unroll
     for (int i = 0; i < N; ++i)
-      if (e0 + i < d) y[i] = a[i];
+      if (e0 + i < d) y[i] = add ? y[i] + a[i] : a[i];
   }
 };
 
@@ -121,9 +123,8 @@ static int cholqr3(lne_ctx* ctx, float* X, float* tmp, int64_t n, int64_t ld, in
 
 template <typename XT>
 static int spmm_store(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ld, int d, float* Y, int* launches) {
-  CsrRows R{A->row_ptr, A->col, A->val};
-  EpiStore epi{Y, ld, d};
-  return spmm_run<XT>(ctx, R, A->plan, X, ld, d, epi, launches);
+  EpiStore epi{Y, ld, d, false};
+  return spmm_csr_panels<XT>(ctx, A, X, ld, d, epi, launches);
 }
 
 }  // namespace lne

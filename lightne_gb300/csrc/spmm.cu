@@ -106,18 +106,73 @@ void free_plan(SpmmPlan& p) {
   p = SpmmPlan();
 }
 
-// Y = alpha * acc + beta * Y on columns < d (beta == 0 does not read Y).
+// seg[r * np1 + p] = (first entry of row r with column >= p * pw) - row_ptr[r]
+__global__ void k_panel_seg(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, int64_t n,
+                            int64_t pw, int np1, int32_t* __restrict__ seg) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int64_t a = row_ptr[r], b = row_ptr[r + 1];
+  seg[r * np1] = 0;
+  int64_t lo = a;
+  for (int p = 1; p < np1; ++p) {
+    const int64_t bound = (int64_t)p * pw;
+    int64_t hi = b;
+    while (lo < hi) {  // first index in [lo, b) with col >= bound
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)col[mid] < bound) lo = mid + 1; else hi = mid;
+    }
+    seg[r * np1 + p] = (int32_t)(lo - a);
+  }
+}
+
+void free_panels(lne_csr* c) {
+  for (auto& p : c->panel_plans) free_plan(p);
+  c->panel_plans.clear();
+  if (c->seg) cudaFree(c->seg);
+  c->seg = nullptr;
+  c->npanels = 0;
+  c->panel_width = 0;
+}
+
+int build_panels(lne_ctx* ctx, lne_csr* c, int64_t pw) {
+  if (c->panel_width == pw && c->seg) return LNE_OK;
+  free_panels(c);
+  const int64_t n = c->n;
+  const int np = (int)((n + pw - 1) / pw);
+  int32_t* seg = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, (void**)&seg, sizeof(int32_t) * n * (np + 1), "spmm panel segments"))) return rc;
+  k_panel_seg<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(c->row_ptr, c->col, n, pw, np + 1, seg);
+  LNE_CUDA_TRY(cudaGetLastError());
+  c->seg = seg;
+  c->npanels = np;
+  c->panel_width = pw;
+  c->panel_plans.resize(np);
+  for (int p = 0; p < np; ++p) {
+    PanelRows R{c->row_ptr, seg, c->col, c->val, np + 1, p};
+    if ((rc = build_plan(ctx, R, n, c->panel_plans[p]))) {
+      free_panels(c);
+      return rc;
+    }
+  }
+  return LNE_OK;
+}
+
+// Y = alpha * acc + beta * Y on columns < d (beta == 0 does not read Y);
+// later column panels add alpha * acc.
 struct EpiAxpby {
   float alpha, beta;
   float* __restrict__ Y;
   int64_t ldy;
   int d;
+  bool add;
   template <int N>
   __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&a)[N]) const {
     float* y = Y + r * ldy + e0;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      if (e0 + i < d) y[i] = beta == 0.f ? alpha * a[i] : fmaf(alpha, a[i], beta * y[i]);
+      if (e0 + i < d)
+        y[i] = add ? fmaf(alpha, a[i], y[i]) : (beta == 0.f ? alpha * a[i] : fmaf(alpha, a[i], beta * y[i]));
     }
   }
 };
@@ -135,13 +190,7 @@ extern "C" int lne_spmm(lne_ctx* ctx, const lne_csr* A, int x_prec, const void* 
                 "lne_spmm: X rows must start on 16-byte boundaries (ldx a multiple of 8)");
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
   lne_csr* Am = const_cast<lne_csr*>(A);
-  int rc = build_plan_csr(ctx, Am);
-  if (rc) return rc;
-  CsrRows R{A->row_ptr, A->col, A->val};
-  EpiAxpby epi{alpha, beta, Y, ldy, (int)d};
-  if (x_prec == LNE_PREC_FP32)
-    rc = spmm_run<float>(ctx, R, Am->plan, (const float*)X, ldx, d, epi);
-  else
-    rc = spmm_run<__nv_bfloat16>(ctx, R, Am->plan, (const __nv_bfloat16*)X, ldx, d, epi);
-  return rc;
+  EpiAxpby epi{alpha, beta, Y, ldy, (int)d, false};
+  if (x_prec == LNE_PREC_FP32) return spmm_csr_panels<float>(ctx, Am, (const float*)X, ldx, d, epi);
+  return spmm_csr_panels<__nv_bfloat16>(ctx, Am, (const __nv_bfloat16*)X, ldx, d, epi);
 }

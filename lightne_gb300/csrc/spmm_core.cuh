@@ -35,6 +35,25 @@ struct CsrRows {  // explicit CSR: int64 row_ptr, int32 col, float val
   static constexpr bool kHasVal = true;
 };
 
+// The entries of a CSR row whose columns fall in one column panel.
+struct PanelRows {
+  const int64_t* __restrict__ row_ptr;
+  const int32_t* __restrict__ seg;  // n x (np1) relative panel starts
+  const int32_t* __restrict__ col;
+  const float* __restrict__ val;
+  int np1;                          // panels + 1
+  int p;                            // this panel
+  __device__ __forceinline__ int64_t begin(int64_t r) const {
+    return __ldg(row_ptr + r) + __ldg(seg + r * np1 + p);
+  }
+  __device__ __forceinline__ int64_t end(int64_t r) const {
+    return __ldg(row_ptr + r) + __ldg(seg + r * np1 + p + 1);
+  }
+  __device__ __forceinline__ uint32_t c(int64_t j) const { return (uint32_t)__ldg(col + j); }
+  __device__ __forceinline__ float v(int64_t j) const { return __ldg(val + j); }
+  static constexpr bool kHasVal = true;
+};
+
 struct GraphRows {  // graph adjacency: {offset, degree} per vertex, unit values
   const Vertex* __restrict__ vdata;
   const uint32_t* __restrict__ nbrs;

@@ -6,6 +6,8 @@
 #include "lne_internal.h"
 #include "spmm_core.cuh"
 
+#include <algorithm>
+
 namespace lne {
 
 template <typename XT, int G, int VPL, class Rows, class Epi>
@@ -63,6 +65,33 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
   if (e != cudaSuccess) {
     set_error(std::string("spmm launch: ") + cudaGetErrorString(e));
     return LNE_ERR_CUDA;
+  }
+  return LNE_OK;
+}
+
+// Cache-blocked SpMM over a CSR: when the dense operand is larger than the
+// context's panel budget, the columns are cut into panels whose slice of X
+// fits in L2 and one pass per panel gathers only from that slice.  The
+// epilogue is called with add = false on the first panel and add = true on
+// the later ones (fixed panel order: reproducible sums).
+template <typename XT, class EpiT>
+static int spmm_csr_panels(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ldx, int64_t d, EpiT epi,
+                           int* launches = nullptr) {
+  const int64_t row_bytes = ldx * (int64_t)sizeof(XT);
+  const int64_t xbytes = A->n * row_bytes;
+  int rc;
+  if (ctx->spmm_panel_bytes <= 0 || xbytes <= ctx->spmm_panel_bytes) {
+    if ((rc = build_plan_csr(ctx, A))) return rc;
+    CsrRows R{A->row_ptr, A->col, A->val};
+    epi.add = false;
+    return spmm_run<XT>(ctx, R, A->plan, X, ldx, d, epi, launches);
+  }
+  const int64_t pw = std::max<int64_t>(1, ctx->spmm_panel_bytes / row_bytes);
+  if ((rc = build_panels(ctx, A, pw))) return rc;
+  for (int p = 0; p < A->npanels; ++p) {
+    PanelRows R{A->row_ptr, A->seg, A->col, A->val, A->npanels + 1, p};
+    epi.add = p > 0;
+    if ((rc = spmm_run<XT>(ctx, R, A->panel_plans[p], X, ldx, d, epi, launches))) return rc;
   }
   return LNE_OK;
 }

@@ -83,3 +83,37 @@ def test_spmm_rejects_misaligned(ctx, lib):
                       ctypes.c_void_p(X.data_ptr()), 12)
     assert rc == _lib.LNE_ERR_INVALID
     A.free()
+
+
+@pytest.mark.parametrize("prec", [LNE_PREC_FP32, LNE_PREC_BF16])
+def test_spmm_column_panels(ctx, lib, prec):
+    # a panel budget far below the operand size forces many column panels
+    n, d = 6000, 138
+    rp, col, val = random_csr(n, 40, long_rows=[(3, 5000), (4000, 3000)], seed=7)
+    ld = 144
+    rng = np.random.default_rng(2)
+    X = np.zeros((n, ld), np.float32)
+    X[:, :d] = rng.standard_normal((n, d))
+    dt = torch.float32 if prec == LNE_PREC_FP32 else torch.bfloat16
+    dX = torch.from_numpy(X).to(dt).cuda()
+    d_rp, d_col, d_val = (torch.from_numpy(a).cuda() for a in (rp, col, val))
+    A = CSR.wrap_device(ctx, n, int(rp[-1]), d_rp.data_ptr(), d_col.data_ptr(), d_val.data_ptr())
+    outs = []
+    for budget in (64 << 20, 100 * ld * 4, 777 * ld * 4):
+        assert lib.lne_ctx_set_spmm_panel_bytes(ctx.handle, budget) == 0
+        dY = torch.zeros((n, ld), device="cuda")
+        torch.cuda.synchronize()
+        rc = lib.lne_spmm(ctx.handle, A.handle, prec, ctypes.c_void_p(dX.data_ptr()), ld, d, 1.0, 0.0,
+                          ctypes.c_void_p(dY.data_ptr()), ld)
+        assert rc == 0, lib.lne_last_error()
+        ctx.synchronize()
+        outs.append(dY.cpu().numpy()[:, :d].astype(np.float64))
+    lib.lne_ctx_set_spmm_panel_bytes(ctx.handle, 64 << 20)
+    Xd = X.astype(np.float64) if prec == LNE_PREC_FP32 else to_bf16_f64(X)
+    import scipy.sparse as sp
+    Am = sp.csr_matrix((val.astype(np.float64), col, rp), shape=(n, n))
+    ref = Am @ Xd[:, :d]
+    bound = 1e-5 * (abs(Am) @ np.abs(Xd[:, :d])) + 1e-30
+    for o in outs:
+        assert (np.abs(o - ref) <= bound).all()
+    A.free()
