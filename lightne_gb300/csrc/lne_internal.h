@@ -57,8 +57,10 @@ struct lne_ctx {
   int num_sms = 0;
   size_t smem_optin = 0;
   void* log_table = nullptr;    // device lne::LogTable (double-float log(c_j), 1/c_j)
-  // L2 bytes a column panel of the SpMM dense operand may take (0: no panels)
-  int64_t spmm_panel_bytes = 64ll << 20;
+  // L2 bytes a column panel of the SpMM dense operand may take (0: no
+  // panels, the default: with full-width lane layouts the gathers run as
+  // fast from HBM as from L2-sized panels at 1.1M x 144)
+  int64_t spmm_panel_bytes = 0;
 };
 
 struct lne_graph {

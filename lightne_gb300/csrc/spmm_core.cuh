@@ -85,7 +85,9 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
                                                 int64_t ldx, int C, Acc<XT, VPL>& acc) {
   constexpr int P = 32 / G;
   constexpr int E = Vec16<XT>::E;
-  constexpr int kUnroll = 4;
+  // nonzeros whose gathers are in flight per lane: about 16 staged floats
+  constexpr int kStaged = 16 / (VPL * E);
+  constexpr int kUnroll = kStaged < 1 ? 1 : (kStaged > 4 ? 4 : kStaged);
   const int lane = threadIdx.x & 31;
   const int grp = lane / G, gl = lane % G;
   for (int64_t base = j0; base < j1; base += 32) {
@@ -132,7 +134,7 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
 // Main kernel: short rows call the epilogue directly; chunks of long rows
 // store partial sums (FP32, ld = ldp) for k_spmm_finish.
 template <typename XT, int G, int VPL, class Rows, class Epi>
-__global__ void __launch_bounds__(256, 2) k_spmm(Rows R, SpmmPlan plan, const XT* __restrict__ X, int64_t ldx, int C,
+__global__ void __launch_bounds__(256, 4) k_spmm(Rows R, SpmmPlan plan, const XT* __restrict__ X, int64_t ldx, int C,
                                               float* __restrict__ partial, int64_t ldp, int e_base, Epi epi) {
   constexpr int E = Vec16<XT>::E;
   const int lane = threadIdx.x & 31;

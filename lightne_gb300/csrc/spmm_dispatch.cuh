@@ -32,8 +32,14 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
   float* partial = nullptr;
   int rc;
   int nl = 0;
-  for (int64_t c_off = 0; c_off < c_total; c_off += 128) {
-    const int C = (int)((c_total - c_off) < 128 ? (c_total - c_off) : 128);
+  // Column slabs of a power-of-two number of 16-byte vectors (at most 128),
+  // largest first: each slab fills its lane layout exactly (a 144-wide FP32
+  // row is a 32-vector slab and a 4-vector slab, not 36 vectors on 32 lanes).
+  int64_t c_off = 0;
+  while (c_off < c_total) {
+    int64_t rem = c_total - c_off, C2 = 1;
+    while (C2 * 2 <= rem && C2 * 2 <= 128) C2 *= 2;
+    const int C = (int)C2;
     const int64_t ldp = (int64_t)C * E;
     if (plan.n_chunks > 0 && partial == nullptr) {
       const int64_t w = (c_total < 128 ? c_total : 128) * E;
@@ -41,7 +47,11 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
     }
     const XT* Xs = X + c_off * E;
     const int e_base = (int)(c_off * E);
-    if (C <= 8)
+    if (C <= 2)
+      spmm_launch<XT, 2, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+    else if (C <= 4)
+      spmm_launch<XT, 4, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+    else if (C <= 8)
       spmm_launch<XT, 8, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
     else if (C <= 16)
       spmm_launch<XT, 16, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
@@ -58,6 +68,7 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
       k_spmm_finish<Epi><<<(unsigned)blocks, 256, 0, ctx->stream>>>(plan, partial, ldp, (int)ldp, e_base, epi);
       ++nl;
     }
+    c_off += C;
   }
   if (partial) dfree(ctx, partial);
   if (launches) *launches += nl;
