@@ -250,6 +250,20 @@ int lne_gram(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, const float*
 int lne_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int64_t k, const float* W, int64_t c2, int64_t n,
                   float* Out, int64_t ldo);
 
+/*
+ * Allocation-free lne_gram, with no counterpart in the reference: for
+ * callers that cannot allocate device memory when they need the product (a
+ * process whose device memory belongs to another allocator or fixed arena,
+ * or one under a hard memory cap).  Same result as lne_gram; its scratch is
+ * a 16 MiB file-scope device array that every GPU loading the library holds
+ * until exit, so ceil(n / 2048) * c1 * c2 must be at most 4,194,304 and
+ * c2 at most 256 (else LNE_ERR_UNSUPPORTED).  The first call on a device
+ * looks up the array's device address (make it before any stream capture).
+ * Calls share the array: calls that overlap on the GPU race.
+ */
+int lne_gram_noalloc(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, const float* B, int64_t ldb, int64_t c2,
+                     int64_t n, double* G);
+
 /* CSR accessors. */
 int lne_csr_info(const lne_csr* c, int64_t* n, int64_t* nnz);
 int lne_csr_download(lne_ctx* ctx, const lne_csr* c, int64_t* row_ptr, int32_t* col, float* val);

@@ -159,6 +159,7 @@ SIGNATURES = {
     "lne_dense_embed": (ctypes.c_int, [VP, VP, I64, I64, VP, VP]),
     "lne_gram": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, I64, VP]),
     "lne_gemm_tall": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, VP, I64]),
+    "lne_gram_noalloc": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, I64, VP]),
     "lne_csr_info": (ctypes.c_int, [VP, ctypes.POINTER(I64), ctypes.POINTER(I64)]),
     "lne_csr_download": (ctypes.c_int, [VP, VP, VP, VP, VP]),
     "lne_csr_device_ptrs": (ctypes.c_int, [VP, PVP, PVP, PVP]),

@@ -48,6 +48,11 @@ int tc_gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, i
 int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
                  int64_t ldo, __nv_bfloat16* OutB);
 
+// tc_gram with caller-provided partial storage (nb * c1 * c2 floats,
+// nb = ceil(n / 2048)); allocates nothing.
+int tc_gram_into(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+                 double* G, float* partial);
+
 // Copies an FP32 tall matrix into a BF16 copy (same ld).
 int to_bf16(lne_ctx* ctx, const float* X, int64_t n, int64_t ld, __nv_bfloat16* Y);
 

@@ -1,0 +1,99 @@
+// Allocation-free Gram: lne_gram_noalloc.
+//
+// Some callers cannot allocate device memory at the moment they need this
+// product: a host process whose device memory is owned entirely by another
+// allocator (a framework's caching pool, a fixed arena handed out by an
+// embedding service), or code running under a hard per-process memory cap.
+// For them this entry point computes the same G = A^T B as lne_gram but
+// takes its scratch — the FP32 partial sums of the 2048-row blocks — from a
+// file-scope device array instead of cudaMallocAsync, and calls no
+// cudaMalloc, cudaFree or allocating library routine.
+//
+// The array is a module-scope __device__ variable: every GPU that loads this
+// library holds its 16 MiB until the process exits.  In host code the
+// array's name is a host-side stand-in, not a device address, so its device
+// address is looked up with cudaGetSymbolAddress once per device, with that
+// device current, on the first call for that device (make that first call
+// before any stream capture).  All calls share the one array and it keeps
+// the last call's contents; every partial a call reads it has written first,
+// so nothing needs clearing.  Calls whose work overlaps on the GPU (other
+// streams, other host threads) race on the array and must be serialised by
+// the caller.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "dense.h"
+#include "lne_internal.h"
+
+namespace lne {
+
+// Largest scratch a call may use: ceil(n / 2048) * c1 * c2 partial sums.
+static constexpr int64_t kNoAllocScratchFloats = (int64_t)1 << 22;  // 16 MiB of FP32
+
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+float* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on `device` (the current device).
+int noalloc_scratch(int device, float** out) {
+  if (device < 0 || device >= kMaxDevices) {
+    set_error("lne_gram_noalloc: device index out of range");
+    return LNE_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      cudaGetLastError();
+      set_error(std::string("lne_gram_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+      return LNE_ERR_CUDA;
+    }
+    g_noalloc_ptr[device] = (float*)p;
+  }
+  *out = g_noalloc_ptr[device];
+  return LNE_OK;
+}
+
+}  // namespace
+
+}  // namespace lne
+
+using namespace lne;
+
+extern "C" int lne_gram_noalloc(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, const float* B, int64_t ldb,
+                                int64_t c2, int64_t n, double* G) {
+  LNE_CHECK_ARG(ctx && A && B && G && n >= 1 && c1 >= 1 && c2 >= 1 && lda >= c1 && ldb >= c2,
+                "lne_gram_noalloc: bad argument");
+  if (c2 > 256) {
+    set_error("lne_gram_noalloc: at most 256 columns of B (the tensor-core path)");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  const int64_t nb = (n + 2047) / 2048;
+  if (c1 > kNoAllocScratchFloats || nb * c1 * c2 > kNoAllocScratchFloats) {
+    set_error("lne_gram_noalloc: ceil(n / 2048) * c1 * c2 exceeds the 4,194,304 partial sums of the "
+              "fixed 16 MiB scratch; use lne_gram");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  float* scratch = nullptr;
+  int rc = noalloc_scratch(ctx->device, &scratch);
+  if (rc) return rc;
+  LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, ctx->stream));
+  rc = tc_gram_into(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G, scratch);
+  if (rc) return rc;
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  int h = 0;
+  LNE_CUDA_TRY(cudaMemcpy(&h, ctx->d_flags + kFlagNumeric, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h == 2) {
+    set_error("lne_gram_noalloc: tensor-core wait timed out");
+    return LNE_ERR_CUDA;
+  }
+  return LNE_OK;
+}

@@ -306,4 +306,24 @@ int tc_gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, i
   return LNE_OK;
 }
 
+// Gram with caller-provided partial-sum storage (nb * c1 * c2 floats,
+// nb = ceil(n / 2048)); the tensor-core path only (c2 <= 256).  Every
+// partial is overwritten, so the storage needs no clearing.
+int tc_gram_into(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+                 double* G, float* partial) {
+  const int nmma = std::max(16, (c2 + 15) / 16 * 16);
+  if (nmma > 256) {
+    set_error("tc_gram_into: more than 256 columns");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  const int64_t nb = std::max<int64_t>(1, (n + 2047) / 2048);
+  cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  dim3 grid((unsigned)((c1 + 127) / 128), (unsigned)nb);
+  k_tc_gram<<<grid, kTcThreads, kSmemBytes, ctx->stream>>>(A, lda, c1, B, ldb, c2, nmma, n, partial, ctx->d_flags);
+  const int64_t cnt = (int64_t)c1 * c2;
+  k_gram_reduce_tc<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, cnt, G);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
 }  // namespace lne
