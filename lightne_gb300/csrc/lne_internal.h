@@ -17,7 +17,7 @@ void clear_error();
 enum FlagIndex : int {
   kFlagTableFull = 0,   // a probe sequence exceeded the probe limit
   kFlagCountOverflow = 1,
-  kFlagSortOverflow = 2,  // a row exceeded the sort scratch
+  kFlagSortOverflow = 2,  // a device buffer sized from host counts was too small (internal)
   kFlagNumeric = 3,     // 2: a tensor-core kernel's wait timed out (the other CTAs stop waiting)
   kFlagTimeoutGuard = 4,  // always 0: the no-abort flag of the final bounded wait
   kFlagWords = 8,

@@ -1,0 +1,229 @@
+// Stable LSD radix sort of (u64 key, u32 value) pairs on the device, used to
+// order the sparsifier's kept entries by (row, column).
+//
+// Each pass sorts by one digit of at most 8 bits (reduce-then-scan):
+//   k_radix_hist     per-tile digit counts (tile = 4096 consecutive items),
+//                    stored digit-major, so that one exclusive scan over
+//                    [digit][tile] gives every tile the output start of each
+//                    of its digits;
+//   k_radix_scatter  each warp ranks its 512 items of the tile with
+//                    match.any (lanes with equal digits in one step, rounds
+//                    in index order), the warps' counts are combined into
+//                    tile-local digit offsets, the tile is reordered by digit
+//                    in shared memory and then written out in runs of equal
+//                    digits, so that the global writes are contiguous.
+// Items with equal digits keep their input order in every pass, so the sort
+// is stable.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "lne_internal.h"
+#include "radix.h"
+
+namespace lne {
+
+namespace {
+
+constexpr int kRadixThreads = 256;
+constexpr int kRadixWarps = kRadixThreads / 32;
+constexpr int kRadixItems = 16;                            // per thread
+constexpr int kRadixTile = kRadixThreads * kRadixItems;    // 4096 items
+constexpr int kWarpItems = 32 * kRadixItems;               // 512 items per warp
+constexpr int kMaxBins = 256;
+constexpr int kNoDigit = kMaxBins;                         // digit of a lane past the end
+constexpr unsigned kFull = 0xffffffffu;
+constexpr size_t kScatterSmem = (size_t)kRadixTile * (sizeof(unsigned long long) + sizeof(uint32_t));
+
+__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const unsigned long long* __restrict__ keys,
+                                                               int64_t count, int shift, int bins, int64_t ntiles,
+                                                               int64_t* __restrict__ hist) {
+  __shared__ unsigned int h[kMaxBins];
+  for (int i = threadIdx.x; i < bins; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kRadixTile;
+  const unsigned long long mask = (unsigned long long)(bins - 1);
+  const int lane = threadIdx.x & 31;
+#pragma unroll 4
+  for (int r = 0; r < kRadixItems; ++r) {
+    const int64_t i = base + (int64_t)r * kRadixThreads + threadIdx.x;
+    const int d = i < count ? (int)((keys[i] >> shift) & mask) : kNoDigit;
+    const unsigned peers = __match_any_sync(kFull, d);
+    if (d != kNoDigit && lane == __ffs(peers) - 1) atomicAdd(&h[d], (unsigned)__popc(peers));
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < bins; d += blockDim.x) hist[(int64_t)d * ntiles + blockIdx.x] = h[d];
+}
+
+// Exclusive scan of v over the block's threads (kRadixThreads); returns the
+// prefix of this thread.  `warp_tot` is kRadixWarps words of shared memory.
+__device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned* warp_tot) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  unsigned before = 0;
+  for (int w = 0; w < wid; ++w) before += warp_tot[w];
+  return before + incl - v;
+}
+
+// FINAL: write column = key & col_mask and the value (as float) to the CSR
+// arrays; otherwise write key and value to the next pass's buffers.
+template <bool FINAL>
+__global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(
+    const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t count, int shift, int bins,
+    int64_t ntiles, const int64_t* __restrict__ offs, unsigned long long* __restrict__ okeys,
+    uint32_t* __restrict__ ovals, int32_t* __restrict__ ocol, float* __restrict__ oval, unsigned long long col_mask) {
+  extern __shared__ __align__(16) unsigned char radix_smem[];
+  unsigned long long* skey = reinterpret_cast<unsigned long long*>(radix_smem);
+  uint32_t* sval = reinterpret_cast<uint32_t*>(radix_smem + sizeof(unsigned long long) * kRadixTile);
+  __shared__ unsigned wcnt[kRadixWarps][kMaxBins];  // per-warp digit counts, then start offsets
+  __shared__ unsigned tile_start[kMaxBins];          // tile-local start of each digit
+  __shared__ int64_t gstart[kMaxBins];               // global start of each digit for this tile
+  __shared__ unsigned warp_tot[kRadixWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const unsigned long long mask = (unsigned long long)(bins - 1);
+  const int64_t tbase = (int64_t)blockIdx.x * kRadixTile;
+  const int tcount = count - tbase < kRadixTile ? (int)(count - tbase) : kRadixTile;
+
+  for (int d = threadIdx.x; d < bins; d += blockDim.x) gstart[d] = offs[(int64_t)d * ntiles + blockIdx.x];
+  unsigned* my = wcnt[wid];
+  for (int d = lane; d < bins; d += 32) my[d] = 0;
+  __syncwarp();
+
+  // Phase 1: warp-local stable ranks (rounds in index order, lanes in order).
+  unsigned long long k[kRadixItems];
+  uint32_t v[kRadixItems];
+  unsigned short rk[kRadixItems];
+  const int64_t wbase = tbase + (int64_t)wid * kWarpItems;
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const int64_t i = wbase + r * 32 + lane;
+    int d = kNoDigit;
+    k[r] = 0;
+    v[r] = 0;
+    if (i < count) {
+      k[r] = keys[i];
+      v[r] = vals[i];
+      d = (int)((k[r] >> shift) & mask);
+    }
+    const unsigned peers = __match_any_sync(kFull, d);
+    const unsigned before = d != kNoDigit ? my[d] : 0u;
+    __syncwarp();
+    rk[r] = (unsigned short)(before + __popc(peers & lt));
+    if (d != kNoDigit && lane == __ffs(peers) - 1) my[d] = before + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // Phase 2: tile totals per digit, their exclusive scan, and each warp's
+  // start per digit (warps in index order).
+  const int d0 = threadIdx.x;  // bins <= kRadixThreads
+  unsigned tot = 0;
+  if (d0 < bins)
+    for (int w = 0; w < kRadixWarps; ++w) tot += wcnt[w][d0];
+  const unsigned start = block_excl_scan_u32(tot, warp_tot);
+  if (d0 < bins) {
+    tile_start[d0] = start;
+    unsigned s = start;
+    for (int w = 0; w < kRadixWarps; ++w) {
+      const unsigned c = wcnt[w][d0];
+      wcnt[w][d0] = s;
+      s += c;
+    }
+  }
+  __syncthreads();
+
+  // Phase 3: reorder the tile by digit in shared memory.
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const int64_t i = wbase + r * 32 + lane;
+    if (i < count) {
+      const int d = (int)((k[r] >> shift) & mask);
+      const unsigned pos = my[d] + rk[r];
+      skey[pos] = k[r];
+      sval[pos] = v[r];
+    }
+  }
+  __syncthreads();
+
+  // Phase 4: write out; consecutive threads take consecutive items, which
+  // fall into runs of equal digits with consecutive global positions.
+  for (int j = threadIdx.x; j < tcount; j += kRadixThreads) {
+    const unsigned long long key = skey[j];
+    const int d = (int)((key >> shift) & mask);
+    const int64_t pos = gstart[d] + (j - (int)tile_start[d]);
+    if (FINAL) {
+      ocol[pos] = (int32_t)(key & col_mask);
+      oval[pos] = __uint_as_float(sval[j]);
+    } else {
+      okeys[pos] = key;
+      ovals[pos] = sval[j];
+    }
+  }
+}
+
+}  // namespace
+
+int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* vals, unsigned long long* keys_tmp,
+                            uint32_t* vals_tmp, int64_t count, int key_bits, unsigned long long col_mask,
+                            int32_t* out_col, float* out_val, int* launches) {
+  if (count <= 0) return LNE_OK;
+  if (key_bits < 1 || key_bits > 64) {
+    set_error("radix sort: key_bits must be in [1, 64]");
+    return LNE_ERR_INVALID;
+  }
+  cudaStream_t st = ctx->stream;
+  const int passes = (key_bits + 7) / 8;
+  const int dbits = (key_bits + passes - 1) / passes;  // <= 8
+  const int bins = 1 << dbits;
+  const int64_t ntiles = (count + kRadixTile - 1) / kRadixTile;
+  if (ntiles > 0x7fffffffLL) {
+    set_error("radix sort: too many items");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  const int64_t cells = (int64_t)bins * ntiles;
+  char* mem = nullptr;
+  const size_t hist_bytes = sizeof(int64_t) * (size_t)(cells + 1);
+  const size_t scan_bytes = (scan_tmp_bytes(cells) + 255) & ~(size_t)255;
+  int rc = dalloc(ctx, (void**)&mem, 2 * ((hist_bytes + 255) & ~(size_t)255) + scan_bytes, "radix histograms");
+  if (rc) return rc;
+  int64_t* hist = (int64_t*)mem;
+  int64_t* offs = (int64_t*)(mem + ((hist_bytes + 255) & ~(size_t)255));
+  void* scan_tmp = mem + 2 * ((hist_bytes + 255) & ~(size_t)255);
+  cudaFuncSetAttribute(k_radix_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
+  cudaFuncSetAttribute(k_radix_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
+  unsigned long long *src_k = keys, *dst_k = keys_tmp;
+  uint32_t *src_v = vals, *dst_v = vals_tmp;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = p * dbits;
+    k_radix_hist<<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src_k, count, shift, bins, ntiles, hist);
+    scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
+    if (p == passes - 1) {
+      k_radix_scatter<true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, bins, ntiles, offs, nullptr, nullptr, out_col, out_val, col_mask);
+    } else {
+      k_radix_scatter<false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, bins, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0);
+      std::swap(src_k, dst_k);
+      std::swap(src_v, dst_v);
+    }
+    if (launches) *launches += 5;  // histogram, 3-launch scan, scatter
+  }
+  dfree(ctx, mem);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("radix sort: kernel launch failed: ") + cudaGetErrorString(e));
+    return LNE_ERR_CUDA;
+  }
+  return LNE_OK;
+}
+
+}  // namespace lne

@@ -1,0 +1,19 @@
+// Device radix sort used by the CSR build of the sparsifier.
+#pragma once
+#include <stdint.h>
+
+#include "lne_internal.h"
+
+namespace lne {
+
+// Sorts `count` (key, value) pairs by the low `key_bits` bits of the key,
+// stably, in ceil(key_bits / 8) passes on ctx->stream, and writes the result
+// as CSR columns (key & col_mask, int32) and values (value bits as float).
+// keys/vals are overwritten; keys_tmp/vals_tmp are scratch of the same size.
+// Bits of the key above key_bits must be zero.  Launches are added to
+// *launches when it is not NULL.
+int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* vals, unsigned long long* keys_tmp,
+                            uint32_t* vals_tmp, int64_t count, int key_bits, unsigned long long col_mask,
+                            int32_t* out_col, float* out_val, int* launches);
+
+}  // namespace lne

@@ -6,9 +6,10 @@
 //
 // Layout in HBM during one call:
 //   table   Slot[capacity]       16 B per slot: u64 key, u64 count (or f64 weight)
-//   rowcnt  i64[n]               kept entries per row, then the scatter cursor
+//   rowcnt  i64[n]               kept entries per row
 //   row_ptr i64[n+1]             exclusive scan of rowcnt (the output row_ptr)
-//   packed  u64[nnz]             (col << 32 | float bits) per entry; rows sorted in place
+//   items   u64[nnz] + u32[nnz]  (row << cbits | col, float bits) per CSR entry,
+//                                twice (ping-pong buffers of the radix sort)
 //   col/val i32[nnz], f32[nnz]   output CSR
 #include <cuda_runtime.h>
 #include <math.h>
@@ -19,6 +20,7 @@
 
 #include "lne_internal.h"
 #include "lne_math.cuh"
+#include "radix.h"
 
 namespace lne {
 
@@ -351,8 +353,11 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 }
 
 // Trunc-log map (PathEmbed.h:203-218) fused with the per-row counts of the
-// CSR build (PathEmbed.h:226-288).  Kept slots get the float bits of the
-// log value in `val`; dropped slots become empty.
+// CSR build (PathEmbed.h:226-288).  Every kept entry (u, v) is appended to
+// the item list as key u << cbits | v with the float bits of its log value,
+// and, unless -upper or u == v, also as (v, u) (PathEmbed.h:300-311).  The
+// append order depends on scheduling; the keys are distinct, so the radix
+// sort by key that follows makes the CSR independent of it.
 //
 // Counts (-sample 0): adj = ((w * factor) / d_u) / d_v is reproduced
 // exactly by integer arithmetic (the reference's three double roundings),
@@ -361,10 +366,14 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 // result cannot decide go through FP64 (trunc_log_value).  Weights
 // (-sample 1) take the FP64 path throughout.
 template <bool WEIGHTED>
-__global__ void __launch_bounds__(256) k_trunclog(Slot* __restrict__ T, uint64_t cap, const Vertex* __restrict__ vd,
-                                                  double factor, int upper, const LogTable* __restrict__ ltab,
+__global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, uint64_t cap,
+                                                  const Vertex* __restrict__ vd, double factor, int upper,
+                                                  const LogTable* __restrict__ ltab,
                                                   unsigned long long* __restrict__ rowcnt,
-                                                  unsigned long long* __restrict__ kept_total) {
+                                                  unsigned long long* __restrict__ kept_total,
+                                                  unsigned long long* __restrict__ n_items, int cbits,
+                                                  uint64_t max_items, unsigned long long* __restrict__ okeys,
+                                                  uint32_t* __restrict__ ovals, int* __restrict__ flags) {
   __shared__ LogTable tab;
   for (int i = threadIdx.x; i < 128; i += blockDim.x) {
     tab.log_hi[i] = ltab->log_hi[i];
@@ -374,250 +383,72 @@ __global__ void __launch_bounds__(256) k_trunclog(Slot* __restrict__ T, uint64_t
   }
   __syncthreads();
   const XDouble xf = xd_from_double(factor);
-  unsigned long long kept = 0;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
-    const unsigned long long key = T[i].key;
-    if (key == kEmptyKey) continue;
-    const uint32_t u = (uint32_t)(key >> 32), v = (uint32_t)key;
-    const uint4 ru = __ldg(reinterpret_cast<const uint4*>(vd + u));
-    const uint4 rv = __ldg(reinterpret_cast<const uint4*>(vd + v));
-    const unsigned long long raw = T[i].val;
-    float f = 0.0f;
-    bool keep;
-    if (WEIGHTED) {
-      double w = __longlong_as_double((long long)raw);
-      if (u == v) w = __dmul_rn(w, 2.0);
-      const double adj = __ddiv_rn(__ddiv_rn(__dmul_rn(w, factor), (double)ru.y), (double)rv.y);
-      const double L = trunc_log_value(adj);
-      keep = L > 0.0;
-      if (keep) f = __double2float_rn(L);
-    } else {
-      const XDouble adj = trunc_log_adj(raw, u == v, xf, ru.y, ((uint64_t)ru.w << 32) | ru.z, rv.y,
-                                        ((uint64_t)rv.w << 32) | rv.z);
-      keep = adj.e > -52 || (adj.e == -52 && adj.m > (1ull << 52));  // adj > 1  <=>  log(adj) > 0
-      if (keep && !float_of_log_fast(log_df(adj, tab), &f)) f = __double2float_rn(trunc_log_value(xd_to_double(adj)));
-    }
-    if (keep) {
-      T[i].val = (unsigned long long)__float_as_uint(f);
-      atomicAdd(&rowcnt[u], 1ULL);
-      if (!upper && u != v) atomicAdd(&rowcnt[v], 1ULL);
-      ++kept;
-    } else {
-      T[i].key = kEmptyKey;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) kept += __shfl_down_sync(0xffffffffu, kept, o);
-  if ((threadIdx.x & 31) == 0 && kept) atomicAdd(kept_total, kept);
-}
-
-// Scatter each kept entry into its row (and the mirrored row unless -upper),
-// PathEmbed.h:300-311.  rowcnt serves as a decrementing cursor.
-__global__ void k_scatter(const Slot* __restrict__ T, uint64_t cap, const int64_t* __restrict__ row_ptr,
-                          unsigned long long* __restrict__ cursor, int upper, uint64_t* __restrict__ packed) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
-    const unsigned long long key = T[i].key;
-    if (key == kEmptyKey) continue;
-    const uint32_t u = (uint32_t)(key >> 32), v = (uint32_t)key;
-    const uint64_t fb = (uint32_t)T[i].val;
-    unsigned long long p = atomicAdd(&cursor[u], ~0ULL) - 1ULL;  // decrement
-    packed[row_ptr[u] + (int64_t)p] = ((uint64_t)v << 32) | fb;
-    if (!upper && u != v) {
-      p = atomicAdd(&cursor[v], ~0ULL) - 1ULL;
-      packed[row_ptr[v] + (int64_t)p] = ((uint64_t)u << 32) | fb;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Per-row sort of the packed entries (ascending column), by row length class.
-// All classes use the ascending bitonic network in which the first
-// comparator of each merge stage pairs i with i ^ (k-1) and the following
-// ones pair i with i ^ j.  Every comparator keeps the minimum at the lower
-// index, so a row of length L sorts in place as if padded with +inf up to
-// the next power of two: comparators that touch an index >= L never swap.
-// Rows longer than kCapXL are cut into kCapXL-entry segments sorted the same
-// way, then merged pairwise in global memory (merge path).
-// ---------------------------------------------------------------------------
-enum RowClass { kClsWarp = 0, kClsS = 1, kClsM = 2, kClsL = 3, kClsXL = 4, kClsHuge = 5, kNumCls = 6 };
-static constexpr int kCapS = 256, kCapM = 1024, kCapL = 4096, kCapXL = 16384;
-
-struct Segment {  // a run of packed entries to sort in shared memory
-  int64_t start;
-  int32_t len;
-  int32_t final_;  // 1: a whole row, write col/val; 0: a chunk of a long row
-};
-
-__device__ __forceinline__ void unpack_store(uint64_t x, int32_t* col, float* val, int64_t j) {
-  col[j] = (int32_t)(x >> 32);
-  val[j] = __uint_as_float((uint32_t)x);
-}
-
-// cls_cnt: [kNumCls] counts, [kNumCls] = total entries of huge rows,
-// [kNumCls + 1] = longest huge row.
-__global__ void k_classify_rows(const int64_t* __restrict__ row_ptr, int64_t n, const uint64_t* __restrict__ packed,
-                                int32_t* __restrict__ col, float* __restrict__ val, unsigned long long* __restrict__ cls_cnt,
-                                uint32_t* __restrict__ cls_rows, int64_t list_stride, Segment* __restrict__ segs) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int64_t a = row_ptr[i], L = row_ptr[i + 1] - a;
-  if (L == 0) return;
-  if (L == 1) {
-    unpack_store(packed[a], col, val, a);
-    return;
-  }
-  if (L <= kCapL) {
-    const int c = L <= 32 ? kClsWarp : L <= kCapS ? kClsS : L <= kCapM ? kClsM : kClsL;
-    const unsigned long long slot = atomicAdd(&cls_cnt[c], 1ULL);
-    cls_rows[(int64_t)c * list_stride + (int64_t)slot] = (uint32_t)i;
-    return;
-  }
-  if (L <= kCapXL) {
-    const unsigned long long slot = atomicAdd(&cls_cnt[kClsXL], 1ULL);
-    segs[slot] = Segment{a, (int32_t)L, 1};
-    return;
-  }
-  const int64_t nseg = (L + kCapXL - 1) / kCapXL;
-  const unsigned long long s0 = atomicAdd(&cls_cnt[kClsXL], (unsigned long long)nseg);
-  for (int64_t c = 0; c < nseg; ++c) {
-    const int64_t b = c * kCapXL;
-    const int64_t len = (L - b) < kCapXL ? (L - b) : kCapXL;
-    segs[s0 + c] = Segment{a + b, (int32_t)len, 0};
-  }
-  const unsigned long long h = atomicAdd(&cls_cnt[kClsHuge], 1ULL);
-  cls_rows[(int64_t)kClsHuge * list_stride + (int64_t)h] = (uint32_t)i;
-  atomicAdd(&cls_cnt[kNumCls], (unsigned long long)L);
-  atomicMax(&cls_cnt[kNumCls + 1], (unsigned long long)L);
-}
-
-__global__ void k_sort_warp_rows(const int64_t* __restrict__ row_ptr, const unsigned long long* __restrict__ cls_cnt,
-                                 const uint32_t* __restrict__ rows, const uint64_t* __restrict__ packed,
-                                 int32_t* __restrict__ col, float* __restrict__ val) {
   const int lane = threadIdx.x & 31;
-  const int64_t nrows = (int64_t)cls_cnt[kClsWarp];
-  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nrows;
-       w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const uint32_t r = rows[w];
-    const int64_t a = row_ptr[r];
-    const int L = (int)(row_ptr[r + 1] - a);
-    uint64_t x = lane < L ? packed[a + lane] : ~0ULL;
+  unsigned long long kept = 0;
+  // warp-uniform loop: the lanes of a warp take 32 consecutive slots
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < cap; b += stride) {
+    const uint64_t i = b + lane;
+    unsigned nitem = 0;
+    uint32_t u = 0, v = 0;
+    float f = 0.0f;
+    const unsigned long long key = i < cap ? T[i].key : kEmptyKey;
+    if (key != kEmptyKey) {
+      u = (uint32_t)(key >> 32);
+      v = (uint32_t)key;
+      const uint4 ru = __ldg(reinterpret_cast<const uint4*>(vd + u));
+      const uint4 rv = __ldg(reinterpret_cast<const uint4*>(vd + v));
+      const unsigned long long raw = T[i].val;
+      bool keep;
+      if (WEIGHTED) {
+        double w = __longlong_as_double((long long)raw);
+        if (u == v) w = __dmul_rn(w, 2.0);
+        const double adj = __ddiv_rn(__ddiv_rn(__dmul_rn(w, factor), (double)ru.y), (double)rv.y);
+        const double L = trunc_log_value(adj);
+        keep = L > 0.0;
+        if (keep) f = __double2float_rn(L);
+      } else {
+        const XDouble adj = trunc_log_adj(raw, u == v, xf, ru.y, ((uint64_t)ru.w << 32) | ru.z, rv.y,
+                                          ((uint64_t)rv.w << 32) | rv.z);
+        keep = adj.e > -52 || (adj.e == -52 && adj.m > (1ull << 52));  // adj > 1  <=>  log(adj) > 0
+        if (keep && !float_of_log_fast(log_df(adj, tab), &f))
+          f = __double2float_rn(trunc_log_value(xd_to_double(adj)));
+      }
+      if (keep) {
+        nitem = (upper || u == v) ? 1u : 2u;
+        atomicAdd(&rowcnt[u], 1ULL);
+        if (nitem == 2) atomicAdd(&rowcnt[v], 1ULL);
+        ++kept;
+      }
+    }
+    __syncwarp();
+    unsigned incl = nitem;
 #pragma unroll
-    for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        const int partner = (j == (k >> 1)) ? (lane ^ (k - 1)) : (lane ^ j);
-        const uint64_t y = __shfl_sync(0xffffffffu, x, partner);
-        const bool low = lane < partner;
-        x = low ? (x < y ? x : y) : (x < y ? y : x);
-      }
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(kFullMask, incl, o);
+      if (lane >= o) incl += t;
     }
-    if (lane < L) unpack_store(x, col, val, a + lane);
-  }
-}
-
-__device__ __forceinline__ void bitonic_smem(uint64_t* s, int L) {
-  int N = 1;
-  while (N < L) N <<= 1;
-  const int half = N >> 1;
-  for (int k = 2; k <= N; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int c = threadIdx.x; c < half; c += blockDim.x) {
-        int i, l;
-        if (j == (k >> 1)) {
-          const int blk = c / j, pos = c % j;
-          i = blk * k + pos;
-          l = blk * k + k - 1 - pos;
-        } else {
-          i = (c / j) * 2 * j + (c % j);
-          l = i + j;
+    const unsigned wtot = __shfl_sync(kFullMask, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && wtot) base = atomicAdd(n_items, (unsigned long long)wtot);
+    base = __shfl_sync(kFullMask, base, 31);
+    if (nitem) {
+      const uint64_t pos = base + incl - nitem;
+      if (pos + nitem <= max_items) {
+        const uint32_t fb = __float_as_uint(f);
+        okeys[pos] = ((unsigned long long)u << cbits) | v;
+        ovals[pos] = fb;
+        if (nitem == 2) {
+          okeys[pos + 1] = ((unsigned long long)v << cbits) | u;
+          ovals[pos + 1] = fb;
         }
-        if (l < L) {
-          const uint64_t x = s[i], y = s[l];
-          if (x > y) { s[i] = y; s[l] = x; }
-        }
-      }
-      __syncthreads();
-    }
-  }
-}
-
-template <int CLS>
-__global__ void k_sort_block_rows(const int64_t* __restrict__ row_ptr, const unsigned long long* __restrict__ cls_cnt,
-                                  const uint32_t* __restrict__ rows, const uint64_t* __restrict__ packed,
-                                  int32_t* __restrict__ col, float* __restrict__ val) {
-  extern __shared__ uint64_t sbuf[];
-  const int64_t nrows = (int64_t)cls_cnt[CLS];
-  for (int64_t w = blockIdx.x; w < nrows; w += gridDim.x) {
-    const uint32_t r = rows[w];
-    const int64_t a = row_ptr[r];
-    const int L = (int)(row_ptr[r + 1] - a);
-    for (int i = threadIdx.x; i < L; i += blockDim.x) sbuf[i] = packed[a + i];
-    __syncthreads();
-    bitonic_smem(sbuf, L);
-    for (int i = threadIdx.x; i < L; i += blockDim.x) unpack_store(sbuf[i], col, val, a + i);
-    __syncthreads();
-  }
-}
-
-// Segments of up to kCapXL entries: whole rows write col/val, chunks of
-// long rows are written back sorted in place for the merge passes.
-__global__ void k_sort_segments(const unsigned long long* __restrict__ cls_cnt, const Segment* __restrict__ segs,
-                                uint64_t* __restrict__ packed, int32_t* __restrict__ col, float* __restrict__ val) {
-  extern __shared__ uint64_t sbuf[];
-  const int64_t nseg = (int64_t)cls_cnt[kClsXL];
-  for (int64_t w = blockIdx.x; w < nseg; w += gridDim.x) {
-    const Segment sg = segs[w];
-    for (int i = threadIdx.x; i < sg.len; i += blockDim.x) sbuf[i] = packed[sg.start + i];
-    __syncthreads();
-    bitonic_smem(sbuf, sg.len);
-    if (sg.final_) {
-      for (int i = threadIdx.x; i < sg.len; i += blockDim.x) unpack_store(sbuf[i], col, val, sg.start + i);
-    } else {
-      for (int i = threadIdx.x; i < sg.len; i += blockDim.x) packed[sg.start + i] = sbuf[i];
-    }
-    __syncthreads();
-  }
-}
-
-// One merge pass over the long rows: runs of `run` sorted entries are merged
-// pairwise from `src` into `dst` (same offsets).  One block per (row, pair);
-// each thread finds its split of the merged output by binary search along
-// the merge-path diagonal and merges its share sequentially.  The last pass
-// writes col/val instead of dst.
-__global__ void k_merge_pass(const int64_t* __restrict__ row_ptr, const unsigned long long* __restrict__ cls_cnt,
-                             const uint32_t* __restrict__ rows, const uint64_t* __restrict__ src,
-                             uint64_t* __restrict__ dst, int64_t run, int last, int32_t* __restrict__ col,
-                             float* __restrict__ val) {
-  const int64_t nrows = (int64_t)cls_cnt[kClsHuge];
-  for (int64_t w = blockIdx.x; w < nrows; w += gridDim.x) {
-    const uint32_t r = rows[w];
-    const int64_t base = row_ptr[r];
-    const int64_t L = row_ptr[r + 1] - base;
-    for (int64_t p0 = 0; p0 < L; p0 += 2 * run) {
-      const int64_t na = (L - p0) < run ? (L - p0) : run;
-      const int64_t rest = L - p0 - na;
-      const int64_t nb = rest < run ? rest : run;
-      const uint64_t* A = src + base + p0;
-      const uint64_t* B = A + na;
-      const int64_t tot = na + nb;
-      const int64_t per = (tot + blockDim.x - 1) / blockDim.x;
-      const int64_t d0 = (int64_t)threadIdx.x * per;
-      if (d0 < tot) {
-        const int64_t d1 = (d0 + per) < tot ? (d0 + per) : tot;
-        // largest i in [max(0, d0-nb), min(d0, na)] with A[i-1] <= B[d0-i]
-        int64_t lo = d0 - nb > 0 ? d0 - nb : 0, hi = d0 < na ? d0 : na;
-        while (lo < hi) {
-          const int64_t mid = (lo + hi + 1) >> 1;
-          if (A[mid - 1] <= B[d0 - mid]) lo = mid; else hi = mid - 1;
-        }
-        int64_t i = lo, j = d0 - lo;
-        for (int64_t o = d0; o < d1; ++o) {
-          uint64_t x;
-          if (j >= nb || (i < na && A[i] <= B[j])) x = A[i++]; else x = B[j++];
-          if (last) unpack_store(x, col, val, base + p0 + o); else dst[base + p0 + o] = x;
-        }
+      } else {
+        atomicOr(&flags[kFlagSortOverflow], 1);
       }
     }
   }
+  for (int o = 16; o > 0; o >>= 1) kept += __shfl_down_sync(kFullMask, kept, o);
+  if (lane == 0 && kept) atomicAdd(kept_total, kept);
 }
 
 static unsigned grid_for(int64_t items, int threads, int64_t cap_blocks) {
@@ -639,6 +470,10 @@ struct Scratch {
   int k = 0;
   explicit Scratch(lne_ctx* c) : ctx(c) {}
   int get(void** out, size_t bytes, const char* what) {
+    if (k == 12) {
+      set_error("lne_sparsify: scratch list full (internal)");
+      return LNE_ERR_UNSUPPORTED;
+    }
     int rc = dalloc(ctx, out, bytes, what);
     if (rc == LNE_OK) p[k++] = *out;
     return rc;
@@ -785,92 +620,69 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   const double vol = (double)(size_t)m_dir;
   const double factor = vol * (double)(size_t)m_dir / M_exact / 2 / (double)(size_t)p->negative;
 
+  // Item keys: row << cbits | col with cbits bits per vertex id.
+  int cbits = 1;
+  while (cbits < 32 && ((int64_t)1 << cbits) < n) ++cbits;
+  const uint64_t max_items = 2 * (uint64_t)h_cnt[2] + 1;  // each distinct pair gives at most 2 entries
   unsigned long long* rowcnt = nullptr;
   int64_t* row_ptr = nullptr;
   void* scan_tmp = nullptr;
+  unsigned long long* ikeys = nullptr;
+  uint32_t* ivals = nullptr;
   if ((rc = S.get((void**)&rowcnt, sizeof(unsigned long long) * n, "row counts"))) return rc;
+  if ((rc = S.get(&scan_tmp, scan_tmp_bytes(n), "scan scratch"))) return rc;
+  if ((rc = S.get((void**)&ikeys, sizeof(unsigned long long) * max_items, "csr items"))) return rc;
+  if ((rc = S.get((void**)&ivals, sizeof(uint32_t) * max_items, "csr item values"))) return rc;
   if ((rc = dalloc(ctx, (void**)&row_ptr, sizeof(int64_t) * (n + 1), "row_ptr"))) return rc;
-  if ((rc = S.get(&scan_tmp, scan_tmp_bytes(n), "scan scratch"))) { dfree(ctx, row_ptr); return rc; }
   LNE_CUDA_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(unsigned long long) * n, st));
   if (p->sample)
     k_trunclog<true><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper,
-                                            (const LogTable*)ctx->log_table, rowcnt, counters + 3);
+                                            (const LogTable*)ctx->log_table, rowcnt, counters + 3, counters + 4,
+                                            cbits, max_items, ikeys, ivals, ctx->d_flags);
   else
     k_trunclog<false><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper,
-                                             (const LogTable*)ctx->log_table, rowcnt, counters + 3);
+                                             (const LogTable*)ctx->log_table, rowcnt, counters + 3, counters + 4,
+                                             cbits, max_items, ikeys, ivals, ctx->d_flags);
+  S.release(table);
   cudaEventRecord(ev.e[2], st);
   scan_exclusive_i64((const int64_t*)rowcnt, row_ptr, n, scan_tmp, st);
   int64_t nnz = 0;
-  unsigned long long kept = 0;
+  unsigned long long tail[2] = {0, 0};  // kept upper entries, appended items
   LNE_CUDA_TRY(cudaMemcpyAsync(&nnz, row_ptr + n, 8, cudaMemcpyDeviceToHost, st));
-  LNE_CUDA_TRY(cudaMemcpyAsync(&kept, counters + 3, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(tail, counters + 3, sizeof(tail), cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaMemcpyAsync(h_flags, ctx->d_flags, sizeof(h_flags), cudaMemcpyDeviceToHost, st));
   LNE_CUDA_TRY(cudaStreamSynchronize(st));
   LNE_CUDA_TRY(cudaGetLastError());
-
-  uint64_t* packed = nullptr;
-  if ((rc = S.get((void**)&packed, sizeof(uint64_t) * (nnz > 0 ? nnz : 1), "packed entries"))) {
+  const unsigned long long kept = tail[0];
+  if (h_flags[kFlagSortOverflow] || tail[1] != (unsigned long long)nnz) {
     dfree(ctx, row_ptr);
-    return rc;
+    set_error("lne_sparsify: CSR item count does not match the row counts (internal sizing error)");
+    return LNE_ERR_UNSUPPORTED;
   }
-  k_scatter<<<tgrid, 256, 0, st>>>(table, cap, row_ptr, rowcnt, p->upper, packed);
-  S.release(table);
   S.release(rowcnt);
+  S.release(scan_tmp);
 
+  // Sort the items by (row, col) and write the CSR columns and values.
   int32_t* col = nullptr;
   float* val = nullptr;
-  unsigned long long* cls_cnt = nullptr;
-  uint32_t* cls_rows = nullptr;
-  Segment* segs = nullptr;
-  const int64_t max_segs = n + nnz / kCapXL + 8;
+  unsigned long long* tkeys = nullptr;
+  uint32_t* tvals = nullptr;
   if ((rc = dalloc(ctx, (void**)&col, sizeof(int32_t) * (nnz > 0 ? nnz : 1), "csr col")) ||
       (rc = dalloc(ctx, (void**)&val, sizeof(float) * (nnz > 0 ? nnz : 1), "csr val")) ||
-      (rc = S.get((void**)&cls_cnt, sizeof(unsigned long long) * 16, "row classes")) ||
-      (rc = S.get((void**)&cls_rows, sizeof(uint32_t) * kNumCls * n, "row class lists")) ||
-      (rc = S.get((void**)&segs, sizeof(Segment) * max_segs, "sort segments"))) {
+      (rc = S.get((void**)&tkeys, sizeof(unsigned long long) * (nnz > 0 ? nnz : 1), "sort keys")) ||
+      (rc = S.get((void**)&tvals, sizeof(uint32_t) * (nnz > 0 ? nnz : 1), "sort values"))) {
     dfree(ctx, row_ptr);
     dfree(ctx, col);
     dfree(ctx, val);
     return rc;
   }
-  LNE_CUDA_TRY(cudaMemsetAsync(cls_cnt, 0, sizeof(unsigned long long) * 16, st));
-  int launches = 13 + launches_sample;  // 7 + walk/insert before this point, 6 sort launches below
-  k_classify_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(row_ptr, n, packed, col, val, cls_cnt, cls_rows, n,
-                                                               segs);
-  const int64_t sms = ctx->num_sms;
-  k_sort_warp_rows<<<(unsigned)(sms * 16), 256, 0, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsWarp * n, packed,
-                                                          col, val);
-  k_sort_block_rows<kClsS><<<(unsigned)(sms * 16), 128, kCapS * 8, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsS * n,
-                                                                         packed, col, val);
-  k_sort_block_rows<kClsM><<<(unsigned)(sms * 8), 256, kCapM * 8, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsM * n,
-                                                                        packed, col, val);
-  k_sort_block_rows<kClsL><<<(unsigned)(sms * 4), 512, kCapL * 8, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsL * n,
-                                                                        packed, col, val);
-  cudaFuncSetAttribute(k_sort_segments, cudaFuncAttributeMaxDynamicSharedMemorySize, kCapXL * 8);
-  k_sort_segments<<<(unsigned)sms, 1024, kCapXL * 8, st>>>(cls_cnt, segs, packed, col, val);
-  unsigned long long h_cls[16];
-  LNE_CUDA_TRY(cudaMemcpyAsync(h_cls, cls_cnt, sizeof(h_cls), cudaMemcpyDeviceToHost, st));
-  LNE_CUDA_TRY(cudaStreamSynchronize(st));
-  if (h_cls[kClsHuge] > 0) {
-    uint64_t* other = nullptr;
-    if ((rc = S.get((void**)&other, sizeof(uint64_t) * (nnz > 0 ? nnz : 1), "merge buffer"))) {
-      dfree(ctx, row_ptr);
-      dfree(ctx, col);
-      dfree(ctx, val);
-      return rc;
-    }
-    const int64_t maxL = (int64_t)h_cls[kNumCls + 1];
-    uint64_t* src = packed;
-    uint64_t* dst = other;
-    const unsigned mgrid = (unsigned)std::min<int64_t>((int64_t)h_cls[kClsHuge], sms * 8);
-    for (int64_t run = kCapXL; run < maxL; run *= 2) {
-      const int last = (2 * run >= maxL) ? 1 : 0;
-      k_merge_pass<<<mgrid, 512, 0, st>>>(row_ptr, cls_cnt, cls_rows + (int64_t)kClsHuge * n, src, dst, run, last,
-                                          col, val);
-      ++launches;
-      uint64_t* t = src;
-      src = dst;
-      dst = t;
-    }
+  int launches = 7 + launches_sample;  // init, table sum, block sum, trunc-log, 3 scan + walk/insert
+  if ((rc = radix_sort_pairs_to_csr(ctx, ikeys, ivals, tkeys, tvals, nnz, 2 * cbits, ((1ULL << cbits) - 1), col,
+                                    val, &launches))) {
+    dfree(ctx, row_ptr);
+    dfree(ctx, col);
+    dfree(ctx, val);
+    return rc;
   }
   cudaEventRecord(ev.e[3], st);
   cudaError_t le = cudaGetLastError();
@@ -899,8 +711,6 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     cudaEventElapsedTime(&stats->ms_sample, ev.e[0], ev.e[1]);
     cudaEventElapsedTime(&stats->ms_trunclog, ev.e[1], ev.e[2]);
     cudaEventElapsedTime(&stats->ms_csr, ev.e[2], ev.e[3]);
-    // init, sample, table sum, block sum, trunc-log, 3 scan, scatter,
-    // classify, 5 row-sort classes, merge passes
     stats->kernel_launches = launches;
   }
   lne_csr* c = new lne_csr();
