@@ -254,8 +254,9 @@ int lne_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int64_t k, const f
  * Allocation-free lne_gram, with no counterpart in the reference: for
  * callers that cannot allocate device memory when they need the product (a
  * process whose device memory belongs to another allocator or fixed arena,
- * or one under a hard memory cap).  Same result as lne_gram; its scratch is
- * a 16 MiB file-scope device array that every GPU loading the library holds
+ * or one under a hard memory cap).  The same product as lne_gram to FP32
+ * accuracy (the row blocks may differ); its scratch is a 16 MiB file-scope
+ * device array that every GPU loading the library holds
  * until exit, so ceil(n / 2048) * c1 * c2 must be at most 4,194,304 and
  * c2 at most 256 (else LNE_ERR_UNSUPPORTED).  The first call on a device
  * looks up the array's device address (make it before any stream capture).

@@ -121,21 +121,29 @@ __global__ void k_gram_reduce(const float* __restrict__ partial, int64_t nb, int
   G[t] = s;
 }
 
-int gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
-         double* G) {
-  if (tc_supported(c2)) return tc_gram(ctx, A, lda, c1, B, ldb, c2, n, G);
+int gram_simt_into(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+                   double* G, float* partial) {
   const int64_t nb = std::max<int64_t>(1, (n + kGramRows - 1) / kGramRows);
   const int tiles_i = (c1 + 63) / 64, tiles_j = (c2 + 63) / 64;
-  float* partial = nullptr;
-  int rc = dalloc(ctx, (void**)&partial, sizeof(float) * nb * c1 * c2, "gram partials");
-  if (rc) return rc;
   dim3 grid((unsigned)(tiles_i * tiles_j), (unsigned)nb);
   k_gram_partial<<<grid, 256, 0, ctx->stream>>>(A, lda, c1, B, ldb, c2, n, partial, tiles_j);
   const int64_t cnt = (int64_t)c1 * c2;
   k_gram_reduce<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, cnt, G);
-  dfree(ctx, partial);
   LNE_CUDA_TRY(cudaGetLastError());
   return LNE_OK;
+}
+
+int gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+         double* G) {
+  if (tc_supported(c2) && tc_gram_stream_supported(ctx, A, lda, c1, B, ldb, c2))
+    return tc_gram_stream(ctx, A, lda, c1, B, ldb, c2, n, G, nullptr, ctx->num_sms);
+  const int64_t nb = std::max<int64_t>(1, (n + kGramRows - 1) / kGramRows);
+  float* partial = nullptr;
+  int rc = dalloc(ctx, (void**)&partial, sizeof(float) * nb * c1 * c2, "gram partials");
+  if (rc) return rc;
+  rc = gram_simt_into(ctx, A, lda, c1, B, ldb, c2, n, G, partial);
+  dfree(ctx, partial);
+  return rc;
 }
 
 // ---------------------------------------------------------------------------

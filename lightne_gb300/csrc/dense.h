@@ -43,15 +43,20 @@ int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps
 // tcgen05 tensor-core versions (3xTF32, FP32-level accuracy) of gram and
 // gemm_tall for up to 256 columns; gram/gemm_tall use them when they apply.
 bool tc_supported(int c2);
-int tc_gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
-            double* G);
 int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
                  int64_t ldo, __nv_bfloat16* OutB);
-
-// tc_gram with caller-provided partial storage (nb * c1 * c2 floats,
-// nb = ceil(n / 2048)); allocates nothing.
-int tc_gram_into(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
-                 double* G, float* partial);
+// Streaming tensor-core Gram: applies when both operands are 16-byte aligned
+// with row strides that are multiples of 4 floats and the shape fits.  Uses
+// at most max_blocks CTAs; `partial` (NULL: allocated here) holds
+// blocks * c1 * c2 floats.
+bool tc_gram_stream_supported(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb,
+                              int c2);
+int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+                   double* G, float* partial, int64_t max_blocks);
+// CUDA-core Gram with caller-provided partial storage (ceil(n / 2048) * c1 *
+// c2 floats); allocates nothing.
+int gram_simt_into(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+                   double* G, float* partial);
 
 // Copies an FP32 tall matrix into a BF16 copy (same ld).
 int to_bf16(lne_ctx* ctx, const float* X, int64_t n, int64_t ld, __nv_bfloat16* Y);

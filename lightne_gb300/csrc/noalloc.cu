@@ -4,10 +4,11 @@
 // product: a host process whose device memory is owned entirely by another
 // allocator (a framework's caching pool, a fixed arena handed out by an
 // embedding service), or code running under a hard per-process memory cap.
-// For them this entry point computes the same G = A^T B as lne_gram but
-// takes its scratch — the FP32 partial sums of the 2048-row blocks — from a
-// file-scope device array instead of cudaMallocAsync, and calls no
-// cudaMalloc, cudaFree or allocating library routine.
+// For them this entry point computes the same G = A^T B as lne_gram (the
+// streaming tensor-core Gram where it applies, else the CUDA-core one) but
+// takes its scratch — the FP32 partial sums of at most ceil(n / 2048) row
+// blocks — from a file-scope device array instead of cudaMallocAsync, and
+// calls no cudaMalloc, cudaFree or allocating library routine.
 //
 // The array is a module-scope __device__ variable: every GPU that loads this
 // library holds its 16 MiB until the process exits.  In host code the
@@ -72,7 +73,7 @@ extern "C" int lne_gram_noalloc(lne_ctx* ctx, const float* A, int64_t lda, int64
   LNE_CHECK_ARG(ctx && A && B && G && n >= 1 && c1 >= 1 && c2 >= 1 && lda >= c1 && ldb >= c2,
                 "lne_gram_noalloc: bad argument");
   if (c2 > 256) {
-    set_error("lne_gram_noalloc: at most 256 columns of B (the tensor-core path)");
+    set_error("lne_gram_noalloc: at most 256 columns of B");
     return LNE_ERR_UNSUPPORTED;
   }
   const int64_t nb = (n + 2047) / 2048;
@@ -86,7 +87,10 @@ extern "C" int lne_gram_noalloc(lne_ctx* ctx, const float* A, int64_t lda, int64
   int rc = noalloc_scratch(ctx->device, &scratch);
   if (rc) return rc;
   LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, ctx->stream));
-  rc = tc_gram_into(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G, scratch);
+  if (tc_gram_stream_supported(ctx, A, lda, (int)c1, B, ldb, (int)c2))
+    rc = tc_gram_stream(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G, scratch, nb);
+  else
+    rc = gram_simt_into(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G, scratch);
   if (rc) return rc;
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   int h = 0;

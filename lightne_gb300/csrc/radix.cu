@@ -6,12 +6,13 @@
 //                    stored digit-major, so that one exclusive scan over
 //                    [digit][tile] gives every tile the output start of each
 //                    of its digits;
-//   k_radix_scatter  each warp ranks its 512 items of the tile with
-//                    match.any (lanes with equal digits in one step, rounds
-//                    in index order), the warps' counts are combined into
-//                    tile-local digit offsets, the tile is reordered by digit
-//                    in shared memory and then written out in runs of equal
-//                    digits, so that the global writes are contiguous.
+//   k_radix_scatter  each warp ranks its 512 items of the tile by warp
+//                    multisplit (lanes with equal digits found by one ballot
+//                    per digit bit; rounds in index order), the warps'
+//                    counts are combined into tile-local digit offsets, the
+//                    tile is reordered by digit in shared memory and then
+//                    written out in runs of equal digits, so that the global
+//                    writes are contiguous.
 // Items with equal digits keep their input order in every pass, so the sort
 // is stable.
 #include <cuda_runtime.h>
@@ -32,13 +33,29 @@ constexpr int kRadixItems = 16;                            // per thread
 constexpr int kRadixTile = kRadixThreads * kRadixItems;    // 4096 items
 constexpr int kWarpItems = 32 * kRadixItems;               // 512 items per warp
 constexpr int kMaxBins = 256;
-constexpr int kNoDigit = kMaxBins;                         // digit of a lane past the end
 constexpr unsigned kFull = 0xffffffffu;
 constexpr size_t kScatterSmem = (size_t)kRadixTile * (sizeof(unsigned long long) + sizeof(uint32_t));
 
+// Lanes of the warp whose `dbits`-bit digit equals this lane's, among the
+// lanes with `valid` set: one ballot per digit bit (warp multisplit; the
+// hardware match instruction is much slower for many distinct values).
+__device__ __forceinline__ unsigned match_digit(unsigned d, bool valid, int dbits) {
+  unsigned m = __ballot_sync(kFull, valid);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    if (b < dbits) {
+      const bool bit = (d >> b) & 1u;
+      const unsigned bb = __ballot_sync(kFull, bit);
+      m &= bit ? bb : ~bb;
+    }
+  }
+  return m;
+}
+
 __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const unsigned long long* __restrict__ keys,
-                                                               int64_t count, int shift, int bins, int64_t ntiles,
+                                                               int64_t count, int shift, int dbits, int64_t ntiles,
                                                                int64_t* __restrict__ hist) {
+  const int bins = 1 << dbits;
   __shared__ unsigned int h[kMaxBins];
   for (int i = threadIdx.x; i < bins; i += blockDim.x) h[i] = 0;
   __syncthreads();
@@ -48,9 +65,10 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const unsigned lon
 #pragma unroll 4
   for (int r = 0; r < kRadixItems; ++r) {
     const int64_t i = base + (int64_t)r * kRadixThreads + threadIdx.x;
-    const int d = i < count ? (int)((keys[i] >> shift) & mask) : kNoDigit;
-    const unsigned peers = __match_any_sync(kFull, d);
-    if (d != kNoDigit && lane == __ffs(peers) - 1) atomicAdd(&h[d], (unsigned)__popc(peers));
+    const bool valid = i < count;
+    const unsigned d = valid ? (unsigned)((keys[i] >> shift) & mask) : 0u;
+    const unsigned peers = match_digit(d, valid, dbits);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(&h[d], (unsigned)__popc(peers));
   }
   __syncthreads();
   for (int d = threadIdx.x; d < bins; d += blockDim.x) hist[(int64_t)d * ntiles + blockIdx.x] = h[d];
@@ -76,8 +94,8 @@ __device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned* wa
 // FINAL: write column = key & col_mask and the value (as float) to the CSR
 // arrays; otherwise write key and value to the next pass's buffers.
 template <bool FINAL>
-__global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(
-    const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t count, int shift, int bins,
+__global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
+    const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t count, int shift, int dbits,
     int64_t ntiles, const int64_t* __restrict__ offs, unsigned long long* __restrict__ okeys,
     uint32_t* __restrict__ ovals, int32_t* __restrict__ ocol, float* __restrict__ oval, unsigned long long col_mask) {
   extern __shared__ __align__(16) unsigned char radix_smem[];
@@ -89,6 +107,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(
   __shared__ unsigned warp_tot[kRadixWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
+  const int bins = 1 << dbits;
   const unsigned long long mask = (unsigned long long)(bins - 1);
   const int64_t tbase = (int64_t)blockIdx.x * kRadixTile;
   const int tcount = count - tbase < kRadixTile ? (int)(count - tbase) : kRadixTile;
@@ -106,19 +125,15 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
     const int64_t i = wbase + r * 32 + lane;
-    int d = kNoDigit;
-    k[r] = 0;
-    v[r] = 0;
-    if (i < count) {
-      k[r] = keys[i];
-      v[r] = vals[i];
-      d = (int)((k[r] >> shift) & mask);
-    }
-    const unsigned peers = __match_any_sync(kFull, d);
-    const unsigned before = d != kNoDigit ? my[d] : 0u;
+    const bool valid = i < count;
+    k[r] = valid ? keys[i] : 0ULL;
+    v[r] = valid ? vals[i] : 0u;
+    const unsigned d = (unsigned)((k[r] >> shift) & mask);
+    const unsigned peers = match_digit(d, valid, dbits);
+    const unsigned before = valid ? my[d] : 0u;
     __syncwarp();
     rk[r] = (unsigned short)(before + __popc(peers & lt));
-    if (d != kNoDigit && lane == __ffs(peers) - 1) my[d] = before + __popc(peers);
+    if (valid && lane == __ffs(peers) - 1) my[d] = before + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
@@ -204,14 +219,14 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
   uint32_t *src_v = vals, *dst_v = vals_tmp;
   for (int p = 0; p < passes; ++p) {
     const int shift = p * dbits;
-    k_radix_hist<<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src_k, count, shift, bins, ntiles, hist);
+    k_radix_hist<<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist);
     scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
     if (p == passes - 1) {
       k_radix_scatter<true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
-          src_k, src_v, count, shift, bins, ntiles, offs, nullptr, nullptr, out_col, out_val, col_mask);
+          src_k, src_v, count, shift, dbits, ntiles, offs, nullptr, nullptr, out_col, out_val, col_mask);
     } else {
       k_radix_scatter<false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
-          src_k, src_v, count, shift, bins, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0);
+          src_k, src_v, count, shift, dbits, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0);
       std::swap(src_k, dst_k);
       std::swap(src_v, dst_v);
     }

@@ -365,6 +365,47 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 // double-float; only values whose narrowing to float the double-float
 // result cannot decide go through FP64 (trunc_log_value).  Weights
 // (-sample 1) take the FP64 path throughout.
+//
+// The slots of a warp's stretch of the table are compacted into a per-warp
+// queue first (about a third of the slots are occupied), so that the
+// log evaluation runs with all 32 lanes busy.
+template <bool WEIGHTED>
+struct TruncLogOut {
+  unsigned nitem;  // 0, 1 or 2 CSR entries
+  uint32_t u, v;
+  float f;
+};
+
+template <bool WEIGHTED>
+__device__ __forceinline__ TruncLogOut<WEIGHTED> trunclog_entry(unsigned long long key, unsigned long long raw,
+                                                                const Vertex* __restrict__ vd, double factor,
+                                                                const XDouble& xf, int upper, const LogTable& tab) {
+  TruncLogOut<WEIGHTED> o;
+  o.nitem = 0;
+  o.f = 0.0f;
+  o.u = (uint32_t)(key >> 32);
+  o.v = (uint32_t)key;
+  const uint4 ru = __ldg(reinterpret_cast<const uint4*>(vd + o.u));
+  const uint4 rv = __ldg(reinterpret_cast<const uint4*>(vd + o.v));
+  bool keep;
+  if (WEIGHTED) {
+    double w = __longlong_as_double((long long)raw);
+    if (o.u == o.v) w = __dmul_rn(w, 2.0);
+    const double adj = __ddiv_rn(__ddiv_rn(__dmul_rn(w, factor), (double)ru.y), (double)rv.y);
+    const double L = trunc_log_value(adj);
+    keep = L > 0.0;
+    if (keep) o.f = __double2float_rn(L);
+  } else {
+    const XDouble adj = trunc_log_adj(raw, o.u == o.v, xf, ru.y, ((uint64_t)ru.w << 32) | ru.z, rv.y,
+                                      ((uint64_t)rv.w << 32) | rv.z);
+    keep = adj.e > -52 || (adj.e == -52 && adj.m > (1ull << 52));  // adj > 1  <=>  log(adj) > 0
+    if (keep && !float_of_log_fast(log_df(adj, tab), &o.f))
+      o.f = __double2float_rn(trunc_log_value(xd_to_double(adj)));
+  }
+  if (keep) o.nitem = (upper || o.u == o.v) ? 1u : 2u;
+  return o;
+}
+
 template <bool WEIGHTED>
 __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, uint64_t cap,
                                                   const Vertex* __restrict__ vd, double factor, int upper,
@@ -375,6 +416,7 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
                                                   uint64_t max_items, unsigned long long* __restrict__ okeys,
                                                   uint32_t* __restrict__ ovals, int* __restrict__ flags) {
   __shared__ LogTable tab;
+  __shared__ unsigned long long qkey[8][64], qraw[8][64];  // per-warp queue of occupied slots
   for (int i = threadIdx.x; i < 128; i += blockDim.x) {
     tab.log_hi[i] = ltab->log_hi[i];
     tab.log_lo[i] = ltab->log_lo[i];
@@ -383,70 +425,80 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
   }
   __syncthreads();
   const XDouble xf = xd_from_double(factor);
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned long long* qk = qkey[wid];
+  unsigned long long* qr = qraw[wid];
   unsigned long long kept = 0;
-  // warp-uniform loop: the lanes of a warp take 32 consecutive slots
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < cap; b += stride) {
-    const uint64_t i = b + lane;
-    unsigned nitem = 0;
-    uint32_t u = 0, v = 0;
-    float f = 0.0f;
-    const unsigned long long key = i < cap ? T[i].key : kEmptyKey;
-    if (key != kEmptyKey) {
-      u = (uint32_t)(key >> 32);
-      v = (uint32_t)key;
-      const uint4 ru = __ldg(reinterpret_cast<const uint4*>(vd + u));
-      const uint4 rv = __ldg(reinterpret_cast<const uint4*>(vd + v));
-      const unsigned long long raw = T[i].val;
-      bool keep;
-      if (WEIGHTED) {
-        double w = __longlong_as_double((long long)raw);
-        if (u == v) w = __dmul_rn(w, 2.0);
-        const double adj = __ddiv_rn(__ddiv_rn(__dmul_rn(w, factor), (double)ru.y), (double)rv.y);
-        const double L = trunc_log_value(adj);
-        keep = L > 0.0;
-        if (keep) f = __double2float_rn(L);
-      } else {
-        const XDouble adj = trunc_log_adj(raw, u == v, xf, ru.y, ((uint64_t)ru.w << 32) | ru.z, rv.y,
-                                          ((uint64_t)rv.w << 32) | rv.z);
-        keep = adj.e > -52 || (adj.e == -52 && adj.m > (1ull << 52));  // adj > 1  <=>  log(adj) > 0
-        if (keep && !float_of_log_fast(log_df(adj, tab), &f))
-          f = __double2float_rn(trunc_log_value(xd_to_double(adj)));
-      }
-      if (keep) {
-        nitem = (upper || u == v) ? 1u : 2u;
-        atomicAdd(&rowcnt[u], 1ULL);
-        if (nitem == 2) atomicAdd(&rowcnt[v], 1ULL);
-        ++kept;
-      }
-    }
+  int qn = 0;  // queued entries (warp-uniform), < 32 between flushes
+
+  // Evaluates the first min(qn, 32) queued entries (one per lane) and
+  // appends their CSR entries.
+  auto flush = [&](int take) {
+    TruncLogOut<WEIGHTED> o;
+    o.nitem = 0;
+    if (lane < take) o = trunclog_entry<WEIGHTED>(qk[lane], qr[lane], vd, factor, xf, upper, tab);
     __syncwarp();
-    unsigned incl = nitem;
+    if (o.nitem) {
+      atomicAdd(&rowcnt[o.u], 1ULL);
+      if (o.nitem == 2) atomicAdd(&rowcnt[o.v], 1ULL);
+      ++kept;
+    }
+    unsigned incl = o.nitem;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t = __shfl_up_sync(kFullMask, incl, o);
-      if (lane >= o) incl += t;
+    for (int s = 1; s < 32; s <<= 1) {
+      const unsigned t = __shfl_up_sync(kFullMask, incl, s);
+      if (lane >= s) incl += t;
     }
     const unsigned wtot = __shfl_sync(kFullMask, incl, 31);
     unsigned long long base = 0;
     if (lane == 31 && wtot) base = atomicAdd(n_items, (unsigned long long)wtot);
     base = __shfl_sync(kFullMask, base, 31);
-    if (nitem) {
-      const uint64_t pos = base + incl - nitem;
-      if (pos + nitem <= max_items) {
-        const uint32_t fb = __float_as_uint(f);
-        okeys[pos] = ((unsigned long long)u << cbits) | v;
+    if (o.nitem) {
+      const uint64_t pos = base + incl - o.nitem;
+      if (pos + o.nitem <= max_items) {
+        const uint32_t fb = __float_as_uint(o.f);
+        okeys[pos] = ((unsigned long long)o.u << cbits) | o.v;
         ovals[pos] = fb;
-        if (nitem == 2) {
-          okeys[pos + 1] = ((unsigned long long)v << cbits) | u;
+        if (o.nitem == 2) {
+          okeys[pos + 1] = ((unsigned long long)o.v << cbits) | o.u;
           ovals[pos + 1] = fb;
         }
       } else {
         atomicOr(&flags[kFlagSortOverflow], 1);
       }
     }
+  };
+
+  // warp-uniform loop: the lanes of a warp read 32 consecutive slots
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < cap; b += stride) {
+    const uint64_t i = b + lane;
+    const unsigned long long key = i < cap ? T[i].key : kEmptyKey;
+    const bool occ = key != kEmptyKey;
+    const unsigned occm = __ballot_sync(kFullMask, occ);
+    if (occ) {
+      const int at = qn + __popc(occm & lt);
+      qk[at] = key;
+      qr[at] = T[i].val;
+    }
+    qn += __popc(occm);
+    __syncwarp();
+    if (qn >= 32) {
+      flush(32);
+      // move the entries past the first 32 to the front of the queue
+      const unsigned long long k2 = lane < qn - 32 ? qk[32 + lane] : 0ULL;
+      const unsigned long long r2 = lane < qn - 32 ? qr[32 + lane] : 0ULL;
+      __syncwarp();
+      if (lane < qn - 32) {
+        qk[lane] = k2;
+        qr[lane] = r2;
+      }
+      qn -= 32;
+      __syncwarp();
+    }
   }
+  if (qn > 0) flush(qn);
   for (int o = 16; o > 0; o >>= 1) kept += __shfl_down_sync(kFullMask, kept, o);
   if (lane == 0 && kept) atomicAdd(kept_total, kept);
 }

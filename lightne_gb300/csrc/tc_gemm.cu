@@ -201,74 +201,459 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm_tall(const float* __rest
   tc_teardown(sh, tmem);
 }
 
-// partial[rb] (c1 x c2) = A[rows]^T B[rows] for the 2048-row block rb and the
-// 128-row tile blockIdx.x of the output.
-__global__ void __launch_bounds__(kTcThreads) k_tc_gram(const float* __restrict__ A, int64_t lda, int c1,
-                                                        const float* __restrict__ B, int64_t ldb, int c2, int nmma,
-                                                        int64_t n, float* __restrict__ partial, int* flags) {
-  extern __shared__ __align__(128) uint8_t smem[];
-  TcShared* sh = reinterpret_cast<TcShared*>(smem + kStages * kStageBytes);
-  tc_setup(sh);
-  const uint32_t tmem = sh->tmem_base;
-  const int mt = blockIdx.x;
-  const int64_t rb = blockIdx.y;
-  const int64_t r0 = rb * 2048;
-  const int64_t r1 = std::min<int64_t>(n, r0 + 2048);
-  const int t = threadIdx.x;
-  const int nchunks = (int)((r1 - r0 + kKc - 1) / kKc);
-  const uint32_t idesc = tc::idesc_tf32(128, nmma);
-  const int ca = mt * 128 + t;
-  const bool ok = tc_kloop(smem, sh, tmem, idesc, nchunks, flags + kFlagNumeric, [&](int c, const StageBufs& b) {
-    const int64_t k0 = r0 + (int64_t)c * kKc;
-    {
-      float v[kKc];
+
+// ---------------------------------------------------------------------------
+// Streaming forms (persistent CTAs, one per SM).  The operand rows are copied
+// with 16-byte cp.async straight into the K-major core-matrix positions of a
+// ring of raw slices (so up to kRing - 1 slices are in flight while the tensor
+// core works), split into TF32 high and low parts by an elementwise pass into
+// one of two operand buffers, and consumed by the same three-MMA scheme.
+// Raw slots are free once converted, so refills never wait for the tensor
+// core; operand buffers are reused after the commit of the MMAs that read
+// them.
+// ---------------------------------------------------------------------------
+constexpr int kSThreads = 256;
+constexpr int kSlice = 16;                                 // K per slice
+constexpr uint32_t kSliceRowBytes = kSlice * 4;            // one operand row of a slice
+constexpr uint32_t kASlice = 128 * kSliceRowBytes;         // 8 KB: 128 rows x 16 K
+constexpr int kGemmRing = 4;
+constexpr int kGramRing = 6;
+
+struct StreamShared {
+  unsigned long long mbar[2];
+  uint32_t tmem_base;
+};
+
+__device__ __forceinline__ void split4(const float4& x, float4& h, float4& l) {
+  h.x = tc::to_tf32(x.x);
+  h.y = tc::to_tf32(x.y);
+  h.z = tc::to_tf32(x.z);
+  h.w = tc::to_tf32(x.w);
+  l.x = x.x - h.x;
+  l.y = x.y - h.y;
+  l.z = x.z - h.z;
+  l.w = x.w - h.w;
+}
+
+// 2 K = 8 steps x (hi*hi + hi*lo + lo*hi) on one slice.
+__device__ __forceinline__ void issue_slice(uint32_t tmem_d, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
+                                            uint32_t b_lo, uint32_t idesc, bool first) {
+  const uint32_t lbo = 128, sbo = (kSlice / 4) * 128;
 #pragma unroll
-      for (int k = 0; k < kKc; ++k) v[k] = (k0 + k < r1 && ca < c1) ? A[(k0 + k) * lda + ca] : 0.0f;
-      put_row(b.a_hi, b.a_lo, (uint32_t)t, v);
-    }
-    for (int j = t; j < nmma; j += kTcThreads) {
-      float v[kKc];
-#pragma unroll
-      for (int k = 0; k < kKc; ++k) v[k] = (k0 + k < r1 && j < c2) ? B[(k0 + k) * ldb + j] : 0.0f;
-      put_row(b.b_hi, b.b_lo, (uint32_t)j, v);
-    }
-  });
+  for (int ks = 0; ks < kSlice / 8; ++ks) {
+    const uint32_t koff = (uint32_t)ks * 256;
+    const uint64_t ah = tc::smem_desc(a_hi + koff, lbo, sbo);
+    const uint64_t al = tc::smem_desc(a_lo + koff, lbo, sbo);
+    const uint64_t bh = tc::smem_desc(b_hi + koff, lbo, sbo);
+    const uint64_t bl = tc::smem_desc(b_lo + koff, lbo, sbo);
+    tc::mma_tf32(tmem_d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
+    tc::mma_tf32(tmem_d, ah, bl, idesc, 1u);
+    tc::mma_tf32(tmem_d, al, bh, idesc, 1u);
+  }
+}
+
+__device__ __forceinline__ void stream_setup(StreamShared* sh, uint32_t cols) {
+  if (threadIdx.x == 0) {
+    tc::mbar_init(tc::smem_addr(&sh->mbar[0]), 1);
+    tc::mbar_init(tc::smem_addr(&sh->mbar[1]), 1);
+    tc::fence_mbar_init();
+  }
+  if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(tc::smem_addr(&sh->tmem_base), cols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+}
+
+// After a timed-out wait: record it, wait (bounded, not abortable) for the
+// last commit so that no MMA still writes the TMEM being released, drain the
+// copies in flight, release the TMEM.
+__device__ __forceinline__ void stream_finish(StreamShared* sh, uint32_t tmem, uint32_t cols, bool ok,
+                                              int64_t last_commit, int* flags) {
   if (!ok) {
-    // record the timeout; give the MMAs in flight one more bounded wait
-    // before the TMEM they write is released
-    if (t == 0) atomicExch(flags + kFlagNumeric, 2);
-    const int last = nchunks - 1;
-    if (last >= 0)
-      tc::mbar_wait(tc::smem_addr(&sh->mbar[last % kStages]), (uint32_t)((last / kStages) & 1), kWaitCycles,
+    if (threadIdx.x == 0) atomicExch(flags + kFlagNumeric, 2);
+    if (last_commit >= 0)
+      tc::mbar_wait(tc::smem_addr(&sh->mbar[last_commit & 1]), (uint32_t)((last_commit >> 1) & 1), kWaitCycles,
                     flags + kFlagTimeoutGuard);
-  } else {
-    const int w = t >> 5, lane = t & 31;
-    const int i = mt * 128 + 32 * w + lane;
-    float* out = partial + rb * (int64_t)c1 * c2;
-    for (int cc = 0; cc < nmma; cc += 16) {
-      float v[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(32 * w) << 16) + (uint32_t)cc, v);
-      if (i < c1) {
+  }
+  tc::cp_async_wait<0>();
+  tc::fence_before_sync();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, cols);
+  }
+}
+
+// Out (n x ldo) = In (n x K) * W (K x c2), persistent over 128-row tiles.
+// W (split, K-major per 16-K slice) stays in shared memory.
+__global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __restrict__ In, int64_t ldi, int K,
+                                                                 const float* __restrict__ W, int c2, int nmma,
+                                                                 int64_t n, float* __restrict__ Out, int64_t ldo,
+                                                                 __nv_bfloat16* __restrict__ OutB, int* flags) {
+  extern __shared__ __align__(1024) uint8_t stream_smem[];
+  const int nsl = (K + kSlice - 1) / kSlice;
+  const uint32_t wslice = (uint32_t)nmma * kSliceRowBytes;
+  uint8_t* w_hi = stream_smem;
+  uint8_t* w_lo = stream_smem + (size_t)nsl * wslice;
+  uint8_t* raw = w_lo + (size_t)nsl * wslice;
+  uint8_t* conv = raw + (size_t)kGemmRing * kASlice;  // 2 x (hi, lo)
+  StreamShared* sh = reinterpret_cast<StreamShared*>(conv + 4 * kASlice);
+  const int t = threadIdx.x;
+
+  // W into shared memory: element (j, k) of the B operand is W[k][j]
+  for (int idx = t; idx < nsl * 4 * nmma; idx += kSThreads) {
+    const int j = idx % nmma, sq = idx / nmma, sl = sq >> 2, q = sq & 3;
+    float4 x;
+    float* xv = reinterpret_cast<float*>(&x);
 #pragma unroll
-        for (int q = 0; q < 16; ++q)
-          if (cc + q < c2) out[(int64_t)i * c2 + cc + q] = v[q];
+    for (int e = 0; e < 4; ++e) {
+      const int k = sl * kSlice + 4 * q + e;
+      xv[e] = (j < c2 && k < K) ? W[(int64_t)k * c2 + j] : 0.0f;
+    }
+    float4 h, l;
+    split4(x, h, l);
+    const uint32_t off = (uint32_t)sl * wslice + tc::kmajor_off((uint32_t)j, (uint32_t)(4 * q), kSlice);
+    *reinterpret_cast<float4*>(w_hi + off) = h;
+    *reinterpret_cast<float4*>(w_lo + off) = l;
+  }
+  stream_setup(sh, 256);
+  const uint32_t tmem = sh->tmem_base;
+  const uint32_t idesc = tc::idesc_tf32(128, nmma);
+  const int64_t ntiles = (n + 127) / 128;
+  const int64_t my_tiles = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int64_t total = my_tiles * nsl;
+
+  auto issue_load = [&](int64_t g) {
+    const int64_t tile = blockIdx.x + (g / nsl) * gridDim.x;
+    const int k0 = (int)(g % nsl) * kSlice;
+    const uint32_t dst0 = tc::smem_addr(raw + (size_t)(g % kGemmRing) * kASlice);
+    for (int idx = t; idx < 128 * 4; idx += kSThreads) {
+      const int r = idx >> 2, q = idx & 3;
+      const int64_t row = tile * 128 + r;
+      const int k = k0 + 4 * q;
+      const int kb = K - k;
+      const uint32_t bytes = (row < n && kb > 0) ? (uint32_t)(kb >= 4 ? 16 : 4 * kb) : 0u;
+      const float* src = bytes ? In + row * ldi + k : In;
+      tc::cp_async16(dst0 + tc::kmajor_off((uint32_t)r, (uint32_t)(4 * q), kSlice), src, bytes);
+    }
+  };
+
+  bool ok = true;
+  int64_t last_commit = -1;
+  for (int64_t g = 0; g < kGemmRing - 1; ++g) {
+    if (g < total) issue_load(g);
+    tc::cp_async_commit();
+  }
+  for (int64_t g = 0; g < total && ok; ++g) {
+    if (g + kGemmRing - 1 < total) issue_load(g + kGemmRing - 1);
+    tc::cp_async_commit();
+    tc::cp_async_wait<kGemmRing - 1>();
+    const int cb = (int)(g & 1);
+    if (g >= 2 && !tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)(((g - 2) >> 1) & 1), kWaitCycles,
+                                 flags + kFlagNumeric))
+      ok = false;
+    __syncthreads();  // slice g visible to every thread; operand buffer cb free
+    {
+      const float4* src = reinterpret_cast<const float4*>(raw + (size_t)(g % kGemmRing) * kASlice);
+      float4* hi = reinterpret_cast<float4*>(conv + (size_t)cb * 2 * kASlice);
+      float4* lo = reinterpret_cast<float4*>(conv + (size_t)cb * 2 * kASlice + kASlice);
+      for (int idx = t; idx < (int)(kASlice / 16); idx += kSThreads) {
+        float4 h, l;
+        split4(src[idx], h, l);
+        hi[idx] = h;
+        lo[idx] = l;
+      }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (!ok) break;
+    const int sl = (int)(g % nsl);
+    if (t == 0) {
+      tc::fence_after_sync();
+      const uint32_t a_hi = tc::smem_addr(conv + (size_t)cb * 2 * kASlice);
+      issue_slice(tmem, a_hi, a_hi + kASlice, tc::smem_addr(w_hi + (size_t)sl * wslice),
+                  tc::smem_addr(w_lo + (size_t)sl * wslice), idesc, sl == 0);
+      tc::commit(tc::smem_addr(&sh->mbar[cb]));
+    }
+    last_commit = g;
+    if (sl == nsl - 1) {
+      // tile done: wait for its MMAs, then write it out
+      if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)((g >> 1) & 1), kWaitCycles, flags + kFlagNumeric))
+        ok = false;
+      ok = __syncthreads_and(ok ? 1 : 0) != 0;
+      if (!ok) break;
+      tc::fence_after_sync();
+      const int64_t tile = blockIdx.x + (g / nsl) * gridDim.x;
+      const int w = t >> 5, lane = t & 31, lg = w & 3;
+      const int64_t row = tile * 128 + 32 * lg + lane;
+      const bool vec = ((ldo & 3) == 0) && ((reinterpret_cast<uintptr_t>(Out) & 15) == 0);
+      for (int cg = w >> 2; cg * 16 < nmma; cg += 2) {
+        float v[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(32 * lg) << 16) + (uint32_t)(cg * 16), v);
+        if (row < n) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (cg * 16 + i >= c2) v[i] = 0.0f;
+          float* orow = Out + row * ldo + cg * 16;
+          if (vec && cg * 16 + 16 <= ldo) {
+#pragma unroll
+            for (int i = 0; i < 16; i += 4) *reinterpret_cast<float4*>(orow + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+          } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (cg * 16 + i < ldo) orow[i] = v[i];
+          }
+          if (OutB) {
+            __nv_bfloat16* brow = OutB + row * ldo + cg * 16;
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (cg * 16 + i < ldo) brow[i] = __float2bfloat16_rn(v[i]);
+          }
+        }
+      }
+      tc::fence_before_sync();  // the next tile's first MMA follows a __syncthreads
+    }
+  }
+  stream_finish(sh, tmem, 256, ok, last_commit, flags);
+}
+
+// Partial Gram of one contiguous range of 16-row slices per CTA:
+// partial[b] (c1 x c2) = A[rows]^T B[rows].  Both 128-column tiles of A are
+// accumulated by the CTA (D0 for columns 0..127 of A, D1 for 128..255; D1
+// sits right after D0 in the TMEM column space).  When A and B are the same
+// matrix (sym), D1 only computes columns >= 128 and the reduction mirrors
+// the lower triangle.
+//
+// The tensor core accumulates in FP32 without rounding to nearest (the
+// low bits of each addition are dropped), so a long accumulation chain
+// drifts towards zero by about 2^-25 of the sum per MMA.  Every kGroup
+// slices (64 rows) the TMEM sums are therefore added into FP32 registers
+// (rounded to nearest) and the next group starts a fresh TMEM sum.  With
+// room for two TMEM sets the group just finished is read while the next
+// one accumulates in the other set; otherwise the drain waits for the
+// group's MMAs.
+constexpr int kGroup = 4;
+constexpr int kMaxChunks = 9;  // 16-column chunks per thread: sets up to 288 columns
+
+__global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __restrict__ A, int64_t lda, int c1,
+                                                                 const float* __restrict__ B, int64_t ldb, int c2,
+                                                                 int nmma, int64_t n, int sym, int64_t per,
+                                                                 float* __restrict__ partial, int* flags) {
+  extern __shared__ __align__(1024) uint8_t stream_smem[];
+  const int mt = c1 > 128 ? 2 : 1;
+  const uint32_t a_part = (uint32_t)(128 * mt) * kSliceRowBytes;   // one part (hi or lo) of the A operand
+  const uint32_t b_part = sym ? 0u : (uint32_t)nmma * kSliceRowBytes;
+  const uint32_t stage = 2 * a_part + 2 * b_part;
+  const int c1p = (c1 + 3) & ~3, c2p = sym ? 0 : (c2 + 3) & ~3;
+  const uint32_t raw_slot = (uint32_t)(kSlice * (c1p + c2p) * 4);
+  uint8_t* conv = stream_smem;
+  uint8_t* raw = stream_smem + 2 * (size_t)stage;
+  StreamShared* sh = reinterpret_cast<StreamShared*>(raw + (size_t)kGramRing * raw_slot);
+  const int t = threadIdx.x;
+  stream_setup(sh, 512);
+  const uint32_t tmem = sh->tmem_base;
+  const int n1 = sym ? nmma - 128 : nmma;  // N of D1
+  const int set_cols = mt == 2 ? nmma + n1 : nmma;
+  const bool dbuf = 2 * set_cols <= 512;
+  const uint32_t idesc0 = tc::idesc_tf32(128, nmma);
+  const uint32_t idesc1 = tc::idesc_tf32(128, n1 > 0 ? n1 : 16);
+  const int64_t nslices = (n + kSlice - 1) / kSlice;
+  const int64_t s0 = (int64_t)blockIdx.x * per;
+  const int64_t left = nslices - s0;
+  const int64_t total = left <= 0 ? 0 : (left < per ? left : per);
+  const int qa = c1p >> 2, qb = c2p >> 2;
+  const int w = t >> 5, lane = t & 31, lg = w & 3, half = w >> 2;
+  const int nchunks = set_cols / 16;
+  const uint32_t lane_addr = (uint32_t)(32 * lg) << 16;
+
+  float acc[kMaxChunks][16];
+#pragma unroll
+  for (int i = 0; i < kMaxChunks; ++i)
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[i][e] = 0.0f;
+  // adds the TMEM set at column `base` into acc (warp-collective loads)
+  auto drain = [&](uint32_t base) {
+#pragma unroll
+    for (int i = 0; i < kMaxChunks; ++i) {
+      const int ch = half + 2 * i;
+      if (ch < nchunks) {
+        float v[16];
+        tc::tmem_ld16(tmem + lane_addr + base + (uint32_t)(ch * 16), v);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) acc[i][e] += v[e];
+      }
+    }
+  };
+  auto set_base = [&](int64_t g) -> uint32_t { return dbuf ? (uint32_t)(((g / kGroup) & 1) * 256) : 0u; };
+
+  auto issue_load = [&](int64_t g) {
+    const int64_t r0 = (s0 + g) * kSlice;
+    const uint32_t dst0 = tc::smem_addr(raw + (size_t)(g % kGramRing) * raw_slot);
+    for (int idx = t; idx < kSlice * (qa + qb); idx += kSThreads) {
+      const bool isb = idx >= kSlice * qa;
+      const int li = isb ? idx - kSlice * qa : idx;
+      const int qn = isb ? qb : qa;
+      const int k = li / qn, q = li % qn;
+      const int64_t row = r0 + k;
+      const int cb = (isb ? c2 : c1) - 4 * q;
+      const uint32_t bytes = (row < n) ? (uint32_t)(cb >= 4 ? 16 : 4 * cb) : 0u;
+      const float* src = isb ? B + row * ldb + 4 * q : A + row * lda + 4 * q;
+      const uint32_t doff = isb ? (uint32_t)((kSlice * c1p + k * c2p + 4 * q) * 4) : (uint32_t)((k * c1p + 4 * q) * 4);
+      tc::cp_async16(dst0 + doff, bytes ? src : (isb ? B : A), bytes);
+    }
+  };
+
+  bool ok = true;
+  int64_t last_commit = -1;
+  for (int64_t g = 0; g < kGramRing - 1; ++g) {
+    if (g < total) issue_load(g);
+    tc::cp_async_commit();
+  }
+  for (int64_t g = 0; g < total && ok; ++g) {
+    if (g + kGramRing - 1 < total) issue_load(g + kGramRing - 1);
+    tc::cp_async_commit();
+    tc::cp_async_wait<kGramRing - 1>();
+    const int cb = (int)(g & 1);
+    if (g >= 2 && !tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)(((g - 2) >> 1) & 1), kWaitCycles,
+                                 flags + kFlagNumeric))
+      ok = false;
+    // the MMAs of slice g - 2 are done, hence (dbuf) every MMA of the group
+    // that ended with slice g - 2: add that set into the registers
+    if (dbuf && g % kGroup == 1 && g > kGroup) {
+      ok = __syncthreads_and(ok ? 1 : 0) != 0;
+      if (!ok) break;
+      tc::fence_after_sync();
+      drain(set_base(g - 2));
+      tc::fence_before_sync();
+    }
+    __syncthreads();
+    {
+      const float* rs = reinterpret_cast<const float*>(raw + (size_t)(g % kGramRing) * raw_slot);
+      uint8_t* st = conv + (size_t)cb * stage;
+      // operand row j, K group q <- raw rows 4q..4q+3, column j
+      for (int idx = t; idx < 4 * (c1 + (sym ? 0 : c2)); idx += kSThreads) {
+        const bool isb = idx >= 4 * c1;
+        const int li = isb ? idx - 4 * c1 : idx;
+        const int cn = isb ? c2 : c1;
+        const int q = li / cn, j = li % cn;
+        const float* col = isb ? rs + kSlice * c1p + j : rs + j;
+        const int ld = isb ? c2p : c1p;
+        float4 x = make_float4(col[(4 * q) * ld], col[(4 * q + 1) * ld], col[(4 * q + 2) * ld], col[(4 * q + 3) * ld]);
+        float4 h, l;
+        split4(x, h, l);
+        uint8_t* hi = isb ? st + 2 * a_part : st;
+        const uint32_t part = isb ? b_part : a_part;
+        const uint32_t off = tc::kmajor_off((uint32_t)j, (uint32_t)(4 * q), kSlice);
+        *reinterpret_cast<float4*>(hi + off) = h;
+        *reinterpret_cast<float4*>(hi + part + off) = l;
+      }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (!ok) break;
+    const uint32_t sb = set_base(g);
+    if (t == 0) {
+      tc::fence_after_sync();
+      const uint32_t a_hi = tc::smem_addr(conv + (size_t)cb * stage);
+      const uint32_t a_lo = a_hi + a_part;
+      const uint32_t b_hi = sym ? a_hi : a_hi + 2 * a_part;
+      const uint32_t b_lo = sym ? a_lo : b_hi + b_part;
+      const bool first = g % kGroup == 0;
+      issue_slice(tmem + sb, a_hi, a_lo, b_hi, b_lo, idesc0, first);
+      if (mt == 2 && n1 > 0) {
+        const uint32_t m1 = 128 * kSliceRowBytes;  // row 128 of the A operand
+        const uint32_t b1 = sym ? m1 : 0u;
+        issue_slice(tmem + sb + (uint32_t)nmma, a_hi + m1, a_lo + m1, b_hi + b1, b_lo + b1, idesc1, first);
+      }
+      tc::commit(tc::smem_addr(&sh->mbar[cb]));
+    }
+    last_commit = g;
+    if (!dbuf && (g % kGroup == kGroup - 1 || g == total - 1)) {
+      // one TMEM set: wait for this group's MMAs, then drain it
+      if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)((g >> 1) & 1), kWaitCycles, flags + kFlagNumeric))
+        ok = false;
+      ok = __syncthreads_and(ok ? 1 : 0) != 0;
+      if (!ok) break;
+      tc::fence_after_sync();
+      drain(0);
+      tc::fence_before_sync();
+    }
+  }
+  if (ok && total > 0 && dbuf) {
+    const int64_t g = total - 1;
+    if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[g & 1]), (uint32_t)((g >> 1) & 1), kWaitCycles, flags + kFlagNumeric))
+      ok = false;
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (ok) {
+      tc::fence_after_sync();
+      // groups whose drain point (first slice + kGroup + 1) was not reached
+      const int64_t last_group = g / kGroup;
+      if (last_group >= 1 && (last_group * kGroup + 1) >= total) drain(set_base((last_group - 1) * kGroup));
+      drain(set_base(g));
+    }
+  }
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  if (ok) {
+    float* out = partial + (int64_t)blockIdx.x * c1 * c2;
+#pragma unroll
+    for (int i = 0; i < kMaxChunks; ++i) {
+      const int ch = half + 2 * i;
+      if (ch < nchunks) {
+        const bool d1 = ch * 16 >= nmma;
+        const int row = (d1 ? 128 : 0) + 32 * lg + lane;
+        const int j0 = d1 ? (sym ? 128 : 0) + ch * 16 - nmma : ch * 16;
+        if (row < c1) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e)
+            if (j0 + e < c2) out[(int64_t)row * c2 + j0 + e] = acc[i][e];
+        }
       }
     }
   }
-  tc_teardown(sh, tmem);
+  stream_finish(sh, tmem, 512, ok, last_commit, flags);
 }
 
-__global__ void k_gram_reduce_tc(const float* __restrict__ partial, int64_t nb, int64_t cnt, double* __restrict__ G) {
+// G[i][j] = sum over CTAs of partial[b][i][j] in FP64, in CTA order; with
+// sym, the lower triangle is the mirror of the upper one (so G is exactly
+// symmetric; entries i >= 128, j < 128 are not computed by the CTAs).
+__global__ void k_gram_reduce_stream(const float* __restrict__ partial, int64_t nb, int c1, int c2, int sym,
+                                     double* __restrict__ G) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t cnt = (int64_t)c1 * c2;
   if (t >= cnt) return;
+  int i = (int)(t / c2), j = (int)(t % c2);
+  if (sym && i > j) {
+    const int x = i;
+    i = j;
+    j = x;
+  }
+  const int64_t e = (int64_t)i * c2 + j;
   double s = 0.0;
-  for (int64_t b = 0; b < nb; ++b) s += (double)partial[b * cnt + t];
+  for (int64_t b = 0; b < nb; ++b) s += (double)partial[b * cnt + e];
   G[t] = s;
 }
 
 }  // namespace
 
 bool tc_supported(int c2) { return c2 >= 1 && c2 <= 256; }
+
+// Shared memory of the streaming kernels (0 when the shape does not fit).
+static size_t gemm_stream_smem(int K, int nmma) {
+  const size_t nsl = (size_t)(K + kSlice - 1) / kSlice;
+  return 2 * nsl * nmma * kSliceRowBytes + (size_t)kGemmRing * kASlice + 4 * kASlice + sizeof(StreamShared);
+}
+static size_t gram_stream_smem(int c1, int c2, int nmma, bool sym) {
+  const int mt = c1 > 128 ? 2 : 1;
+  const size_t a_part = (size_t)(128 * mt) * kSliceRowBytes;
+  const size_t b_part = sym ? 0 : (size_t)nmma * kSliceRowBytes;
+  const size_t c1p = (c1 + 3) & ~3, c2p = sym ? 0 : (c2 + 3) & ~3;
+  return 2 * (2 * a_part + 2 * b_part) + (size_t)kGramRing * kSlice * (c1p + c2p) * 4 + sizeof(StreamShared);
+}
+static bool aligned16(const void* p, int64_t ld) {
+  return (reinterpret_cast<uintptr_t>(p) & 15) == 0 && (ld & 3) == 0;
+}
 
 int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
                  int64_t ldo, __nv_bfloat16* OutB) {
@@ -278,6 +663,18 @@ int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float*
     set_error("tc_gemm_tall: more than 256 output columns");
     return LNE_ERR_UNSUPPORTED;
   }
+  const size_t ssmem = gemm_stream_smem(k, nmma);
+  if (aligned16(In, ldi) && ssmem <= ctx->smem_optin && k >= 1) {
+    const int64_t ntiles = (n + 127) / 128;
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, ctx->num_sms);
+    // at most two CTAs per SM: each holds 256 TMEM columns
+    const size_t lsmem = std::max(ssmem, std::min(ctx->smem_optin, (size_t)80 * 1024));
+    cudaFuncSetAttribute(k_tc_gemm_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
+    k_tc_gemm_stream<<<grid, kSThreads, lsmem, ctx->stream>>>(In, ldi, k, W, c2, nmma, n, Out, ldo, OutB,
+                                                              ctx->d_flags);
+    LNE_CUDA_TRY(cudaGetLastError());
+    return LNE_OK;
+  }
   cudaFuncSetAttribute(k_tc_gemm_tall, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
   k_tc_gemm_tall<<<(unsigned)((n + 127) / 128), kTcThreads, kSmemBytes, ctx->stream>>>(In, ldi, k, W, c2, nmma, n, Out,
                                                                                        ldo, OutB, ctx->d_flags);
@@ -285,43 +682,47 @@ int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float*
   return LNE_OK;
 }
 
-int tc_gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
-            double* G) {
+bool tc_gram_stream_supported(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb,
+                               int c2) {
+  if (c1 < 1 || c2 < 1 || c1 > 256 || c2 > 256) return false;
   const int nmma = std::max(16, (c2 + 15) / 16 * 16);
-  if (nmma > 256) {
-    set_error("tc_gram: more than 256 columns");
-    return LNE_ERR_UNSUPPORTED;
-  }
-  const int64_t nb = std::max<int64_t>(1, (n + 2047) / 2048);
-  float* partial = nullptr;
-  int rc = dalloc(ctx, (void**)&partial, sizeof(float) * nb * c1 * c2, "gram partials");
-  if (rc) return rc;
-  cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  dim3 grid((unsigned)((c1 + 127) / 128), (unsigned)nb);
-  k_tc_gram<<<grid, kTcThreads, kSmemBytes, ctx->stream>>>(A, lda, c1, B, ldb, c2, nmma, n, partial, ctx->d_flags);
-  const int64_t cnt = (int64_t)c1 * c2;
-  k_gram_reduce_tc<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, cnt, G);
-  dfree(ctx, partial);
-  LNE_CUDA_TRY(cudaGetLastError());
-  return LNE_OK;
+  const bool sym = A == B && lda == ldb && c1 == c2;
+  const int set_cols = c1 > 128 ? nmma + (sym ? nmma - 128 : nmma) : nmma;
+  return aligned16(A, lda) && aligned16(B, ldb) && set_cols <= 32 * kMaxChunks &&
+         gram_stream_smem(c1, c2, nmma, sym) <= ctx->smem_optin;
 }
 
-// Gram with caller-provided partial-sum storage (nb * c1 * c2 floats,
-// nb = ceil(n / 2048)); the tensor-core path only (c2 <= 256).  Every
-// partial is overwritten, so the storage needs no clearing.
-int tc_gram_into(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
-                 double* G, float* partial) {
-  const int nmma = std::max(16, (c2 + 15) / 16 * 16);
-  if (nmma > 256) {
-    set_error("tc_gram_into: more than 256 columns");
+int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
+                   double* G, float* partial, int64_t max_blocks) {
+  if (!tc_gram_stream_supported(ctx, A, lda, c1, B, ldb, c2)) {
+    set_error("tc_gram_stream: shape or alignment not supported");
     return LNE_ERR_UNSUPPORTED;
   }
-  const int64_t nb = std::max<int64_t>(1, (n + 2047) / 2048);
-  cudaFuncSetAttribute(k_tc_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  dim3 grid((unsigned)((c1 + 127) / 128), (unsigned)nb);
-  k_tc_gram<<<grid, kTcThreads, kSmemBytes, ctx->stream>>>(A, lda, c1, B, ldb, c2, nmma, n, partial, ctx->d_flags);
+  if (n <= 0) {
+    LNE_CUDA_TRY(cudaMemsetAsync(G, 0, sizeof(double) * c1 * c2, ctx->stream));
+    return LNE_OK;
+  }
+  const int nmma = std::max(16, (c2 + 15) / 16 * 16);
+  const bool sym = A == B && lda == ldb && c1 == c2;
+  const size_t ssmem = gram_stream_smem(c1, c2, nmma, sym);
+  const int64_t nslices = (n + kSlice - 1) / kSlice;
+  const int64_t want = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(nslices, ctx->num_sms), max_blocks));
+  const int64_t per = (nslices + want - 1) / want;
+  const int64_t nb = (nslices + per - 1) / per;  // <= want
+  float* own = nullptr;
+  if (!partial) {
+    int rc = dalloc(ctx, (void**)&own, sizeof(float) * nb * c1 * c2, "gram partials");
+    if (rc) return rc;
+    partial = own;
+  }
+  // the CTA allocates all 512 TMEM columns: one CTA per SM
+  const size_t lsmem = std::max(ssmem, std::min(ctx->smem_optin, (size_t)120 * 1024));
+  cudaFuncSetAttribute(k_tc_gram_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
+  k_tc_gram_stream<<<(unsigned)nb, kSThreads, lsmem, ctx->stream>>>(A, lda, c1, B, ldb, c2, nmma, n, sym ? 1 : 0, per,
+                                                                    partial, ctx->d_flags);
   const int64_t cnt = (int64_t)c1 * c2;
-  k_gram_reduce_tc<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, cnt, G);
+  k_gram_reduce_stream<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, c1, c2, sym ? 1 : 0, G);
+  if (own) dfree(ctx, own);
   LNE_CUDA_TRY(cudaGetLastError());
   return LNE_OK;
 }

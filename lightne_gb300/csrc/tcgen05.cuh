@@ -121,6 +121,20 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long l
   }
 }
 
+// Asynchronous 16-byte global -> shared copy (cp.async, L2 only); bytes of
+// the source past `src_bytes` (0..16) are not read and land as zeros.  Both
+// addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(uint32_t dst_saddr, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst_saddr), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits until at most N of this thread's committed copy groups are pending.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // FP32 -> TF32 (round to nearest, ties away), as a float bit pattern.
 __device__ __forceinline__ float to_tf32(float x) {
   uint32_t r;
