@@ -265,14 +265,85 @@ __global__ void k_tri_inv_t(const double* __restrict__ L, int r, float* __restri
   }
 }
 
+// The same factorisation and inverse with the matrix in shared memory (one
+// CTA, r <= 160): L in the lower triangle, X = L^-1 stored transposed in the
+// upper triangle (X[i][j] at [j][i]) and its diagonal apart, so W = X^T is
+// the upper triangle.  Same operations in the same order as the two kernels
+// above; the matrix is read from global memory once and W written once.
+constexpr int kCholSmemMax = 160;
+
+__global__ void __launch_bounds__(1024) k_chol_inv_smem(const double* __restrict__ G, int r, double shift,
+                                                        float* __restrict__ W, int* __restrict__ status) {
+  extern __shared__ double A[];  // r * r, then the diagonal of X (r)
+  double* xd = A + (int64_t)r * r;
+  __shared__ double dk;
+  __shared__ int bad;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  for (int t = tid; t < r * r; t += blockDim.x) A[t] = G[t];
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int i = tid; i < r; i += blockDim.x) A[i * r + i] += shift;
+  __syncthreads();
+  for (int k = 0; k < r; ++k) {
+    if (tid == 0) {
+      const double d = A[k * r + k];
+      if (!(d > 0.0) || !isfinite(d)) {
+        bad = 1;
+        dk = 1.0;
+      } else {
+        dk = sqrt(d);
+      }
+      A[k * r + k] = dk;
+    }
+    __syncthreads();
+    if (bad) break;
+    const double piv = dk;
+    for (int i = k + 1 + tid; i < r; i += blockDim.x) A[i * r + k] /= piv;
+    __syncthreads();
+    for (int i = k + 1 + ty; i < r; i += 32) {
+      const double lik = A[i * r + k];
+      for (int j = k + 1 + tx; j <= i; j += 32) A[i * r + j] -= lik * A[j * r + k];
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (tid == 0) *status = 1;
+    return;
+  }
+  // rows of X = L^-1 in order; thread j < i computes X[i][j]
+  for (int i = 0; i < r; ++i) {
+    for (int j = tid; j <= i; j += blockDim.x) {
+      if (j == i) {
+        xd[i] = 1.0 / A[i * r + i];
+      } else {
+        double sacc = A[i * r + j] * xd[j];  // k = j
+        for (int k = j + 1; k < i; ++k) sacc += A[i * r + k] * A[j * r + k];
+        A[j * r + i] = -sacc / A[i * r + i];
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < r * r; t += blockDim.x) {
+    const int j = t / r, i = t - (t / r) * r;  // W[j][i] = X[i][j]
+    W[t] = i < j ? 0.0f : (i == j ? (float)xd[i] : (float)A[j * r + i]);
+  }
+  if (tid == 0) *status = 0;
+}
+
 int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W) {
   double* X = nullptr;
   int* status = nullptr;
   int rc;
   if ((rc = dalloc(ctx, (void**)&X, sizeof(double) * r * r + 16, "triangular inverse"))) return rc;
   status = (int*)(X + (int64_t)r * r);
-  k_cholesky<<<1, 1024, 0, ctx->stream>>>(G, r, shift, status);
-  k_tri_inv_t<<<(r + 127) / 128, 128, 0, ctx->stream>>>(G, r, W, X);
+  const size_t csmem = sizeof(double) * ((size_t)r * r + r);
+  if (r <= kCholSmemMax && csmem <= ctx->smem_optin) {
+    cudaFuncSetAttribute(k_chol_inv_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
+    k_chol_inv_smem<<<1, 1024, csmem, ctx->stream>>>(G, r, shift, W, status);
+  } else {
+    k_cholesky<<<1, 1024, 0, ctx->stream>>>(G, r, shift, status);
+    k_tri_inv_t<<<(r + 127) / 128, 128, 0, ctx->stream>>>(G, r, W, X);
+  }
   int h = 0;
   LNE_CUDA_TRY(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -286,18 +357,24 @@ int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W) {
 }
 
 // ---------------------------------------------------------------------------
-// One-sided Jacobi SVD (Hestenes), FP64.  Columns of the working copy Wc
-// (column-major, in global memory / L2) are rotated pairwise in round-robin
-// order until every pair is orthogonal to 1e-15 relative; singular values
-// are the column norms, left singular vectors the normalised columns.
+// One-sided Jacobi SVD (Hestenes), FP64.  Columns of the working copy are
+// rotated pairwise in round-robin order until every pair is orthogonal to
+// 1e-15 relative; singular values are the column norms, left singular
+// vectors the normalised columns.  Dot products, rotations and the
+// convergence test are FP64; the distributed-shared-memory form computes
+// the rotation angle in FP32 and then makes (c, s) orthogonal in FP64.
 //
 // The sweeps run on one thread-block cluster (16 CTAs where the device
 // allows that size, else 8): each warp of the cluster takes pairs of the
 // current round-robin step, and a cluster barrier (release/acquire at
-// cluster scope) separates the steps.  Columns are read with ld.global.cg
-// so that no CTA sees a stale L1 line of a column another CTA rotated.
-// FP64 runs at 1/68 of the FP32 rate on this part, so one SM would spend
-// about 30 ms on a 138 x 138 core; 16 SMs share the work.
+// cluster scope) separates the steps.  The columns live in the CTAs' shared
+// memory (column c in CTA c % size) and are read and written through
+// distributed shared memory; a lane keeps its elements of both columns in
+// registers between the dot products and the rotation.  When the columns do
+// not fit there, they stay in global memory (L2), read with ld.global.cg so
+// that no CTA sees a stale L1 line of a column another CTA rotated.  FP64
+// runs at 1/68 of the FP32 rate on this part, so one SM would spend about
+// 30 ms on a 138 x 138 core; 16 SMs share the work.
 // ---------------------------------------------------------------------------
 __global__ void k_jacobi_init(const double* __restrict__ C, int r, double* __restrict__ Wc,
                               int* __restrict__ rotated, int max_sweeps) {
@@ -366,6 +443,141 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict
   if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep + 1;
 }
 
+constexpr int kJacobiPer = 5;  // column elements per lane held in registers (r <= 160)
+constexpr int kJacobiMaxSweeps = 60;
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t dsmem_map(uint32_t saddr, uint32_t rank) {
+  uint32_t a;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(saddr), "r"(rank));
+  return a;
+}
+__device__ __forceinline__ double dsmem_ld(uint32_t a) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ int dsmem_ld32(uint32_t a) {
+  int v;
+  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void dsmem_st(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+
+// Same sweeps, same arithmetic, with the columns in distributed shared
+// memory (r <= 32 * kJacobiPer).
+__global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __restrict__ Wc, int* __restrict__ rotated,
+                                                             int max_sweeps, int* __restrict__ sweeps_out) {
+  extern __shared__ double jcols[];  // slot s: column s * csize + rank
+  __shared__ int rot_flag[kJacobiMaxSweeps];  // this CTA rotated some pair in sweep k
+  const int lane = threadIdx.x & 31;
+  for (int k = threadIdx.x; k < kJacobiMaxSweeps; k += blockDim.x) rot_flag[k] = 0;
+  const int csize = gridDim.x;  // the grid is one cluster (8 or 16 CTAs)
+  const uint32_t rank = cluster_rank();
+  const int nslots = (r + csize - 1) / csize;
+  for (int s = 0; s < nslots; ++s) {
+    const int c = s * csize + (int)rank;
+    if (c < r)
+      for (int i = threadIdx.x; i < r; i += blockDim.x) jcols[(int64_t)s * r + i] = Wc[(int64_t)c * r + i];
+  }
+  cluster_barrier();
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(jcols);
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int rp = (r + 1) & ~1;
+  const int m = rp - 1;
+  const int cshift = __ffs(csize) - 1;  // csize is a power of two
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    for (int s = 0; s < m; ++s) {
+      for (int pk = gw; pk < rp / 2; pk += nwarps) {
+        // the round-robin pairs of step s: (s + pk, s - pk) mod m, and (m, s)
+        int p, q;
+        if (pk == 0) {
+          p = m;
+          q = s;
+        } else {
+          p = s + pk;
+          if (p >= m) p -= m;
+          q = s - pk;
+          if (q < 0) q += m;
+        }
+        if (p >= r || q >= r) continue;
+        if (p > q) { const int t = p; p = q; q = t; }
+        const uint32_t ap = dsmem_map(base + (uint32_t)((p >> cshift) * r) * 8u, (uint32_t)(p & (csize - 1)));
+        const uint32_t aq = dsmem_map(base + (uint32_t)((q >> cshift) * r) * 8u, (uint32_t)(q & (csize - 1)));
+        double x[kJacobiPer], y[kJacobiPer];
+#pragma unroll
+        for (int k = 0; k < kJacobiPer; ++k) {
+          const int i = lane + 32 * k;
+          x[k] = i < r ? dsmem_ld(ap + 8u * i) : 0.0;
+          y[k] = i < r ? dsmem_ld(aq + 8u * i) : 0.0;
+        }
+        double a = 0.0, b = 0.0, g = 0.0;
+#pragma unroll
+        for (int k = 0; k < kJacobiPer; ++k) {
+          if (lane + 32 * k < r) {
+            a = fma(x[k], x[k], a);
+            b = fma(y[k], y[k], b);
+            g = fma(x[k], y[k], g);
+          }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          a += __shfl_xor_sync(0xffffffffu, a, o);
+          b += __shfl_xor_sync(0xffffffffu, b, o);
+          g += __shfl_xor_sync(0xffffffffu, g, o);
+        }
+        // |g| > 1e-15 sqrt(ab), without the square root
+        if (g != 0.0 && g * g > 1e-30 * (a * b)) {
+          // Rotation angle in FP32 (the FP64 units are scarce on this part;
+          // an angle accurate to 2^-24 leaves a residual of that size in
+          // g, which the next sweep removes), then (c, s) made orthogonal
+          // to FP64 precision by two Newton steps on c^2 + s^2 = 1.
+          const float zeta = (float)(b - a) / (float)(2.0 * g);
+          const float az = fabsf(zeta);
+          const float t32 = az < 1e18f ? copysignf(1.0f, zeta) / (az + sqrtf(fmaf(az, az, 1.0f))) : 0.5f / zeta;
+          const float c32 = rsqrtf(fmaf(t32, t32, 1.0f));
+          double c = (double)c32, sn = (double)c32 * (double)t32;
+#pragma unroll
+          for (int it = 0; it < 2; ++it) {
+            const double f = fma(-0.5, fma(c, c, sn * sn), 1.5);
+            c *= f;
+            sn *= f;
+          }
+#pragma unroll
+          for (int k = 0; k < kJacobiPer; ++k) {
+            const int i = lane + 32 * k;
+            if (i < r) {
+              dsmem_st(ap + 8u * i, c * x[k] - sn * y[k]);
+              dsmem_st(aq + 8u * i, sn * x[k] + c * y[k]);
+            }
+          }
+          if (lane == 0) rot_flag[sweep] = 1;
+        }
+      }
+      cluster_barrier();
+    }
+    int any = 0;
+    const uint32_t fa = (uint32_t)__cvta_generic_to_shared(&rot_flag[sweep]);
+    for (int c = 0; c < csize; ++c) any |= dsmem_ld32(dsmem_map(fa, (uint32_t)c));
+    if (!any) break;
+  }
+  (void)rotated;
+  cluster_barrier();  // no CTA leaves while another may still read its flags
+  for (int s = 0; s < nslots; ++s) {
+    const int c = s * csize + (int)rank;
+    if (c < r)
+      for (int i = threadIdx.x; i < r; i += blockDim.x) Wc[(int64_t)c * r + i] = jcols[(int64_t)s * r + i];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep + 1;
+}
+
 __global__ void k_jacobi_finish(int r, const double* __restrict__ Wc, double* __restrict__ U,
                                 double* __restrict__ S) {
   __shared__ int order[1024];
@@ -396,7 +608,7 @@ int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps
     set_error("jacobi_svd: rank above 1024 is not supported");
     return LNE_ERR_UNSUPPORTED;
   }
-  const int kMaxSweeps = 60;
+  const int kMaxSweeps = kJacobiMaxSweeps;
   double* Wc = nullptr;
   int rc;
   if ((rc = dalloc(ctx, (void**)&Wc, sizeof(double) * r * r + sizeof(int) * (kMaxSweeps + 4), "jacobi work")))
@@ -414,22 +626,24 @@ int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaError_t e = cudaErrorUnknown;
+  const bool dsmem = r <= 32 * kJacobiPer;
+  auto kern = dsmem ? k_jacobi_sweeps_dsmem : k_jacobi_sweeps;
   for (int cl : {16, 8}) {
-    if (cl == 16 && cudaFuncSetAttribute(k_jacobi_sweeps, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-                        cudaSuccess) {
+    if (cl == 16 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
       cudaGetLastError();
       continue;
     }
     cfg.gridDim = dim3(cl, 1, 1);
+    cfg.dynamicSmemBytes = dsmem ? sizeof(double) * (size_t)((r + cl - 1) / cl) * r : 0;
     attr[0].val.clusterDim.x = cl;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, k_jacobi_sweeps, &cfg) != cudaSuccess || nclusters < 1) {
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) != cudaSuccess || nclusters < 1) {
       cudaGetLastError();
       continue;
     }
-    e = cudaLaunchKernelEx(&cfg, k_jacobi_sweeps, r, Wc, rotated, kMaxSweeps, d_sw);
+    e = cudaLaunchKernelEx(&cfg, kern, r, Wc, rotated, kMaxSweeps, d_sw);
     if (e == cudaSuccess) break;
     cudaGetLastError();
   }

@@ -34,7 +34,13 @@ constexpr int kRadixTile = kRadixThreads * kRadixItems;    // 4096 items
 constexpr int kWarpItems = 32 * kRadixItems;               // 512 items per warp
 constexpr int kMaxBins = 256;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr size_t kScatterSmem = (size_t)kRadixTile * (sizeof(unsigned long long) + sizeof(uint32_t));
+constexpr size_t kTileBytes = (size_t)kRadixTile * (sizeof(unsigned long long) + sizeof(uint32_t));
+constexpr size_t kScatterSmem = 2 * kTileBytes;  // raw tile + reordered tile
+
+// 16-byte cp.async global -> shared; source bytes past `src_bytes` land as zeros.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
 
 // Lanes of the warp whose `dbits`-bit digit equals this lane's, among the
 // lanes with `valid` set: one ballot per digit bit (warp multisplit; the
@@ -52,26 +58,30 @@ __device__ __forceinline__ unsigned match_digit(unsigned d, bool valid, int dbit
   return m;
 }
 
+// Per-warp sub-histograms in shared memory (plain shared atomics: the
+// counting is issue-bound otherwise), summed per tile.
 __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const unsigned long long* __restrict__ keys,
                                                                int64_t count, int shift, int dbits, int64_t ntiles,
                                                                int64_t* __restrict__ hist) {
   const int bins = 1 << dbits;
-  __shared__ unsigned int h[kMaxBins];
-  for (int i = threadIdx.x; i < bins; i += blockDim.x) h[i] = 0;
+  __shared__ unsigned int h[kRadixWarps][kMaxBins];
+  for (int i = threadIdx.x; i < kRadixWarps * kMaxBins; i += blockDim.x) (&h[0][0])[i] = 0;
   __syncthreads();
   const int64_t base = (int64_t)blockIdx.x * kRadixTile;
   const unsigned long long mask = (unsigned long long)(bins - 1);
-  const int lane = threadIdx.x & 31;
-#pragma unroll 4
+  unsigned int* my = h[threadIdx.x >> 5];
+#pragma unroll 8
   for (int r = 0; r < kRadixItems; ++r) {
     const int64_t i = base + (int64_t)r * kRadixThreads + threadIdx.x;
-    const bool valid = i < count;
-    const unsigned d = valid ? (unsigned)((keys[i] >> shift) & mask) : 0u;
-    const unsigned peers = match_digit(d, valid, dbits);
-    if (valid && lane == __ffs(peers) - 1) atomicAdd(&h[d], (unsigned)__popc(peers));
+    if (i < count) atomicAdd(&my[(keys[i] >> shift) & mask], 1u);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < bins; d += blockDim.x) hist[(int64_t)d * ntiles + blockIdx.x] = h[d];
+  for (int d = threadIdx.x; d < bins; d += blockDim.x) {
+    unsigned s = 0;
+#pragma unroll
+    for (int w = 0; w < kRadixWarps; ++w) s += h[w][d];
+    hist[(int64_t)d * ntiles + blockIdx.x] = s;
+  }
 }
 
 // Exclusive scan of v over the block's threads (kRadixThreads); returns the
@@ -92,7 +102,10 @@ __device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned* wa
 }
 
 // FINAL: write column = key & col_mask and the value (as float) to the CSR
-// arrays; otherwise write key and value to the next pass's buffers.
+// arrays; otherwise write key and value to the next pass's buffers.  The
+// tile is first copied to shared memory with cp.async (48 KB in flight per
+// CTA, no registers held), ranked from there, reordered into a second
+// shared buffer and written out.
 template <bool FINAL>
 __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
     const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t count, int shift, int dbits,
@@ -101,9 +114,11 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
   extern __shared__ __align__(16) unsigned char radix_smem[];
   unsigned long long* skey = reinterpret_cast<unsigned long long*>(radix_smem);
   uint32_t* sval = reinterpret_cast<uint32_t*>(radix_smem + sizeof(unsigned long long) * kRadixTile);
-  __shared__ unsigned wcnt[kRadixWarps][kMaxBins];  // per-warp digit counts, then start offsets
-  __shared__ unsigned tile_start[kMaxBins];          // tile-local start of each digit
-  __shared__ int64_t gstart[kMaxBins];               // global start of each digit for this tile
+  unsigned long long* rkey = reinterpret_cast<unsigned long long*>(radix_smem + kTileBytes);
+  uint32_t* rval = reinterpret_cast<uint32_t*>(radix_smem + kTileBytes + sizeof(unsigned long long) * kRadixTile);
+  __shared__ unsigned short wcnt[kRadixWarps][kMaxBins];  // per-warp digit counts, then start offsets
+  __shared__ unsigned short tile_start[kMaxBins];          // tile-local start of each digit
+  __shared__ int64_t gstart[kMaxBins];                     // global start of each digit for this tile
   __shared__ unsigned warp_tot[kRadixWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -112,28 +127,49 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
   const int64_t tbase = (int64_t)blockIdx.x * kRadixTile;
   const int tcount = count - tbase < kRadixTile ? (int)(count - tbase) : kRadixTile;
 
+  // Phase 0: the tile's keys and values into rkey / rval (zeros past the end)
+  {
+    const uint32_t kdst = (uint32_t)__cvta_generic_to_shared(rkey);
+    const uint32_t vdst = (uint32_t)__cvta_generic_to_shared(rval);
+    for (int c = threadIdx.x; c < kRadixTile / 2 + kRadixTile / 4; c += kRadixThreads) {
+      if (c < kRadixTile / 2) {
+        const int left = tcount - 2 * c;
+        const uint32_t bytes = left >= 2 ? 16u : (left == 1 ? 8u : 0u);
+        cp_async16(kdst + 16 * c, bytes ? (const void*)(keys + tbase + 2 * c) : (const void*)keys, bytes);
+      } else {
+        const int cv = c - kRadixTile / 2;
+        const int left = tcount - 4 * cv;
+        const uint32_t bytes = left >= 4 ? 16u : (left > 0 ? 4u * left : 0u);
+        cp_async16(vdst + 16 * cv, bytes ? (const void*)(vals + tbase + 4 * cv) : (const void*)vals, bytes);
+      }
+    }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+  }
   for (int d = threadIdx.x; d < bins; d += blockDim.x) gstart[d] = offs[(int64_t)d * ntiles + blockIdx.x];
-  unsigned* my = wcnt[wid];
+  unsigned short* my = wcnt[wid];
   for (int d = lane; d < bins; d += 32) my[d] = 0;
   __syncwarp();
 
+  __syncthreads();  // raw tile visible to every warp
+
   // Phase 1: warp-local stable ranks (rounds in index order, lanes in order).
-  unsigned long long k[kRadixItems];
-  uint32_t v[kRadixItems];
-  unsigned short rk[kRadixItems];
-  const int64_t wbase = tbase + (int64_t)wid * kWarpItems;
+  uint32_t rk[kRadixItems / 2];  // two 16-bit ranks per word
+  const int wofs = wid * kWarpItems;
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
-    const int64_t i = wbase + r * 32 + lane;
-    const bool valid = i < count;
-    k[r] = valid ? keys[i] : 0ULL;
-    v[r] = valid ? vals[i] : 0u;
-    const unsigned d = (unsigned)((k[r] >> shift) & mask);
+    const int li = wofs + r * 32 + lane;
+    const bool valid = li < tcount;
+    const unsigned long long key = rkey[li];
+    const unsigned d = (unsigned)((key >> shift) & mask);
     const unsigned peers = match_digit(d, valid, dbits);
     const unsigned before = valid ? my[d] : 0u;
     __syncwarp();
-    rk[r] = (unsigned short)(before + __popc(peers & lt));
-    if (valid && lane == __ffs(peers) - 1) my[d] = before + __popc(peers);
+    const uint32_t rank = before + __popc(peers & lt);
+    if (r & 1)
+      rk[r >> 1] |= rank << 16;
+    else
+      rk[r >> 1] = rank;
+    if (valid && lane == __ffs(peers) - 1) my[d] = (unsigned short)(before + __popc(peers));
     __syncwarp();
   }
   __syncthreads();
@@ -146,11 +182,11 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
     for (int w = 0; w < kRadixWarps; ++w) tot += wcnt[w][d0];
   const unsigned start = block_excl_scan_u32(tot, warp_tot);
   if (d0 < bins) {
-    tile_start[d0] = start;
+    tile_start[d0] = (unsigned short)start;
     unsigned s = start;
     for (int w = 0; w < kRadixWarps; ++w) {
       const unsigned c = wcnt[w][d0];
-      wcnt[w][d0] = s;
+      wcnt[w][d0] = (unsigned short)s;
       s += c;
     }
   }
@@ -159,12 +195,13 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
   // Phase 3: reorder the tile by digit in shared memory.
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
-    const int64_t i = wbase + r * 32 + lane;
-    if (i < count) {
-      const int d = (int)((k[r] >> shift) & mask);
-      const unsigned pos = my[d] + rk[r];
-      skey[pos] = k[r];
-      sval[pos] = v[r];
+    const int li = wofs + r * 32 + lane;
+    if (li < tcount) {
+      const unsigned long long key = rkey[li];
+      const int d = (int)((key >> shift) & mask);
+      const unsigned pos = my[d] + ((rk[r >> 1] >> ((r & 1) * 16)) & 0xffffu);
+      skey[pos] = key;
+      sval[pos] = rval[li];
     }
   }
   __syncthreads();
