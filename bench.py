@@ -262,9 +262,142 @@ def time_form(ctx, g, w, precision, seed, steps, warmup, stream, flush):
     return ms, stats, out, emb
 
 
+# lne_dense_embed: CholeskyQR3 (3 x (Gram + reduction, Cholesky/inverse,
+# update GEMM) + one trace), Gram, Jacobi (init, sweeps, finish), column
+# scaling, GEMM, row normalisation
+DENSE_EMBED_LAUNCHES = 3 * 4 + 1 + 2 + 3 + 1 + 1 + 1
+
+
 def launches_of(st):
     return (st["sparsify"]["kernel_launches"] + st["randsvd"]["kernel_launches"] +
-            st["propagate"]["kernel_launches"] + 12)  # dense embed: QR3 (12 incl. gram/chol), gram, jacobi, gemm...
+            st["propagate"]["kernel_launches"] + DENSE_EMBED_LAUNCHES)
+
+
+class _DevArray:
+    """A device buffer of the library seen by torch without a copy."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, False), "version": 3}
+
+
+def plain_fp32_step(ctx, g, w, seed, A_struct, lib):
+    """The plain FP32 GPU form: the same sparsifier, then the reference's
+    dense stages as unfused library calls on the GPU (cuSPARSE SpMM through
+    torch.sparse, cuSOLVER QR and SVD, cuBLAS GEMMs, one elementwise kernel
+    per axpy): MKLRedSVD::run (mklredsvd.cc:93-403), compute_u_sigma_root
+    (PathEmbed.h:371-408), chebyshev_expansion (SpectralPropagation.h:45-221)
+    and get_embedding_dense (SpectralPropagation.h:16-43)."""
+    import ctypes
+
+    import torch
+
+    from lightne_gb300.api import generate_trunc_log_matrix_v2
+    ratio = float(np.float32(w["sample_ratio"]))
+    csr, _ = generate_trunc_log_matrix_v2(ctx, g, seed, walk_len=w["walk_len"], table_size=w["tablesz"],
+                                          sample_ratio=ratio)
+    n, nnz, r, d = csr.n, csr.nnz, w["rank"], w["dim"]
+    rp, cp, vp = csr.device_ptrs()
+    crow = torch.as_tensor(_DevArray(rp, (n + 1,), "<i8"), device="cuda").to(torch.int32)
+    col = torch.as_tensor(_DevArray(cp, (nnz,), "<i4"), device="cuda")
+    val = torch.as_tensor(_DevArray(vp, (nnz,), "<f4"), device="cuda")
+    A = torch.sparse_csr_tensor(crow, col, val, size=(n, n))
+    omega = torch.empty(n, r, dtype=torch.float32, device="cuda")
+    _lib_check(lib.lne_gaussian(ctx.handle, SVD_SEED, 0, n, r, ctypes.c_void_p(omega.data_ptr()), r))
+    P = torch.empty(r, r, dtype=torch.float32, device="cuda")
+    _lib_check(lib.lne_gaussian(ctx.handle, SVD_SEED, 1, r, r, ctypes.c_void_p(P.data_ptr()), r))
+    Y = A @ omega
+    Q = torch.linalg.qr(Y).Q
+    B = A @ Q
+    Z = torch.linalg.qr(B @ P).Q
+    C = Z.T @ B
+    U, S, _ = torch.linalg.svd(C)
+    emb = Z @ (U[:, :d] * torch.sqrt(S[:d]))
+    # propagation: M = (I - D~^-1 (A + I)) - mu I on the graph, recursion
+    # with one SpMM and separate axpys per half-step
+    crow_m, col_m, dt = A_struct
+    mu, sp = 0.2, 0.5
+    inv = 1.0 / dt
+    vals = torch.empty(col_m.numel(), dtype=torch.float32, device="cuda")
+    vals.copy_(torch.repeat_interleave(-inv, (crow_m[1:] - crow_m[:-1]).long()))
+    vals[crow_m[:-1].long()] = 1.0 - mu - inv
+    M = torch.sparse_csr_tensor(crow_m, col_m, vals, size=(n, n))
+    coef = [float(x) for x in chebyshev_coef(w["order"], sp)]
+    a = emb
+    T0 = a
+    T1 = 0.5 * (M @ (M @ a)) - a
+    conv = coef[0] * T0 + coef[1] * T1
+    for k in range(2, w["order"]):
+        T2 = M @ (M @ T1) - 2.0 * T1 - T0
+        conv = conv + coef[k] * T2
+        T0, T1 = T1, T2
+    a = a - conv
+    ones = torch.ones(col_m.numel(), dtype=torch.float32, device="cuda")
+    AI = torch.sparse_csr_tensor(crow_m, col_m, ones, size=(n, n))
+    y = AI @ a
+    Uy, Sy, _ = torch.linalg.svd(y, full_matrices=False)
+    out = Uy * torch.sqrt(Sy)
+    out = out / torch.clamp(out.norm(dim=1, keepdim=True), min=1e-30)
+    csr.free()
+    return out
+
+
+def chebyshev_coef(order, s):
+    from lightne_gb300.api import chebyshev_coefficients
+    return chebyshev_coefficients(order, s)
+
+
+def _lib_check(rc):
+    from lightne_gb300 import _lib
+    _lib.check(rc)
+
+
+def plain_struct(off, nbrs):
+    """CSR structure of A + I with the self loop first in every row (the
+    operator's layout, SpectralPropagation.h:51-75) and d~ = degree + 1."""
+    import torch
+    n = off.size - 1
+    deg = np.diff(off)
+    crow = (off + np.arange(n + 1)).astype(np.int32)
+    col = np.empty(crow[-1], dtype=np.int32)
+    col[crow[:-1]] = np.arange(n, dtype=np.int32)
+    mask = np.ones(crow[-1], dtype=bool)
+    mask[crow[:-1]] = False
+    col[mask] = nbrs
+    return (torch.from_numpy(crow).cuda(), torch.from_numpy(col).cuda(),
+            torch.from_numpy((deg + 1).astype(np.float32)).cuda())
+
+
+def time_plain(ctx, g, w, seed, off, nbrs, steps, warmup, stream, flush):
+    import torch
+
+    from lightne_gb300 import _lib
+    lib = _lib.load()
+    st = plain_struct(off, nbrs)
+    for _ in range(warmup):
+        plain_fp32_step(ctx, g, w, seed, st, lib)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        plain_fp32_step(ctx, g, w, seed, st, lib)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    return float(np.mean(times))
+
+
+def profiled_traffic(name):
+    """dram__bytes_read.sum + dram__bytes_write.sum per launch, from the line
+    `traffic_bytes_per_launch: N` of a committed ncu summary in profiles/."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return int(line.split(":")[1])
+    return None
 
 
 def run_ours(args, ws, rank, local):
@@ -319,6 +452,9 @@ def run_ours(args, ws, rank, local):
     e2e_s = allmax(ws, float(np.mean(e2e_t)))
     h2d = off.nbytes + nbrs.nbytes
     d2h = host_out.numel() * 4
+    ms_plain = None
+    if rank == 0 and not args.no_plain:
+        ms_plain = time_plain(ctx, g, w, seed, off, nbrs, max(1, min(args.steps, 2)), 1, stream, flush)
 
     if rank == 0:
         hbm, kind = peaks()
@@ -333,21 +469,25 @@ def run_ours(args, ws, rank, local):
             gath = 8 * (n + 1) + 8 * nnz + nnz * ld * sx + n * ld * 4
             return ms, comp / (ms / 1e3) / 1e9, gath / (ms / 1e3) / 1e9
 
-        ms_spmm_bf, comp_bf, gath_bf = spmm_gbs(st_bf, 2)
+        # B = A Q reads the FP32 Q in both forms (s_x = 4)
+        ms_spmm_bf, comp_bf, gath_bf = spmm_gbs(st_bf, 4)
         ms_spmm_fp, comp_fp, gath_fp = spmm_gbs(st_fp, 4)
         ms_sample = float(np.mean([x["sparsify"]["ms_sample"] for x in st_bf]))
         sampler_gbs = samples * 70.0 / (ms_sample / 1e3) / 1e9
         stage = lambda st, a, b: float(np.mean([x[a][b] for x in st]))  # noqa: E731
-        # the largest single kernel: the sampler (one launch) or the SVD SpMM
-        if ms_sample >= ms_spmm_bf:
-            roof = {"kernel": "k_sample (path sampler + pair-table insert)", "bound": "hbm",
-                    "achieved": sampler_gbs, "bytes_model": "70 B/sample (54 B walk gathers + 16 B slot)",
-                    "ms_per_launch": ms_sample}
-        else:
-            roof = {"kernel": "k_spmm (B = A Q, BF16 operand)", "bound": "hbm", "achieved": comp_bf,
-                    "bytes_model": "compulsory: 8(n+1) + 8 nnz + n ld 2 + n ld 4", "ms_per_launch": ms_spmm_bf}
-        roof.update({"peak": hbm, "unit": "GB/s", "frac": roof["achieved"] / hbm, "peak_kind": kind,
-                     "traffic": None})
+        # The dominant kernel (largest share of the step in the ncu launch
+        # list): the randomized SVD's SpMM B = A Q (k_spmm<float>, one launch
+        # per step), timed by the library's CUDA events on the launching
+        # stream.  Its DRAM traffic per launch comes from the committed ncu
+        # capture of the same kernel at this workload.
+        comp_bytes = 8 * (n + 1) + 8 * nnz + 2 * n * ld * 4
+        traffic = profiled_traffic("spmm_fp32_c2.md") if args.workload == "c2" else None
+        roof = {"kernel": "k_spmm<float> (B = A Q, FP32 Q, n x %d: one lne_spmm call, two column-slab launches "
+                          "+ chunk sums)" % ld, "bound": "hbm", "achieved": comp_bf,
+                "bytes_model": "compulsory 8(n+1) + 8 nnz + n ld 4 (Q) + n ld 4 (B) = %d B per launch" % comp_bytes,
+                "ms_per_launch": ms_spmm_bf, "achieved_gather_model": gath_bf,
+                "peak": hbm, "unit": "GB/s", "frac": comp_bf / hbm, "peak_kind": kind, "traffic": traffic,
+                "traffic_GB/s": None if traffic is None else traffic / (ms_spmm_bf / 1e3) / 1e9}
         line = {
             "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_bf, "higher_is_better": True, "scaling": "weak",
@@ -368,6 +508,10 @@ def run_ours(args, ws, rank, local):
                 "spmm_svd_bf16": {"ms": ms_spmm_bf, "GB/s_compulsory": comp_bf, "GB/s_gather": gath_bf},
                 "spmm_svd_fp32": {"ms": ms_spmm_fp, "GB/s_compulsory": comp_fp, "GB/s_gather": gath_fp},
                 "sampler_GB/s": sampler_gbs,
+                "plain_fp32_gpu": None if ms_plain is None else {
+                    "embed_secs": ms_plain / 1e3, "bf16_form_speedup": ms_plain / ms_bf,
+                    "form": "same sparsifier; dense stages as unfused cuSPARSE/cuSOLVER/cuBLAS calls via torch, "
+                            "FP32"},
             },
             "e2e": {"value": samples * ws / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s},
@@ -382,6 +526,78 @@ def run_ours(args, ws, rank, local):
             line["cpu_baseline"] = {"value": c["samples"] / c["total"], "unit": "samples/s", "cores": c["cores"],
                                     "kind": "port", "sample": cpu_sample_text(c), "seconds": c["total"]}
         print(json.dumps(line))
+    ctx.close()
+
+
+def run_micro(args, local):
+    """One C-ABI call timed alone at the workload's sizes (CUDA events on the
+    context's stream, 512 MiB L2 flush before every launch): the Gram
+    (lne_gram, A = B, n x rank), the tall update GEMM (lne_gemm_tall,
+    n x rank times rank x rank) or the randomized SVD's SpMM B = A Q
+    (lne_spmm, FP32 Q, n x ld).  Prints ms per launch and the bytes model."""
+    import ctypes
+
+    import torch
+
+    from lightne_gb300 import _lib
+    from lightne_gb300.api import Context, Graph, generate_trunc_log_matrix_v2
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    lib = _lib.load()
+    stream = torch.cuda.current_stream()
+    ctx = Context(local, stream=stream.cuda_stream)
+    n = w["n"]
+    r = w["rank"]
+    ld = (r + 7) // 8 * 8
+    vp = ctypes.c_void_p
+    X = torch.empty((n, ld), dtype=torch.float32, device="cuda")
+    _lib.check(lib.lne_gaussian(ctx.handle, 1, 7, n, ld, vp(X.data_ptr()), ld))
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    csr = None
+    if args.micro == "gram":
+        G = torch.empty((r, r), dtype=torch.float64, device="cuda")
+        call = lambda: lib.lne_gram(ctx.handle, vp(X.data_ptr()), ld, r, vp(X.data_ptr()), ld, r, n,  # noqa: E731
+                                    vp(G.data_ptr()))
+        model = n * ld * 4
+        bytes_text = "n ld 4 (A read once)"
+    elif args.micro == "gemm":
+        W = torch.randn((r, r), dtype=torch.float32, device="cuda")
+        Out = torch.empty((n, ld), dtype=torch.float32, device="cuda")
+        call = lambda: lib.lne_gemm_tall(ctx.handle, vp(X.data_ptr()), ld, r, vp(W.data_ptr()), r, n,  # noqa: E731
+                                         vp(Out.data_ptr()), ld)
+        model = 2 * n * ld * 4
+        bytes_text = "2 n ld 4 (In read, Out written)"
+    else:
+        off, nbrs = load_graph(args.workload)
+        g = Graph.from_numpy(ctx, off, nbrs)
+        csr, _ = generate_trunc_log_matrix_v2(ctx, g, w["seed"], walk_len=w["walk_len"], table_size=w["tablesz"],
+                                              sample_ratio=float(np.float32(w["sample_ratio"])))
+        g.free()
+        Y = torch.empty((n, ld), dtype=torch.float32, device="cuda")
+        call = lambda: lib.lne_spmm(ctx.handle, csr.handle, 0, vp(X.data_ptr()), ld, ld, 1.0, 0.0,  # noqa: E731
+                                    vp(Y.data_ptr()), ld)
+        model = 8 * (n + 1) + 8 * csr.nnz + 2 * n * ld * 4
+        bytes_text = "8(n+1) + 8 nnz + 2 n ld 4 (CSR, Q once, B written)"
+    for _ in range(args.warmup):
+        _lib.check(call())
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        _lib.check(call())
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = float(np.mean(times))
+    hbm, kind = peaks()
+    print(json.dumps({"micro": args.micro, "workload": w["label"], "n": n, "rank": r, "ld": ld,
+                      "nnz": csr.nnz if csr else None, "ms_per_launch": ms, "bytes_model": bytes_text,
+                      "bytes": model, "GB/s": model / (ms / 1e3) / 1e9, "peak_GB/s": hbm, "peak_kind": kind,
+                      "frac": model / (ms / 1e3) / 1e9 / hbm}))
+    if csr:
+        csr.free()
     ctx.close()
 
 
@@ -434,6 +650,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy", action="store_true")
     ap.add_argument("--quick", action="store_true", help="BF16 form only, no e2e / CPU legs (for profiling)")
+    ap.add_argument("--micro", choices=["gram", "gemm", "spmm"], help="time one C-ABI call alone (for profiling)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 GPU form (library calls) leg")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -443,7 +661,10 @@ def main():
         if rank == 0:
             build.build()
         barrier(ws)
-        run_ours(args, ws, rank, local)
+        if args.micro:
+            run_micro(args, local)
+        else:
+            run_ours(args, ws, rank, local)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -330,6 +330,10 @@ __global__ void __launch_bounds__(1024) k_chol_inv_smem(const double* __restrict
   if (tid == 0) *status = 0;
 }
 
+int cholesky_inv_launches(lne_ctx* ctx, int r) {
+  return (r <= kCholSmemMax && sizeof(double) * ((size_t)r * r + r) <= ctx->smem_optin) ? 1 : 2;
+}
+
 int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W) {
   double* X = nullptr;
   int* status = nullptr;

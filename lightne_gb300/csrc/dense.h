@@ -33,6 +33,8 @@ int gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W,
 // Cholesky G + shift*I = L L^T (FP64, in place on a device r x r buffer) and
 // W = L^-T as FP32 (r x r row-major, upper triangular).  Returns
 // LNE_ERR_NUMERIC when a pivot is not positive.
+// Kernel launches of one cholesky_inv call for an r x r matrix.
+int cholesky_inv_launches(lne_ctx* ctx, int r);
 int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W);
 
 // One-sided Jacobi SVD of C (r x r, FP64 row-major, device; overwritten):

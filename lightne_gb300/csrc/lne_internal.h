@@ -124,7 +124,9 @@ size_t scan_tmp_bytes(int64_t n);
 void scan_exclusive_i64(const int64_t* counts, int64_t* out, int64_t n, void* tmp,
                         cudaStream_t stream);
 
-// SpMM work lists (built on ctx->stream; synchronises once).
+// SpMM work lists (built on ctx->stream; synchronises once): a count
+// kernel, three exclusive scans of three launches each, a fill kernel.
+static constexpr int kPlanLaunches = 11;
 int build_plan_csr(lne_ctx* ctx, lne_csr* c);
 int build_plan_graph(lne_ctx* ctx, lne_graph* g);
 void free_plan(SpmmPlan& p);

@@ -105,7 +105,7 @@ static int cholqr3(lne_ctx* ctx, float* X, float* tmp, int64_t n, int64_t ld, in
         shift = (pass == 0 && attempt == 0 ? 64.0 : 64.0 * pow(10.0, attempt)) * u32 * tr;
       }
       rc = cholesky_inv(ctx, G, r, shift, W);
-      *launches += 2;
+      *launches += cholesky_inv_launches(ctx, r);
       if (rc == LNE_OK) break;
       if (rc != LNE_ERR_NUMERIC || attempt == 5) return rc;
     }
@@ -228,7 +228,7 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
   if ((rc = gram(ctx, Y, ld, r, Bm, ld, r, n, C))) return rc;
   int sweeps = 0;
   if ((rc = jacobi_svd(ctx, C, r, U, S, &sweeps))) return rc;
-  launches += 3;
+  launches += 2 + 3;  // Gram + reduction, Jacobi init / sweeps / finish
   // emb = Z * (U_C[:, :dim] * diag(sqrt(S[:dim])))
   if ((rc = B.get(&Wf, (size_t)r * dim, "U sqrt(S)"))) return rc;
   k_scale_cols<<<(r * dim + 255) / 256, 256, 0, st>>>(U, S, r, dim, Wf);

@@ -92,6 +92,7 @@ static int spmm_csr_panels(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ldx, i
   const int64_t xbytes = A->n * row_bytes;
   int rc;
   if (ctx->spmm_panel_bytes <= 0 || xbytes <= ctx->spmm_panel_bytes) {
+    if (!A->plan_ready && launches) *launches += kPlanLaunches;
     if ((rc = build_plan_csr(ctx, A))) return rc;
     CsrRows R{A->row_ptr, A->col, A->val};
     epi.add = false;

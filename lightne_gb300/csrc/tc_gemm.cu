@@ -235,21 +235,24 @@ __device__ __forceinline__ void split4(const float4& x, float4& h, float4& l) {
   l.w = x.w - h.w;
 }
 
-// 2 K = 8 steps x (hi*hi + hi*lo + lo*hi) on one slice.
-__device__ __forceinline__ void issue_slice(uint32_t tmem_d, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
-                                            uint32_t b_lo, uint32_t idesc, bool first) {
-  const uint32_t lbo = 128, sbo = (kSlice / 4) * 128;
+// 2 K = 8 steps x (hi*hi + hi*lo + lo*hi) on one slice.  The descriptors
+// of the slice's first K step are passed in; the start address field is
+// address >> 4 (shared memory addresses stay below 2^18, so the 14-bit field
+// never carries), so the next K step (256 bytes on) is descriptor + 16.
+template <int SL = kSlice>
+__device__ __forceinline__ void issue_slice(uint32_t tmem_d, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
+                                            uint32_t idesc, bool first) {
 #pragma unroll
-  for (int ks = 0; ks < kSlice / 8; ++ks) {
-    const uint32_t koff = (uint32_t)ks * 256;
-    const uint64_t ah = tc::smem_desc(a_hi + koff, lbo, sbo);
-    const uint64_t al = tc::smem_desc(a_lo + koff, lbo, sbo);
-    const uint64_t bh = tc::smem_desc(b_hi + koff, lbo, sbo);
-    const uint64_t bl = tc::smem_desc(b_lo + koff, lbo, sbo);
-    tc::mma_tf32(tmem_d, ah, bh, idesc, (first && ks == 0) ? 0u : 1u);
-    tc::mma_tf32(tmem_d, ah, bl, idesc, 1u);
-    tc::mma_tf32(tmem_d, al, bh, idesc, 1u);
+  for (int ks = 0; ks < SL / 8; ++ks) {
+    const uint64_t ko = (uint64_t)(ks * 16);
+    tc::mma_tf32(tmem_d, ah + ko, bh + ko, idesc, (first && ks == 0) ? 0u : 1u);
+    tc::mma_tf32(tmem_d, ah + ko, bl + ko, idesc, 1u);
+    tc::mma_tf32(tmem_d, al + ko, bh + ko, idesc, 1u);
   }
+}
+template <int SL = kSlice>
+__device__ __forceinline__ uint64_t slice_desc(uint32_t saddr) {
+  return tc::smem_desc(saddr, 128, (SL / 4) * 128);
 }
 
 __device__ __forceinline__ void stream_setup(StreamShared* sh, uint32_t cols) {
@@ -349,8 +352,11 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
     tc::cp_async_commit();
     tc::cp_async_wait<kGemmRing - 1>();
     const int cb = (int)(g & 1);
-    if (g >= 2 && !tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)(((g - 2) >> 1) & 1), kWaitCycles,
-                                 flags + kFlagNumeric))
+    // operand buffer cb is free once the MMAs of slice g - 2 are done: one
+    // thread waits, the barrier releases the others
+    if (g >= 2 && t == 0 &&
+        !tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)(((g - 2) >> 1) & 1), kWaitCycles,
+                       flags + kFlagNumeric))
       ok = false;
     __syncthreads();  // slice g visible to every thread; operand buffer cb free
     {
@@ -372,8 +378,8 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
     if (t == 0) {
       tc::fence_after_sync();
       const uint32_t a_hi = tc::smem_addr(conv + (size_t)cb * 2 * kASlice);
-      issue_slice(tmem, a_hi, a_hi + kASlice, tc::smem_addr(w_hi + (size_t)sl * wslice),
-                  tc::smem_addr(w_lo + (size_t)sl * wslice), idesc, sl == 0);
+      issue_slice(tmem, slice_desc(a_hi), slice_desc(a_hi + kASlice), slice_desc(tc::smem_addr(w_hi) + sl * wslice),
+                  slice_desc(tc::smem_addr(w_lo) + sl * wslice), idesc, sl == 0);
       tc::commit(tc::smem_addr(&sh->mbar[cb]));
     }
     last_commit = g;
@@ -418,7 +424,8 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
   stream_finish(sh, tmem, 256, ok, last_commit, flags);
 }
 
-// Partial Gram of one contiguous range of 16-row slices per CTA:
+// Partial Gram of one contiguous range of SL-row slices per CTA (SL = 32
+// where the stages fit in shared memory, else 16):
 // partial[b] (c1 x c2) = A[rows]^T B[rows].  Both 128-column tiles of A are
 // accumulated by the CTA (D0 for columns 0..127 of A, D1 for 128..255; D1
 // sits right after D0 in the TMEM column space).  When A and B are the same
@@ -429,27 +436,33 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
 // low bits of each addition are dropped), so a long accumulation chain
 // drifts towards zero by about 2^-25 of the sum per MMA.  Every kGroup
 // slices (64 rows) the TMEM sums are therefore added into FP32 registers
-// (rounded to nearest) and the next group starts a fresh TMEM sum.  With
+// (rounded to nearest) and the next group starts a fresh TMEM sum.  (A group
+// is 64 / SL slices.)  With
 // room for two TMEM sets the group just finished is read while the next
 // one accumulates in the other set; otherwise the drain waits for the
 // group's MMAs.
-constexpr int kGroup = 4;
+constexpr int kGroupRows = 64;
 constexpr int kMaxChunks = 9;  // 16-column chunks per thread: sets up to 288 columns
 
+template <int SL, int RING>
 __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __restrict__ A, int64_t lda, int c1,
                                                                  const float* __restrict__ B, int64_t ldb, int c2,
                                                                  int nmma, int64_t n, int sym, int64_t per,
                                                                  float* __restrict__ partial, int* flags) {
   extern __shared__ __align__(1024) uint8_t stream_smem[];
   const int mt = c1 > 128 ? 2 : 1;
-  const uint32_t a_part = (uint32_t)(128 * mt) * kSliceRowBytes;   // one part (hi or lo) of the A operand
-  const uint32_t b_part = sym ? 0u : (uint32_t)nmma * kSliceRowBytes;
+  constexpr uint32_t kRowBytes = SL * 4;   // one operand row of a slice
+  constexpr int kGroup = kGroupRows / SL;
+  constexpr int kTpr = kSThreads / SL;     // loading threads per slice row
+  constexpr int kQ = SL / 4;               // K groups per slice
+  const uint32_t a_part = (uint32_t)(128 * mt) * kRowBytes;   // one part (hi or lo) of the A operand
+  const uint32_t b_part = sym ? 0u : (uint32_t)nmma * kRowBytes;
   const uint32_t stage = 2 * a_part + 2 * b_part;
   const int c1p = (c1 + 3) & ~3, c2p = sym ? 0 : (c2 + 3) & ~3;
-  const uint32_t raw_slot = (uint32_t)(kSlice * (c1p + c2p) * 4);
+  const uint32_t raw_slot = (uint32_t)(SL * (c1p + c2p) * 4);
   uint8_t* conv = stream_smem;
   uint8_t* raw = stream_smem + 2 * (size_t)stage;
-  StreamShared* sh = reinterpret_cast<StreamShared*>(raw + (size_t)kGramRing * raw_slot);
+  StreamShared* sh = reinterpret_cast<StreamShared*>(raw + (size_t)RING * raw_slot);
   const int t = threadIdx.x;
   stream_setup(sh, 512);
   const uint32_t tmem = sh->tmem_base;
@@ -458,7 +471,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __
   const bool dbuf = 2 * set_cols <= 512;
   const uint32_t idesc0 = tc::idesc_tf32(128, nmma);
   const uint32_t idesc1 = tc::idesc_tf32(128, n1 > 0 ? n1 : 16);
-  const int64_t nslices = (n + kSlice - 1) / kSlice;
+  const int64_t nslices = (n + SL - 1) / SL;
   const int64_t s0 = (int64_t)blockIdx.x * per;
   const int64_t left = nslices - s0;
   const int64_t total = left <= 0 ? 0 : (left < per ? left : per);
@@ -487,40 +500,72 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __
   };
   auto set_base = [&](int64_t g) -> uint32_t { return dbuf ? (uint32_t)(((g / kGroup) & 1) * 256) : 0u; };
 
+  // Loads: thread t copies row t / kTpr of the slice, 16-byte chunks
+  // t % kTpr, t % kTpr + kTpr, ...; rows past n land as zeros.
+  const int lk = t / kTpr, lq = t % kTpr;
   auto issue_load = [&](int64_t g) {
-    const int64_t r0 = (s0 + g) * kSlice;
-    const uint32_t dst0 = tc::smem_addr(raw + (size_t)(g % kGramRing) * raw_slot);
-    for (int idx = t; idx < kSlice * (qa + qb); idx += kSThreads) {
-      const bool isb = idx >= kSlice * qa;
-      const int li = isb ? idx - kSlice * qa : idx;
-      const int qn = isb ? qb : qa;
-      const int k = li / qn, q = li % qn;
-      const int64_t row = r0 + k;
-      const int cb = (isb ? c2 : c1) - 4 * q;
-      const uint32_t bytes = (row < n) ? (uint32_t)(cb >= 4 ? 16 : 4 * cb) : 0u;
-      const float* src = isb ? B + row * ldb + 4 * q : A + row * lda + 4 * q;
-      const uint32_t doff = isb ? (uint32_t)((kSlice * c1p + k * c2p + 4 * q) * 4) : (uint32_t)((k * c1p + 4 * q) * 4);
-      tc::cp_async16(dst0 + doff, bytes ? src : (isb ? B : A), bytes);
+    const int64_t row = (s0 + g) * SL + lk;
+    const bool rv = row < n;
+    const uint32_t dst0 = tc::smem_addr(raw + (size_t)(g % RING) * raw_slot);
+    const float* arow = A + (rv ? row : 0) * lda;
+    for (int q = lq; q < qa; q += kTpr) {
+      const int cb = c1 - 4 * q;
+      tc::cp_async16(dst0 + (uint32_t)((lk * c1p + 4 * q) * 4), arow + 4 * q,
+                     rv ? (uint32_t)(cb >= 4 ? 16 : 4 * cb) : 0u);
     }
+    if (!sym) {
+      const float* brow = B + (rv ? row : 0) * ldb;
+      for (int q = lq; q < qb; q += kTpr) {
+        const int cb = c2 - 4 * q;
+        tc::cp_async16(dst0 + (uint32_t)((SL * c1p + lk * c2p + 4 * q) * 4), brow + 4 * q,
+                       rv ? (uint32_t)(cb >= 4 ? 16 : 4 * cb) : 0u);
+      }
+    }
+  };
+  // Conversion of operand row j (a column of the data), K group q (raw rows
+  // 4q..4q+3).  Thread t takes column t % 128 with groups q0 = (t / 128)
+  // kQ / 2 .. q0 + kQ / 2 - 1, and the columns past 128 are spread one
+  // (column, group) per thread: e -> (128 + e / kQ, e % kQ).
+  auto convert_one = [&](const float* rs, int ld, int j, int q, uint8_t* hi, uint32_t part) {
+    const float* col = rs + (4 * q) * ld + j;
+    const float4 x = make_float4(col[0], col[ld], col[2 * ld], col[3 * ld]);
+    float4 h, l;
+    split4(x, h, l);
+    const uint32_t off = tc::kmajor_off((uint32_t)j, (uint32_t)(4 * q), SL);
+    *reinterpret_cast<float4*>(hi + off) = h;
+    *reinterpret_cast<float4*>(hi + part + off) = l;
+  };
+  auto convert = [&](const float* rs, int ld, int cn, uint8_t* hi, uint32_t part) {
+    const int j = t & 127, q0 = (t >> 7) * (kQ / 2);
+    if (j < cn) {
+#pragma unroll
+      for (int q = 0; q < kQ / 2; ++q) convert_one(rs, ld, j, q0 + q, hi, part);
+    }
+    for (int e = t; e < kQ * (cn - 128); e += kSThreads) convert_one(rs, ld, 128 + e / kQ, e % kQ, hi, part);
   };
 
   bool ok = true;
   int64_t last_commit = -1;
-  for (int64_t g = 0; g < kGramRing - 1; ++g) {
+  for (int64_t g = 0; g < RING - 1; ++g) {
     if (g < total) issue_load(g);
     tc::cp_async_commit();
   }
   for (int64_t g = 0; g < total && ok; ++g) {
-    if (g + kGramRing - 1 < total) issue_load(g + kGramRing - 1);
+    if (g + RING - 1 < total) issue_load(g + RING - 1);
     tc::cp_async_commit();
-    tc::cp_async_wait<kGramRing - 1>();
+    tc::cp_async_wait<RING - 1>();
     const int cb = (int)(g & 1);
-    if (g >= 2 && !tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)(((g - 2) >> 1) & 1), kWaitCycles,
-                                 flags + kFlagNumeric))
+    const bool drain_now = dbuf && g % kGroup == 1 && g > kGroup;
+    // operand buffer cb is free once the MMAs of slice g - 2 are done: one
+    // thread waits and the barrier below releases the others (every thread
+    // waits when TMEM is read next)
+    if (g >= 2 && (t == 0 || drain_now) &&
+        !tc::mbar_wait(tc::smem_addr(&sh->mbar[cb]), (uint32_t)(((g - 2) >> 1) & 1), kWaitCycles,
+                       flags + kFlagNumeric))
       ok = false;
     // the MMAs of slice g - 2 are done, hence (dbuf) every MMA of the group
     // that ended with slice g - 2: add that set into the registers
-    if (dbuf && g % kGroup == 1 && g > kGroup) {
+    if (drain_now) {
       ok = __syncthreads_and(ok ? 1 : 0) != 0;
       if (!ok) break;
       tc::fence_after_sync();
@@ -529,25 +574,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __
     }
     __syncthreads();
     {
-      const float* rs = reinterpret_cast<const float*>(raw + (size_t)(g % kGramRing) * raw_slot);
+      const float* rs = reinterpret_cast<const float*>(raw + (size_t)(g % RING) * raw_slot);
       uint8_t* st = conv + (size_t)cb * stage;
-      // operand row j, K group q <- raw rows 4q..4q+3, column j
-      for (int idx = t; idx < 4 * (c1 + (sym ? 0 : c2)); idx += kSThreads) {
-        const bool isb = idx >= 4 * c1;
-        const int li = isb ? idx - 4 * c1 : idx;
-        const int cn = isb ? c2 : c1;
-        const int q = li / cn, j = li % cn;
-        const float* col = isb ? rs + kSlice * c1p + j : rs + j;
-        const int ld = isb ? c2p : c1p;
-        float4 x = make_float4(col[(4 * q) * ld], col[(4 * q + 1) * ld], col[(4 * q + 2) * ld], col[(4 * q + 3) * ld]);
-        float4 h, l;
-        split4(x, h, l);
-        uint8_t* hi = isb ? st + 2 * a_part : st;
-        const uint32_t part = isb ? b_part : a_part;
-        const uint32_t off = tc::kmajor_off((uint32_t)j, (uint32_t)(4 * q), kSlice);
-        *reinterpret_cast<float4*>(hi + off) = h;
-        *reinterpret_cast<float4*>(hi + part + off) = l;
-      }
+      convert(rs, c1p, c1, st, a_part);
+      if (!sym) convert(rs + SL * c1p, c2p, c2, st + 2 * a_part, b_part);
     }
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
@@ -561,11 +591,13 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __
       const uint32_t b_hi = sym ? a_hi : a_hi + 2 * a_part;
       const uint32_t b_lo = sym ? a_lo : b_hi + b_part;
       const bool first = g % kGroup == 0;
-      issue_slice(tmem + sb, a_hi, a_lo, b_hi, b_lo, idesc0, first);
+      issue_slice<SL>(tmem + sb, slice_desc<SL>(a_hi), slice_desc<SL>(a_lo), slice_desc<SL>(b_hi),
+                      slice_desc<SL>(b_lo), idesc0, first);
       if (mt == 2 && n1 > 0) {
-        const uint32_t m1 = 128 * kSliceRowBytes;  // row 128 of the A operand
+        const uint32_t m1 = 128 * kRowBytes;  // row 128 of the A operand
         const uint32_t b1 = sym ? m1 : 0u;
-        issue_slice(tmem + sb + (uint32_t)nmma, a_hi + m1, a_lo + m1, b_hi + b1, b_lo + b1, idesc1, first);
+        issue_slice<SL>(tmem + sb + (uint32_t)nmma, slice_desc<SL>(a_hi + m1), slice_desc<SL>(a_lo + m1),
+                        slice_desc<SL>(b_hi + b1), slice_desc<SL>(b_lo + b1), idesc1, first);
       }
       tc::commit(tc::smem_addr(&sh->mbar[cb]));
     }
@@ -644,12 +676,18 @@ static size_t gemm_stream_smem(int K, int nmma) {
   const size_t nsl = (size_t)(K + kSlice - 1) / kSlice;
   return 2 * nsl * nmma * kSliceRowBytes + (size_t)kGemmRing * kASlice + 4 * kASlice + sizeof(StreamShared);
 }
-static size_t gram_stream_smem(int c1, int c2, int nmma, bool sym) {
+static size_t gram_stream_smem(int c1, int c2, int nmma, bool sym, int sl, int ring) {
   const int mt = c1 > 128 ? 2 : 1;
-  const size_t a_part = (size_t)(128 * mt) * kSliceRowBytes;
-  const size_t b_part = sym ? 0 : (size_t)nmma * kSliceRowBytes;
+  const size_t a_part = (size_t)(128 * mt) * sl * 4;
+  const size_t b_part = sym ? 0 : (size_t)nmma * sl * 4;
   const size_t c1p = (c1 + 3) & ~3, c2p = sym ? 0 : (c2 + 3) & ~3;
-  return 2 * (2 * a_part + 2 * b_part) + (size_t)kGramRing * kSlice * (c1p + c2p) * 4 + sizeof(StreamShared);
+  return 2 * (2 * a_part + 2 * b_part) + (size_t)ring * sl * (c1p + c2p) * 4 + sizeof(StreamShared);
+}
+// Slice rows: 32 (ring of 5) when that fits, else 16 (ring of 6); 0: neither fits.
+static int gram_slice_rows(lne_ctx* ctx, int c1, int c2, int nmma, bool sym) {
+  if (gram_stream_smem(c1, c2, nmma, sym, 32, 5) <= ctx->smem_optin) return 32;
+  if (gram_stream_smem(c1, c2, nmma, sym, 16, kGramRing) <= ctx->smem_optin) return 16;
+  return 0;
 }
 static bool aligned16(const void* p, int64_t ld) {
   return (reinterpret_cast<uintptr_t>(p) & 15) == 0 && (ld & 3) == 0;
@@ -689,7 +727,7 @@ bool tc_gram_stream_supported(lne_ctx* ctx, const float* A, int64_t lda, int c1,
   const bool sym = A == B && lda == ldb && c1 == c2;
   const int set_cols = c1 > 128 ? nmma + (sym ? nmma - 128 : nmma) : nmma;
   return aligned16(A, lda) && aligned16(B, ldb) && set_cols <= 32 * kMaxChunks &&
-         gram_stream_smem(c1, c2, nmma, sym) <= ctx->smem_optin;
+         gram_slice_rows(ctx, c1, c2, nmma, sym) > 0;
 }
 
 int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int64_t ldb, int c2, int64_t n,
@@ -704,8 +742,10 @@ int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const floa
   }
   const int nmma = std::max(16, (c2 + 15) / 16 * 16);
   const bool sym = A == B && lda == ldb && c1 == c2;
-  const size_t ssmem = gram_stream_smem(c1, c2, nmma, sym);
-  const int64_t nslices = (n + kSlice - 1) / kSlice;
+  const int sl = gram_slice_rows(ctx, c1, c2, nmma, sym);
+  const int ring = sl == 32 ? 5 : kGramRing;
+  const size_t ssmem = gram_stream_smem(c1, c2, nmma, sym, sl, ring);
+  const int64_t nslices = (n + sl - 1) / sl;
   const int64_t want = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(nslices, ctx->num_sms), max_blocks));
   const int64_t per = (nslices + want - 1) / want;
   const int64_t nb = (nslices + per - 1) / per;  // <= want
@@ -717,9 +757,10 @@ int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const floa
   }
   // the CTA allocates all 512 TMEM columns: one CTA per SM
   const size_t lsmem = std::max(ssmem, std::min(ctx->smem_optin, (size_t)120 * 1024));
-  cudaFuncSetAttribute(k_tc_gram_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
-  k_tc_gram_stream<<<(unsigned)nb, kSThreads, lsmem, ctx->stream>>>(A, lda, c1, B, ldb, c2, nmma, n, sym ? 1 : 0, per,
-                                                                    partial, ctx->d_flags);
+  auto kern = sl == 32 ? k_tc_gram_stream<32, 5> : k_tc_gram_stream<16, kGramRing>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
+  kern<<<(unsigned)nb, kSThreads, lsmem, ctx->stream>>>(A, lda, c1, B, ldb, c2, nmma, n, sym ? 1 : 0, per, partial,
+                                                        ctx->d_flags);
   const int64_t cnt = (int64_t)c1 * c2;
   k_gram_reduce_stream<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, c1, c2, sym ? 1 : 0, G);
   if (own) dfree(ctx, own);

@@ -102,12 +102,12 @@ __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 // Waits for the phase with the given parity to complete; gives up after
-// `max_cycles` SM clock cycles (or at once when *abort is set) and returns
-// false so that the caller can record the timeout.
+// `max_cycles` SM clock cycles (or within 64 polls of *abort being set) and
+// returns false so that the caller can record the timeout.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long max_cycles,
                                           const volatile int* abort) {
   const long long t0 = clock64();
-  for (;;) {
+  for (uint32_t it = 0;; ++it) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred P1;\n\t"
@@ -117,7 +117,8 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long l
         : "r"(mbar), "r"(parity)
         : "memory");
     if (done) return true;
-    if (*abort != 0 || clock64() - t0 > max_cycles) return false;
+    // the abort flag is in global memory: look at it every 64 polls
+    if (((it & 63u) == 63u && *abort != 0) || clock64() - t0 > max_cycles) return false;
   }
 }
 
