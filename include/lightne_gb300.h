@@ -151,7 +151,10 @@ typedef struct lne_randsvd_params {
                                    A * Q reads FP32 Q in both forms */
   uint64_t seed;                /* Gaussian sketch seed (the reference's VSL seed is 777) */
   int32_t random_project_only;  /* -random_project_only: return (A * Omega)[:, :dim] */
-  int32_t reserved;
+  int32_t sparse_project;       /* -sparse_project: Omega is the very sparse random projection
+                                   (mklredsvd.cc:148-226) instead of the Gaussian sketch */
+  double sparse_project_s;      /* -sparse_project_s: s of the projection (density 1/s, values
+                                   +-sqrt(s)); below 1 means s = sqrt(n), as the reference */
 } lne_randsvd_params;
 
 typedef struct lne_randsvd_stats {
@@ -182,6 +185,27 @@ int lne_randsvd(lne_ctx* ctx, const lne_csr* A, const lne_randsvd_params* p, flo
  */
 int lne_gaussian(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols, float* d_out,
                  int64_t ld);
+
+/*
+ * -ne_method ne_zhang_et_al: the matrix NE_Zhang_et_al factorises
+ * (LightNE/PathEmbed.h:410-448): the graph's structure (neighbours in file
+ * order) with values (float)(log(1/d_i) - log(neg_v / sum neg)),
+ * neg_v = (sum over neighbours u of v of 1/d_u)^0.75, in FP64.  The CSR is
+ * passed to lne_randsvd with normalize = 1, as the reference does.
+ */
+int lne_ne_zhang_matrix(lne_ctx* ctx, const lne_graph* g, lne_csr** out);
+
+/*
+ * The very sparse random projection lne_randsvd uses with sparse_project
+ * (mklredsvd.cc:148-226): n x rank, row i with Binomial(rank, 1/s)
+ * nonzeros at distinct columns, values +-sqrt(s) (s as in
+ * lne_randsvd_params.sparse_project_s), written densely into device memory
+ * with leading dimension ld; *nnz_out (optional) receives its nonzero count.
+ * The reference draws it from MKL's VSL stream and time(0); this generator
+ * is counter-based, so a checker can rebuild the same sketch from the seed.
+ */
+int lne_sparse_projection(lne_ctx* ctx, uint64_t seed, int64_t n, int64_t rank, double s, float* d_out, int64_t ld,
+                          int64_t* nnz_out);
 
 /* Parameters of the spectral propagation (chebyshev_expansion). */
 typedef struct lne_propagate_params {

@@ -84,7 +84,8 @@ class RandsvdParams(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
         ("random_project_only", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("sparse_project", ctypes.c_int32),
+        ("sparse_project_s", ctypes.c_double),
     ]
 
 
@@ -150,6 +151,8 @@ SIGNATURES = {
     "lne_spmm": (ctypes.c_int, [VP, VP, ctypes.c_int, VP, I64, I64, ctypes.c_float, ctypes.c_float, VP, I64]),
     "lne_randsvd": (ctypes.c_int, [VP, VP, ctypes.POINTER(RandsvdParams), VP, VP, ctypes.POINTER(RandsvdStats)]),
     "lne_gaussian": (ctypes.c_int, [VP, ctypes.c_uint64, ctypes.c_uint64, I64, I64, VP, I64]),
+    "lne_sparse_projection": (ctypes.c_int, [VP, ctypes.c_uint64, I64, I64, ctypes.c_double, VP, I64, VP]),
+    "lne_ne_zhang_matrix": (ctypes.c_int, [VP, VP, VP]),
     "lne_propagate": (ctypes.c_int, [VP, VP, ctypes.POINTER(PropagateParams), VP, VP, VP,
                                      ctypes.POINTER(PropagateStats)]),
     "lne_propagate_adjoint": (ctypes.c_int, [VP, VP, ctypes.POINTER(PropagateParams), VP, VP, VP,

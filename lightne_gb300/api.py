@@ -172,6 +172,25 @@ def _as_device_f32(x, device):
     return x.to(device=f"cuda:{device}", dtype=torch.float32).contiguous()
 
 
+def ne_zhang_matrix(ctx: Context, graph: Graph) -> CSR:
+    """path_embed::NE_Zhang_et_al's matrix (LightNE/PathEmbed.h:410-448) on
+    the device; factorise it with ``randsvd(..., normalize=True)``."""
+    out = ctypes.c_void_p()
+    check(_lib.load().lne_ne_zhang_matrix(ctx.handle, graph.handle, ctypes.byref(out)))
+    return CSR(ctx, out)
+
+
+def sparse_projection(ctx: Context, seed: int, n: int, rank: int, s: float = 100.0):
+    """The very sparse random projection randsvd uses with sparse_project,
+    as a dense torch tensor n x rank, and its nonzero count."""
+    torch = _torch()
+    out = torch.empty(n, rank, dtype=torch.float32, device=f"cuda:{ctx.device}")
+    nnz = ctypes.c_int64()
+    check(_lib.load().lne_sparse_projection(ctx.handle, seed, n, rank, s, ctypes.c_void_p(out.data_ptr()), rank,
+                                            ctypes.byref(nnz)))
+    return out, nnz.value
+
+
 def gaussian(ctx: Context, seed: int, stream_id: int, rows: int, cols: int):
     """The device Gaussian sketch (stream 0: Omega, 1: P) as a torch tensor."""
     torch = _torch()
@@ -182,15 +201,19 @@ def gaussian(ctx: Context, seed: int, stream_id: int, rows: int, cols: int):
 
 
 def randsvd(ctx: Context, A: CSR, rank: int, dim: int, normalize: bool = False, precision: str = "fp32",
-            seed: int = 777, random_project_only: bool = False):
+            seed: int = 777, random_project_only: bool = False, sparse_project: bool = False,
+            sparse_project_s: float = 100.0):
     """MKLRedSVD(...).run() + compute_u_sigma_root on the device
     (LightNE/mklredsvd/mklredsvd.cc:93-403, LightNE/PathEmbed.h:371-408).
+    ``sparse_project`` takes the very sparse random projection sketch
+    (mklredsvd.cc:148-226) instead of the Gaussian one.
     Returns (emb torch n x dim, S numpy[rank], stats)."""
     torch = _torch()
     emb = torch.empty(A.n, dim, dtype=torch.float32, device=f"cuda:{ctx.device}")
     S = np.zeros(rank, dtype=np.float32)
     p = RandsvdParams(rank=rank, dim=dim, normalize=int(bool(normalize)), precision=PRECISIONS[precision],
-                      seed=seed, random_project_only=int(bool(random_project_only)))
+                      seed=seed, random_project_only=int(bool(random_project_only)),
+                      sparse_project=int(bool(sparse_project)), sparse_project_s=float(sparse_project_s))
     st = RandsvdStats()
     check(_lib.load().lne_randsvd(ctx.handle, A.handle, ctypes.byref(p), ctypes.c_void_p(emb.data_ptr()),
                                   _ptr(S), ctypes.byref(st)))

@@ -194,17 +194,13 @@ int main(int argc, char** argv) {
       step_coeff.push_back(std::stof(sub));
     }
   }
-  if (ne_method != "netsmf") {
-    fprintf(stderr, "LightNE: -ne_method %s is not supported by this build (netsmf only)\n", ne_method.c_str());
-    return LNE_ERR_UNSUPPORTED;
+  if (ne_method != "netsmf" && ne_method != "ne_zhang_et_al") {
+    fprintf(stderr, "LightNE: -ne_method must be netsmf or ne_zhang_et_al\n");
+    return LNE_ERR_INVALID;
   }
   if ((long)step_coeff.size() != walk_len) {
     fprintf(stderr, "LightNE: -step_coeff must have -walklen entries\n");
     return LNE_ERR_INVALID;
-  }
-  if (sparse_project) {
-    fprintf(stderr, "LightNE: -sparse_project 1 is not supported by this build\n");
-    return LNE_ERR_UNSUPPORTED;
   }
   const int prec = precision == "bf16" ? LNE_PREC_BF16 : LNE_PREC_FP32;
 
@@ -257,32 +253,40 @@ int main(int argc, char** argv) {
     fflush(stdout);
     const double t0 = now();
 
-    const uint64_t seed = seed_s ? strtoull(seed_s, nullptr, 10) : (uint64_t)time(nullptr);
-    printf("# seed = %llu\n", (unsigned long long)seed);
-    lne_sparsify_params sp = {seed, walk_len, table_size, negative, sample ? 1 : 0, 0, sample_ratio, mem_ratio};
-    // -upper keeps only the upper triangle for MKL's symmetric descriptor;
-    // the matrix is the same, so the full symmetric CSR is built for the SVD.
-    lne_sparsify_stats st;
     lne_csr* csr = nullptr;
-    if ((rc = lne_sparsify(ctx, g, &sp, &csr, &st))) {
-      if (rc == LNE_ERR_TABLE_FULL) printf("looping forever\n");
-      return fail(rc, "lne_sparsify");
+    const bool zhang = ne_method == "ne_zhang_et_al";
+    if (zhang) {
+      // NE_Zhang_et_al (PathEmbed.h:410-463): the 1-hop log matrix, then the
+      // same SVD with normalised rows
+      if ((rc = lne_ne_zhang_matrix(ctx, g, &csr))) return fail(rc, "lne_ne_zhang_matrix");
+    } else {
+      const uint64_t seed = seed_s ? strtoull(seed_s, nullptr, 10) : (uint64_t)time(nullptr);
+      printf("# seed = %llu\n", (unsigned long long)seed);
+      lne_sparsify_params sp = {seed, walk_len, table_size, negative, sample ? 1 : 0, 0, sample_ratio, mem_ratio};
+      // -upper keeps only the upper triangle for MKL's symmetric descriptor;
+      // the matrix is the same, so the full symmetric CSR is built for the SVD.
+      lne_sparsify_stats st;
+      if ((rc = lne_sparsify(ctx, g, &sp, &csr, &st))) {
+        if (rc == LNE_ERR_TABLE_FULL) printf("looping forever\n");
+        return fail(rc, "lne_sparsify");
+      }
+      printf("# logn = %g sample_ratio = %g mem_ratio = %g\n", st.logn, sample_ratio, mem_ratio);
+      printf("# table_size = %lld\n# actual table.size = %lld\n", (long long)st.table_size, (long long)st.capacity);
+      printf("# total samples = %g\n# 1/lambda = %g\n# exp_rv_rounded = %lld\n# fractional_bits = %g\n",
+             st.total_samples, st.inv_lambda, (long long)st.exp_rv_rounded, st.frac);
+      printf("PBBS-time: # count time: %.4f\n", st.ms_sample / 1e3);
+      printf("# tot wgh (samples) = %g\n# factor = %g\n", st.m_exact, st.factor);
+      printf("# nnz in upper triangle of sparsifier = %lld\n# nnz in sparsifier = %lld\n", (long long)st.nnz_upper,
+             (long long)st.nnz);
+      printf("PBBS-time: # generate matrix time: %.4f\n", (st.ms_sample + st.ms_trunclog + st.ms_csr) / 1e3);
     }
-    printf("# logn = %g sample_ratio = %g mem_ratio = %g\n", st.logn, sample_ratio, mem_ratio);
-    printf("# table_size = %lld\n# actual table.size = %lld\n", (long long)st.table_size, (long long)st.capacity);
-    printf("# total samples = %g\n# 1/lambda = %g\n# exp_rv_rounded = %lld\n# fractional_bits = %g\n",
-           st.total_samples, st.inv_lambda, (long long)st.exp_rv_rounded, st.frac);
-    printf("PBBS-time: # count time: %.4f\n", st.ms_sample / 1e3);
-    printf("# tot wgh (samples) = %g\n# factor = %g\n", st.m_exact, st.factor);
-    printf("# nnz in upper triangle of sparsifier = %lld\n# nnz in sparsifier = %lld\n", (long long)st.nnz_upper,
-           (long long)st.nnz);
-    printf("PBBS-time: # generate matrix time: %.4f\n", (st.ms_sample + st.ms_trunclog + st.ms_csr) / 1e3);
 
     float* d_emb = nullptr;
     if ((rc = lne_device_alloc(ctx, (int64_t)sizeof(float) * n * dim, (void**)&d_emb)))
       return fail(rc, "lne_device_alloc");
     std::vector<float> S(rank);
-    lne_randsvd_params rp = {rank, dim, normalize ? 1 : 0, prec, 777, random_project_only ? 1 : 0, 0};
+    lne_randsvd_params rp = {rank, dim, (normalize || zhang) ? 1 : 0, prec, 777, (random_project_only && !zhang) ? 1 : 0,
+                             (sparse_project && !zhang) ? 1 : 0, (double)sparse_project_s};
     lne_randsvd_stats rs;
     if ((rc = lne_randsvd(ctx, csr, &rp, d_emb, S.data(), &rs))) return fail(rc, "lne_randsvd");
     lne_csr_free(csr);

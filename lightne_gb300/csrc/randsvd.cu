@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "dense.h"
+#include "sparse_proj.h"
 #include "dense_common.cuh"
 #include "lne_internal.h"
 #include "spmm_core.cuh"
@@ -177,7 +178,14 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
 
   cudaEventRecord(ev[0], st);
   // Y = A * Omega
-  if (bf16) {
+  if (p->sparse_project) {
+    // Omega = the very sparse random projection (mklredsvd.cc:148-226): the
+    // product only touches A's nonzeros whose O row is not empty
+    SparseProjection O;
+    if ((rc = sparse_projection_build(ctx, n, r, p->seed, p->sparse_project_s, &O, &launches))) return rc;
+    if ((rc = sparse_projection_product(ctx, A, O, Y, ld, &launches))) return rc;
+    launches -= 1;  // the Gaussian draw counted below does not happen
+  } else if (bf16) {
     if ((rc = gaussian_fill_bf16(ctx, p->seed, 0, n, r, Xb, ld))) return rc;
     if ((rc = spmm_store<__nv_bfloat16>(ctx, A, Xb, ld, (int)ld, Y, &launches))) return rc;
   } else {

@@ -81,6 +81,28 @@ def randsvd(A: sp.csr_matrix, omega: np.ndarray, P: np.ndarray, dim: int, normal
     return u_sigma_root(matU, S, dim, normalize), S
 
 
+def ne_zhang_matrix(offsets: np.ndarray, nbrs: np.ndarray) -> sp.csr_matrix:
+    """The matrix NE_Zhang_et_al factorises (LightNE/PathEmbed.h:410-448):
+    the graph's structure with values (float)(log(1/d_i) - log(neg_v /
+    sum neg)), neg_v = (sum over neighbours u of v of 1/d_u)^0.75, FP64
+    before the narrowing (each neg_v summed in file order)."""
+    n = offsets.size - 1
+    deg = np.diff(offsets).astype(np.float64)
+    inv = np.zeros(n)
+    inv[deg > 0] = 1.0 / deg[deg > 0]
+    contrib = inv[nbrs]
+    neg = np.zeros(n)
+    for j in range(n):
+        s = 0.0
+        for e in range(offsets[j], offsets[j + 1]):
+            s += contrib[e]
+        neg[j] = s ** 0.75
+    neg_sum = float(np.sum(neg))
+    src = np.repeat(np.arange(n), np.diff(offsets))
+    val = (np.log(1.0 / deg[src]) - np.log(neg[nbrs] / neg_sum)).astype(np.float32)
+    return sp.csr_matrix((val, nbrs.astype(np.int64), offsets.astype(np.int64)), shape=(n, n))
+
+
 def operator_values(deg: np.ndarray, mu: float, narrow: bool = True):
     """Per-row diagonal and off-diagonal values of M as the reference stores
     them (floats computed in double, SpectralPropagation.h:62-72); with
