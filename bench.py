@@ -601,6 +601,138 @@ def run_micro(args, local):
     ctx.close()
 
 
+SCALE_RUNS = {
+    "c3": dict(kind="rmat", scale=22, edge_factor=16, seed=3, walk_len=10, per_edge=100, tablesz=4_250_000_000,
+               rank=138, dim=128, order=10,
+               label="R-MAT (0.57, 0.19, 0.19, 0.05) scale 22 edge factor 16 symmetrised dedup, T=10, "
+                     "samples=10*T*m, rank 138, dim 128, K=10"),
+    "c5": dict(kind="sbm", n=1 << 23, blocks=50, degree=24.0, ratio=20.0, seed=6, walk_len=10, per_edge=40,
+               tablesz=4_250_000_000, rank=138, dim=128, order=10, adam_steps=20,
+               label="SBM n=2^23, 50 equal blocks, mean degree 24, p_in/p_out=20, T=10, samples=4*T*m (the pair "
+                     "table of 10*T*m would need 2^34 slots = 275 GB), rank 138, dim 128, K=10, 20 Adam steps"),
+}
+
+
+def csr_checksum(csr):
+    """Order-sensitive checksum of a device CSR (row_ptr, col, float bits),
+    in 2^28-entry chunks (int64 sums wrap)."""
+    import torch
+    rp, cp, vp = csr.device_ptrs()
+    n, nnz = csr.n, csr.nnz
+    rpt = torch.as_tensor(_DevArray(rp, (n + 1,), "<i8"), device="cuda")
+    colt = torch.as_tensor(_DevArray(cp, (nnz,), "<i4"), device="cuda")
+    valt = torch.as_tensor(_DevArray(vp, (nnz,), "<i4"), device="cuda")
+    mono = bool((rpt[1:] >= rpt[:-1]).all().item()) and int(rpt[-1].item()) == nnz
+    h = int((rpt * 1000003).sum().item())
+    step = 1 << 28
+    for a in range(0, nnz, step):
+        b = min(nnz, a + step)
+        idx = torch.arange(a, b, device="cuda", dtype=torch.int64)
+        h += int((colt[a:b].long() * 2654435761 + valt[a:b].long() * 40503 + idx).sum().item())
+        h &= (1 << 63) - 1
+    return h, mono
+
+
+def run_scale(args, local):
+    """Configs 3 and 5 at full size (not the headline line): the sparsifier
+    twice (same CSR checksum: determinism at size), both SVD and propagation
+    forms, BF16 vs FP32 embedding distance; config 5 then learns (mu, s)
+    and a softmax classifier on the planted blocks with 20 Adam steps
+    through the propagation adjoint (10% seeded training split)."""
+    import math
+
+    import torch
+
+    from lightne_gb300 import graphs
+    from lightne_gb300.api import (ChebyshevPropagation, Context, Graph, chebyshev_expansion,
+                                   generate_trunc_log_matrix_v2, get_embedding_dense, randsvd)
+    from oracle import linalg_oracle as lo
+    torch.cuda.set_device(local)
+    w = SCALE_RUNS[args.workload]
+    t0 = time.time()
+    labels = None
+    if w["kind"] == "rmat":
+        off, nbrs = graphs.rmat(w["scale"], w["edge_factor"], seed=w["seed"])
+    else:
+        off, nbrs, labels = graphs.sbm(w["n"], w["blocks"], w["degree"], w["ratio"], seed=w["seed"])
+    gen_s = time.time() - t0
+    n, m = off.size - 1, nbrs.size // 2
+    ratio = float(np.float32(w["per_edge"] * m / (w["walk_len"] * n * math.log(n))))
+    stream = torch.cuda.current_stream()
+    ctx = Context(local, stream=stream.cuda_stream)
+    g = Graph.from_numpy(ctx, off, nbrs)
+    out = {"workload": w["label"], "n": n, "m": m, "sample_ratio_float": ratio, "graph_gen_s": gen_s}
+    sums = []
+    csr = None
+    for rep in range(2):
+        if csr is not None:
+            csr.free()
+        torch.cuda.synchronize()
+        t = time.time()
+        csr, st = generate_trunc_log_matrix_v2(ctx, g, w["seed"], walk_len=w["walk_len"], table_size=w["tablesz"],
+                                               sample_ratio=ratio)
+        torch.cuda.synchronize()
+        out["sparsify_s"] = time.time() - t
+        sums.append(csr_checksum(csr))
+    out["sparsify"] = {k: st[k] for k in ("samples_emitted", "distinct", "nnz_upper", "nnz", "capacity",
+                                          "ms_sample", "ms_trunclog", "ms_csr")}
+    out["csr_row_ptr_ok"] = sums[0][1]
+    out["deterministic"] = sums[0][0] == sums[1][0]
+    embs = {}
+    for prec in ("fp32", "bf16"):
+        torch.cuda.synchronize()
+        t = time.time()
+        emb, S, s2 = randsvd(ctx, csr, w["rank"], w["dim"], precision=prec, seed=SVD_SEED)
+        y, s3 = chebyshev_expansion(ctx, g, emb, w["dim"], order=w["order"], precision=prec)
+        pro, _ = get_embedding_dense(ctx, y, w["dim"])
+        torch.cuda.synchronize()
+        out["dense_s_" + prec] = time.time() - t
+        out["randsvd_ms_" + prec] = s2["ms_total"]
+        out["propagate_ms_" + prec] = s3["ms_total"]
+        embs[prec] = (emb, pro)
+        del y
+    csr.free()
+    e32, p32 = (x.double().cpu().numpy() for x in embs["fp32"])
+    e16, p16 = (x.double().cpu().numpy() for x in embs["bf16"])
+    out["bf16_vs_fp32_svd_procrustes"] = lo.procrustes_rel_error(e16, e32)
+    out["bf16_vs_fp32_final_procrustes"] = lo.procrustes_rel_error(p16, p32)
+    del e32, p32, e16, p16
+    if labels is not None:
+        emb = embs["bf16"][0]
+        del embs
+        rng = np.random.default_rng(w["seed"])
+        perm = rng.permutation(n)
+        tr = torch.from_numpy(perm[: n // 10]).cuda()
+        te = torch.from_numpy(perm[n // 10:]).cuda()
+        yl = torch.from_numpy(labels.astype(np.int64)).cuda()
+        mu = torch.tensor(0.2, device="cuda", requires_grad=True)
+        sp_ = torch.tensor(0.5, device="cuda", requires_grad=True)
+        W = torch.zeros(w["dim"], w["blocks"], device="cuda", requires_grad=True)
+        b = torch.zeros(w["blocks"], device="cuda", requires_grad=True)
+        opt = torch.optim.Adam([mu, sp_, W, b], lr=0.05)
+        hist = []
+        torch.cuda.synchronize()
+        t = time.time()
+        for step in range(w["adam_steps"] + 1):
+            y = ChebyshevPropagation(emb, mu, sp_, ctx, g, w["order"], "bf16")
+            z = y / y.norm(dim=1, keepdim=True).clamp_min(1e-12)
+            logits = z @ W + b
+            loss = torch.nn.functional.cross_entropy(logits[tr], yl[tr])
+            with torch.no_grad():
+                acc = (logits[te].argmax(1) == yl[te]).float().mean().item()
+            hist.append({"step": step, "loss": loss.item(), "test_acc": acc, "mu": mu.item(), "s": sp_.item()})
+            if step == w["adam_steps"]:
+                break
+            opt.zero_grad()
+            loss.backward()
+            opt.step()
+        torch.cuda.synchronize()
+        out["adam"] = {"seconds": time.time() - t, "trace": [hist[0], hist[len(hist) // 2], hist[-1]]}
+    print(json.dumps({"scale_run": args.workload, **out}))
+    g.free()
+    ctx.close()
+
+
 def accuracy(ctx, g, w, seed, off, nbrs):
     """Both forms against the FP64 oracle on this workload (minutes of host
     time): randomized SVD singular values, subspace angle and embedding
@@ -646,7 +778,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + sorted(SCALE_RUNS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy", action="store_true")
     ap.add_argument("--quick", action="store_true", help="BF16 form only, no e2e / CPU legs (for profiling)")
@@ -663,6 +795,8 @@ def main():
         barrier(ws)
         if args.micro:
             run_micro(args, local)
+        elif args.workload in SCALE_RUNS:
+            run_scale(args, local)
         else:
             run_ours(args, ws, rank, local)
     if ws > 1:
