@@ -21,6 +21,7 @@
 #include <string>
 
 #include "lne_internal.h"
+#include "lne_math.cuh"
 #include "radix.h"
 
 namespace lne {
@@ -58,11 +59,22 @@ __device__ __forceinline__ unsigned match_digit(unsigned d, bool valid, int dbit
   return m;
 }
 
+// The digit of a key: bits shift.. of the key itself (the CSR sort), or of
+// the key's pair-table slot hash64_2(key) & hmask (the insert partition).
+enum DigitMode : int { kDigitKey = 0, kDigitSlot = 1 };
+template <int MODE>
+__device__ __forceinline__ unsigned digit_of(unsigned long long key, int shift, unsigned long long mask,
+                                             unsigned long long hmask) {
+  if (MODE == kDigitSlot) return (unsigned)(((hash64_2(key) & hmask) >> shift) & mask);
+  return (unsigned)((key >> shift) & mask);
+}
+
 // Per-warp sub-histograms in shared memory (plain shared atomics: the
 // counting is issue-bound otherwise), summed per tile.
+template <int MODE>
 __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const unsigned long long* __restrict__ keys,
                                                                int64_t count, int shift, int dbits, int64_t ntiles,
-                                                               int64_t* __restrict__ hist) {
+                                                               int64_t* __restrict__ hist, unsigned long long hmask) {
   const int bins = 1 << dbits;
   __shared__ unsigned int h[kRadixWarps][kMaxBins];
   for (int i = threadIdx.x; i < kRadixWarps * kMaxBins; i += blockDim.x) (&h[0][0])[i] = 0;
@@ -73,7 +85,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const unsigned lon
 #pragma unroll 8
   for (int r = 0; r < kRadixItems; ++r) {
     const int64_t i = base + (int64_t)r * kRadixThreads + threadIdx.x;
-    if (i < count) atomicAdd(&my[(keys[i] >> shift) & mask], 1u);
+    if (i < count) atomicAdd(&my[digit_of<MODE>(keys[i], shift, mask, hmask)], 1u);
   }
   __syncthreads();
   for (int d = threadIdx.x; d < bins; d += blockDim.x) {
@@ -106,11 +118,12 @@ __device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned* wa
 // tile is first copied to shared memory with cp.async (48 KB in flight per
 // CTA, no registers held), ranked from there, reordered into a second
 // shared buffer and written out.
-template <bool FINAL>
+template <bool FINAL, int MODE, bool VALS>
 __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
     const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t count, int shift, int dbits,
     int64_t ntiles, const int64_t* __restrict__ offs, unsigned long long* __restrict__ okeys,
-    uint32_t* __restrict__ ovals, int32_t* __restrict__ ocol, float* __restrict__ oval, unsigned long long col_mask) {
+    uint32_t* __restrict__ ovals, int32_t* __restrict__ ocol, float* __restrict__ oval, unsigned long long col_mask,
+    unsigned long long hmask) {
   extern __shared__ __align__(16) unsigned char radix_smem[];
   unsigned long long* skey = reinterpret_cast<unsigned long long*>(radix_smem);
   uint32_t* sval = reinterpret_cast<uint32_t*>(radix_smem + sizeof(unsigned long long) * kRadixTile);
@@ -136,7 +149,7 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
         const int left = tcount - 2 * c;
         const uint32_t bytes = left >= 2 ? 16u : (left == 1 ? 8u : 0u);
         cp_async16(kdst + 16 * c, bytes ? (const void*)(keys + tbase + 2 * c) : (const void*)keys, bytes);
-      } else {
+      } else if (VALS) {
         const int cv = c - kRadixTile / 2;
         const int left = tcount - 4 * cv;
         const uint32_t bytes = left >= 4 ? 16u : (left > 0 ? 4u * left : 0u);
@@ -160,7 +173,7 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
     const int li = wofs + r * 32 + lane;
     const bool valid = li < tcount;
     const unsigned long long key = rkey[li];
-    const unsigned d = (unsigned)((key >> shift) & mask);
+    const unsigned d = digit_of<MODE>(key, shift, mask, hmask);
     const unsigned peers = match_digit(d, valid, dbits);
     const unsigned before = valid ? my[d] : 0u;
     __syncwarp();
@@ -198,10 +211,10 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
     const int li = wofs + r * 32 + lane;
     if (li < tcount) {
       const unsigned long long key = rkey[li];
-      const int d = (int)((key >> shift) & mask);
+      const int d = (int)digit_of<MODE>(key, shift, mask, hmask);
       const unsigned pos = my[d] + ((rk[r >> 1] >> ((r & 1) * 16)) & 0xffffu);
       skey[pos] = key;
-      sval[pos] = rval[li];
+      if (VALS) sval[pos] = rval[li];
     }
   }
   __syncthreads();
@@ -210,14 +223,14 @@ __global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
   // fall into runs of equal digits with consecutive global positions.
   for (int j = threadIdx.x; j < tcount; j += kRadixThreads) {
     const unsigned long long key = skey[j];
-    const int d = (int)((key >> shift) & mask);
+    const int d = (int)digit_of<MODE>(key, shift, mask, hmask);
     const int64_t pos = gstart[d] + (j - (int)tile_start[d]);
     if (FINAL) {
       ocol[pos] = (int32_t)(key & col_mask);
       oval[pos] = __uint_as_float(sval[j]);
     } else {
       okeys[pos] = key;
-      ovals[pos] = sval[j];
+      if (VALS) ovals[pos] = sval[j];
     }
   }
 }
@@ -250,20 +263,22 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
   int64_t* hist = (int64_t*)mem;
   int64_t* offs = (int64_t*)(mem + ((hist_bytes + 255) & ~(size_t)255));
   void* scan_tmp = mem + 2 * ((hist_bytes + 255) & ~(size_t)255);
-  cudaFuncSetAttribute(k_radix_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
-  cudaFuncSetAttribute(k_radix_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
+  cudaFuncSetAttribute(k_radix_scatter<true, kDigitKey, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kScatterSmem);
+  cudaFuncSetAttribute(k_radix_scatter<false, kDigitKey, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kScatterSmem);
   unsigned long long *src_k = keys, *dst_k = keys_tmp;
   uint32_t *src_v = vals, *dst_v = vals_tmp;
   for (int p = 0; p < passes; ++p) {
     const int shift = p * dbits;
-    k_radix_hist<<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist);
+    k_radix_hist<kDigitKey><<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist, 0);
     scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
     if (p == passes - 1) {
-      k_radix_scatter<true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
-          src_k, src_v, count, shift, dbits, ntiles, offs, nullptr, nullptr, out_col, out_val, col_mask);
+      k_radix_scatter<true, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, dbits, ntiles, offs, nullptr, nullptr, out_col, out_val, col_mask, 0);
     } else {
-      k_radix_scatter<false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
-          src_k, src_v, count, shift, dbits, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0);
+      k_radix_scatter<false, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, dbits, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0, 0);
       std::swap(src_k, dst_k);
       std::swap(src_v, dst_v);
     }
@@ -273,6 +288,44 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error(std::string("radix sort: kernel launch failed: ") + cudaGetErrorString(e));
+    return LNE_ERR_CUDA;
+  }
+  return LNE_OK;
+}
+
+int partition_by_slot(lne_ctx* ctx, const unsigned long long* keys, unsigned long long* out, int64_t count,
+                      int table_bits, int* launches) {
+  if (count <= 0) return LNE_OK;
+  const int dbits = table_bits < 8 ? (table_bits > 0 ? table_bits : 1) : 8;
+  const int shift = table_bits - dbits > 0 ? table_bits - dbits : 0;
+  const int bins = 1 << dbits;
+  const unsigned long long hmask = table_bits >= 64 ? ~0ULL : ((1ULL << table_bits) - 1);
+  const int64_t ntiles = (count + kRadixTile - 1) / kRadixTile;
+  if (ntiles > 0x7fffffffLL) {
+    set_error("partition: too many keys");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  const int64_t cells = (int64_t)bins * ntiles;
+  char* mem = nullptr;
+  const size_t hist_bytes = (sizeof(int64_t) * (size_t)(cells + 1) + 255) & ~(size_t)255;
+  int rc = dalloc(ctx, (void**)&mem, 2 * hist_bytes + scan_tmp_bytes(cells), "partition histograms");
+  if (rc) return rc;
+  int64_t* hist = (int64_t*)mem;
+  int64_t* offs = (int64_t*)(mem + hist_bytes);
+  void* scan_tmp = mem + 2 * hist_bytes;
+  cudaStream_t st = ctx->stream;
+  cudaFuncSetAttribute(k_radix_scatter<false, kDigitSlot, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kScatterSmem);
+  k_radix_hist<kDigitSlot><<<(unsigned)ntiles, kRadixThreads, 0, st>>>(keys, count, shift, dbits, ntiles, hist,
+                                                                       hmask);
+  scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
+  k_radix_scatter<false, kDigitSlot, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+      keys, nullptr, count, shift, dbits, ntiles, offs, out, nullptr, nullptr, nullptr, 0, hmask);
+  if (launches) *launches += 5;
+  dfree(ctx, mem);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("partition: kernel launch failed: ") + cudaGetErrorString(e));
     return LNE_ERR_CUDA;
   }
   return LNE_OK;

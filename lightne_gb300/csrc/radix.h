@@ -16,4 +16,10 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
                             uint32_t* vals_tmp, int64_t count, int key_bits, unsigned long long col_mask,
                             int32_t* out_col, float* out_val, int* launches);
 
+// Reorders `count` pair keys by the top min(8, table_bits) bits of their
+// pair-table slot (hash64_2(key) & (2^table_bits - 1)) into `out`, so that
+// consecutive inserts touch one slice of the table.  Stable.
+int partition_by_slot(lne_ctx* ctx, const unsigned long long* keys, unsigned long long* out, int64_t count,
+                      int table_bits, int* launches);
+
 }  // namespace lne

@@ -605,9 +605,12 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   const uint64_t buf_keys = want_keys < max_keys ? want_keys : max_keys;
   const int64_t edges_per_batch = (int64_t)std::max<uint64_t>(1, buf_keys / per_edge);
   unsigned long long* keys = nullptr;
+  unsigned long long* keys2 = nullptr;  // counts: the batch reordered by table slice
   double* wts = nullptr;
   if ((rc = S.get((void**)&keys, sizeof(unsigned long long) * buf_keys, "sample buffer"))) return rc;
   if (p->sample && (rc = S.get((void**)&wts, sizeof(double) * buf_keys, "sample weights"))) return rc;
+  if (!p->sample && (rc = S.get((void**)&keys2, sizeof(unsigned long long) * buf_keys, "partitioned samples")))
+    return rc;
   int launches_sample = 0;
   unsigned long long emitted_total = 0;
   for (int64_t eb = 0; eb < m_dir; eb += edges_per_batch) {
@@ -624,16 +627,24 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));
     LNE_CUDA_TRY(cudaStreamSynchronize(st));
     if (got > buf_keys) got = buf_keys;  // overflow is flagged and reported below
-    const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 32);
-    if (p->sample)
+    if (p->sample) {
+      const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 32);
       k_insert<true><<<iblocks, 256, 0, st>>>(keys, wts, got, table, cap - 1, ctx->d_flags);
-    else
-      k_insert<false><<<iblocks, 256, 0, st>>>(keys, wts, got, table, cap - 1, ctx->d_flags);
+    } else {
+      // Counts commute, so the batch is first grouped by the top 8 bits of
+      // its table slot: the inserts then sweep the table one slice (1/256
+      // of it) at a time, and a slice's slots stay in L2 while its atomics
+      // land.  A smaller grid keeps the warps within a slice or two.
+      if ((rc = partition_by_slot(ctx, keys, keys2, (int64_t)got, (int)bits, &launches_sample))) return rc;
+      const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 8);
+      k_insert<false><<<iblocks, 256, 0, st>>>(keys2, wts, got, table, cap - 1, ctx->d_flags);
+    }
     emitted_total += got;
     launches_sample += 2;
   }
   LNE_CUDA_TRY(cudaGetLastError());
   S.release(keys);
+  if (keys2) S.release(keys2);
   if (wts) S.release(wts);
   cudaEventRecord(ev.e[1], st);
 
