@@ -92,6 +92,27 @@ bool read_adjacency_graph(const std::string& path, std::vector<int64_t>& off, st
   buf[got] = '\0';
   const char* p = buf.data();
   const char* end = p + got;
+  // Binary AdjacencyGraph ("LNEADJ01", int64 n, int64 m, int64 offsets[n + 1],
+  // int32 targets[m], little endian), written by lightne_gb300.x2adj and
+  // graphs.write_adjacency_binary: the same arrays without text parsing.
+  if (got >= 24 && memcmp(p, "LNEADJ01", 8) == 0) {
+    int64_t n = 0, m = 0;
+    memcpy(&n, p + 8, 8);
+    memcpy(&m, p + 16, 8);
+    if (n < 0 || m < 0 || (uint64_t)got != 24 + 8 * (uint64_t)(n + 1) + 4 * (uint64_t)m) {
+      err = path + ": bad binary AdjacencyGraph size";
+      return false;
+    }
+    off.resize((size_t)n + 1);
+    nbrs.resize((size_t)m);
+    memcpy(off.data(), p + 24, 8 * (size_t)(n + 1));
+    memcpy(nbrs.data(), p + 24 + 8 * (size_t)(n + 1), 4 * (size_t)m);
+    if (off[0] != 0 || off[n] != m) {
+      err = path + ": binary AdjacencyGraph offsets do not span the targets";
+      return false;
+    }
+    return true;
+  }
   auto skip = [&]() { while (p < end && (*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r')) ++p; };
   auto next_u64 = [&](uint64_t& v) -> bool {
     skip();

@@ -198,6 +198,33 @@ def read_adjacency_graph(path: str):
     return off, arr[n:].astype(np.int32)
 
 
+_ADJ_MAGIC = b"LNEADJ01"
+
+
+def write_adjacency_binary(path: str, off: np.ndarray, nbrs: np.ndarray) -> None:
+    """Binary AdjacencyGraph, read by the LightNE command line without text
+    parsing: magic, int64 n, int64 m, int64 offsets[n+1], int32 targets[m]
+    (little endian)."""
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    with open(path, "wb") as f:
+        f.write(_ADJ_MAGIC)
+        f.write(struct.pack("<qq", off.size - 1, int(nbrs.size)))
+        f.write(off.astype("<i8").tobytes())
+        f.write(np.ascontiguousarray(nbrs, dtype="<i4").tobytes())
+
+
+def read_adjacency_binary(path: str):
+    with open(path, "rb") as f:
+        if f.read(8) != _ADJ_MAGIC:
+            raise ValueError("%s: not an LNEADJ01 file" % path)
+        n, m = struct.unpack("<qq", f.read(16))
+        off = np.frombuffer(f.read(8 * (n + 1)), dtype="<i8").astype(np.int64)
+        nbrs = np.frombuffer(f.read(4 * m), dtype="<i4").astype(np.int32)
+    if off[0] != 0 or off[-1] != m:
+        raise ValueError("%s: offsets do not span the targets" % path)
+    return off, nbrs
+
+
 _CSR_MAGIC = b"LNECSR01"
 
 

@@ -59,3 +59,25 @@ def test_cli_table_full_and_bad_input():
         open(bad, "w").write("NotAGraph\n1\n0\n0\n")
         r = subprocess.run([EXE, "-s", bad], capture_output=True, text=True, timeout=60)
         assert r.returncode != 0 and "AdjacencyGraph" in r.stderr
+
+
+def test_cli_binary_input_matches_text():
+    """The binary AdjacencyGraph (lightne_gb300.x2adj --binary) gives the same
+    run as the text file."""
+    off, nbrs = graphs.chung_lu(1500, 9000, 2.1, seed=33)
+    outs = []
+    with tempfile.TemporaryDirectory() as td:
+        for kind in ("text", "binary"):
+            gpath = os.path.join(td, "g." + kind)
+            if kind == "text":
+                graphs.write_adjacency_graph(gpath, off, nbrs)
+            else:
+                graphs.write_adjacency_binary(gpath, off, nbrs)
+            ne = os.path.join(td, kind + ".ne")
+            r = subprocess.run([EXE, "-rounds", "1", "-s", "-ne_out", ne, "-rank", "24", "-dim", "16",
+                                "-tablesz", "1000000", "-seed", "5", gpath], capture_output=True, text=True,
+                               timeout=300)
+            assert r.returncode == 0, r.stderr
+            assert "### n: 1500" in r.stdout
+            outs.append(np.fromfile(ne, dtype=np.float32))
+    assert np.array_equal(outs[0], outs[1])
