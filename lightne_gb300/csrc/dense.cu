@@ -398,7 +398,9 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict
                                                        int max_sweeps, int* __restrict__ sweeps_out) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;  // the grid is one cluster
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // pairs go to the CTAs round-robin (pair pk -> CTA pk % size), so that
+  // every SM's FP64 units share the step's work
+  const int gw = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
   const int rp = (r + 1) & ~1;  // even number of players (index r is a dummy when r is odd)
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
@@ -478,7 +480,7 @@ __device__ __forceinline__ void dsmem_st(uint32_t a, double v) {
 // memory (r <= 32 * kJacobiPer).
 __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __restrict__ Wc, int* __restrict__ rotated,
                                                              int max_sweeps, int* __restrict__ sweeps_out) {
-  extern __shared__ double jcols[];  // slot s: column s * csize + rank
+  extern __shared__ double jcols[];  // slot s: column s * csize + rank; then the slots' squared norms
   __shared__ int rot_flag[kJacobiMaxSweeps];  // this CTA rotated some pair in sweep k
   const int lane = threadIdx.x & 31;
   for (int k = threadIdx.x; k < kJacobiMaxSweeps; k += blockDim.x) rot_flag[k] = 0;
@@ -491,14 +493,28 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
       for (int i = threadIdx.x; i < r; i += blockDim.x) jcols[(int64_t)s * r + i] = Wc[(int64_t)c * r + i];
   }
   cluster_barrier();
+  double* cnorm = jcols + (int64_t)nslots * r;
   const uint32_t base = (uint32_t)__cvta_generic_to_shared(jcols);
+  const uint32_t nbase = (uint32_t)__cvta_generic_to_shared(cnorm);
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // pairs go to the CTAs round-robin (pair pk -> CTA pk % size), so that
+  // every SM's FP64 units share the step's work
+  const int gw = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
   const int rp = (r + 1) & ~1;
   const int m = rp - 1;
   const int cshift = __ffs(csize) - 1;  // csize is a power of two
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
+    // squared column norms, fresh every sweep; within the sweep each
+    // rotation updates the two norms it changes (only x.y needs a dot)
+    for (int sl = (int)(threadIdx.x >> 5); sl < nslots; sl += (int)(blockDim.x >> 5)) {
+      double a = 0.0;
+      const double* col = jcols + (int64_t)sl * r;
+      for (int i = lane; i < r; i += 32) a = fma(col[i], col[i], a);
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) cnorm[sl] = a;
+    }
+    cluster_barrier();
     for (int s = 0; s < m; ++s) {
       for (int pk = gw; pk < rp / 2; pk += nwarps) {
         // the round-robin pairs of step s: (s + pk, s - pk) mod m, and (m, s)
@@ -516,6 +532,9 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
         if (p > q) { const int t = p; p = q; q = t; }
         const uint32_t ap = dsmem_map(base + (uint32_t)((p >> cshift) * r) * 8u, (uint32_t)(p & (csize - 1)));
         const uint32_t aq = dsmem_map(base + (uint32_t)((q >> cshift) * r) * 8u, (uint32_t)(q & (csize - 1)));
+        const uint32_t np_ = dsmem_map(nbase + (uint32_t)(p >> cshift) * 8u, (uint32_t)(p & (csize - 1)));
+        const uint32_t nq_ = dsmem_map(nbase + (uint32_t)(q >> cshift) * 8u, (uint32_t)(q & (csize - 1)));
+        const double a = dsmem_ld(np_), b = dsmem_ld(nq_);
         double x[kJacobiPer], y[kJacobiPer];
 #pragma unroll
         for (int k = 0; k < kJacobiPer; ++k) {
@@ -523,20 +542,11 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
           x[k] = i < r ? dsmem_ld(ap + 8u * i) : 0.0;
           y[k] = i < r ? dsmem_ld(aq + 8u * i) : 0.0;
         }
-        double a = 0.0, b = 0.0, g = 0.0;
+        double g = 0.0;
 #pragma unroll
-        for (int k = 0; k < kJacobiPer; ++k) {
-          if (lane + 32 * k < r) {
-            a = fma(x[k], x[k], a);
-            b = fma(y[k], y[k], b);
-            g = fma(x[k], y[k], g);
-          }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-          a += __shfl_xor_sync(0xffffffffu, a, o);
-          b += __shfl_xor_sync(0xffffffffu, b, o);
-          g += __shfl_xor_sync(0xffffffffu, g, o);
-        }
+        for (int k = 0; k < kJacobiPer; ++k)
+          if (lane + 32 * k < r) g = fma(x[k], y[k], g);
+        for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
         // |g| > 1e-15 sqrt(ab), without the square root
         if (g != 0.0 && g * g > 1e-30 * (a * b)) {
           // Rotation angle in FP32 (the FP64 units are scarce on this part;
@@ -562,7 +572,12 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
               dsmem_st(aq + 8u * i, sn * x[k] + c * y[k]);
             }
           }
-          if (lane == 0) rot_flag[sweep] = 1;
+          if (lane == 0) {
+            rot_flag[sweep] = 1;
+            const double cc = c * c, ss = sn * sn, cs2 = 2.0 * c * sn * g;
+            dsmem_st(np_, fmax(fma(cc, a, fma(ss, b, -cs2)), 0.0));
+            dsmem_st(nq_, fmax(fma(ss, a, fma(cc, b, cs2)), 0.0));
+          }
         }
       }
       cluster_barrier();
@@ -638,7 +653,7 @@ int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps
       continue;
     }
     cfg.gridDim = dim3(cl, 1, 1);
-    cfg.dynamicSmemBytes = dsmem ? sizeof(double) * (size_t)((r + cl - 1) / cl) * r : 0;
+    cfg.dynamicSmemBytes = dsmem ? sizeof(double) * (size_t)((r + cl - 1) / cl) * (r + 1) : 0;
     attr[0].val.clusterDim.x = cl;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
