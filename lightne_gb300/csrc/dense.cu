@@ -330,7 +330,172 @@ __global__ void __launch_bounds__(1024) k_chol_inv_smem(const double* __restrict
   if (tid == 0) *status = 0;
 }
 
+// Thread-block cluster primitives: barrier, rank, distributed shared memory.
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t dsmem_map(uint32_t saddr, uint32_t rank) {
+  uint32_t a;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(saddr), "r"(rank));
+  return a;
+}
+__device__ __forceinline__ double dsmem_ld(uint32_t a) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ int dsmem_ld32(uint32_t a) {
+  int v;
+  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void dsmem_st(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+
+// The same factorisation on one thread-block cluster (16 CTAs where the
+// device allows that size, else 8), r <= kCholClusterMax: column j in CTA
+// j % size.  Step k: the owner of column k takes the pivot and scales the
+// column, a cluster barrier publishes it, every CTA copies it (distributed
+// shared memory) and updates its own later columns, element by element in
+// the same operations and order as k_cholesky.  Then every CTA gathers L and
+// the cluster's warps solve L x = e_j for their columns j (each entry a
+// lane-parallel dot product), writing row j of W = L^-T.
+constexpr int kCholClusterMax = 144;
+
+__global__ void __launch_bounds__(256) k_chol_inv_cluster(const double* __restrict__ G, int r, double shift,
+                                                          float* __restrict__ W, int* __restrict__ status) {
+  extern __shared__ double chs[];
+  __shared__ int bad;
+  const int csize = gridDim.x;
+  const int rank = (int)cluster_rank();
+  const int nslots = (r + csize - 1) / csize;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  double* col = chs;                          // [nslots][r]: my columns
+  double* colk = col + (size_t)nslots * r;    // [r]: column k of this step
+  double* Lf = colk + r;                      // [r][r]: all of L (inverse phase)
+  double* xw = Lf + (size_t)r * r;            // [nw][r]: a warp's solution column
+  for (int s = 0; s < nslots; ++s) {
+    const int j = s * csize + rank;
+    if (j < r)
+      for (int i = tid; i < r; i += blockDim.x) col[(size_t)s * r + i] = G[(size_t)j * r + i] + (i == j ? shift : 0.0);
+  }
+  if (tid == 0) bad = 0;
+  const uint32_t col_s = (uint32_t)__cvta_generic_to_shared(col);
+  const uint32_t bad_s = (uint32_t)__cvta_generic_to_shared(&bad);
+  cluster_barrier();
+  bool failed = false;
+  for (int k = 0; k < r; ++k) {
+    const int own = k % csize, ks = k / csize;
+    if (rank == own && warp == 0) {
+      double* c = col + (size_t)ks * r;
+      const double d = c[k];
+      const bool ok = d > 0.0 && isfinite(d);
+      const double piv = ok ? sqrt(d) : 1.0;
+      for (int i = k + 1 + lane; i < r; i += 32) c[i] /= piv;
+      __syncwarp();
+      if (lane == 0) {
+        c[k] = piv;
+        if (!ok) bad = 1;
+      }
+    }
+    cluster_barrier();
+    if (dsmem_ld32(dsmem_map(bad_s, (uint32_t)own))) {
+      failed = true;
+      break;
+    }
+    const uint32_t src = dsmem_map(col_s + (uint32_t)(ks * r) * 8u, (uint32_t)own);
+    for (int i = k + tid; i < r; i += blockDim.x) colk[i] = dsmem_ld(src + 8u * (uint32_t)i);
+    __syncthreads();
+    for (int s = warp; s < nslots; s += nw) {
+      const int j = s * csize + rank;
+      if (j > k && j < r) {
+        const double ljk = colk[j];
+        double* c = col + (size_t)s * r;
+        for (int i = j + lane; i < r; i += 32) c[i] -= colk[i] * ljk;
+      }
+    }
+    __syncthreads();
+  }
+  cluster_barrier();
+  if (!failed) {
+    // L row-major in every CTA: Lf[i][k] = column k, row i (i >= k)
+    for (int k = warp; k < r; k += nw) {
+      const uint32_t src = dsmem_map(col_s + (uint32_t)((k / csize) * r) * 8u, (uint32_t)(k % csize));
+      for (int i = k + lane; i < r; i += 32) Lf[(size_t)i * r + k] = dsmem_ld(src + 8u * (uint32_t)i);
+    }
+    __syncthreads();
+    double* x = xw + (size_t)warp * r;
+    for (int j = warp * csize + rank; j < r; j += nw * csize) {
+      if (lane == 0) x[j] = 1.0 / Lf[(size_t)j * r + j];
+      __syncwarp();
+      for (int i = j + 1; i < r; ++i) {
+        double sacc = 0.0;
+        for (int k = j + lane; k < i; k += 32) sacc = fma(Lf[(size_t)i * r + k], x[k], sacc);
+        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+        if (lane == 0) x[i] = -sacc / Lf[(size_t)i * r + i];
+        __syncwarp();
+      }
+      for (int i = lane; i < r; i += 32) W[(size_t)j * r + i] = i < j ? 0.0f : (float)x[i];
+      __syncwarp();
+    }
+  }
+  if (rank == 0 && tid == 0) *status = failed ? 1 : 0;
+  cluster_barrier();  // no CTA leaves while another may still read its shared memory
+}
+
+static size_t chol_cluster_smem(int r, int csize) {
+  const size_t nslots = (size_t)(r + csize - 1) / csize;
+  return sizeof(double) * (nslots * r + r + (size_t)r * r + 8 * (size_t)r);
+}
+
+// Launches k_chol_inv_cluster on a 16- or 8-CTA cluster; false if neither
+// size can be launched.
+static bool chol_inv_cluster_launch(lne_ctx* ctx, const double* G, int r, double shift, float* W, int* status) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.stream = ctx->stream;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  for (int cl : {16, 8}) {
+    const size_t smem = chol_cluster_smem(r, cl);
+    if (smem > ctx->smem_optin) continue;
+    if (cl == 16 &&
+        cudaFuncSetAttribute(k_chol_inv_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (cudaFuncSetAttribute(k_chol_inv_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cfg.gridDim = dim3(cl, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_chol_inv_cluster, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      continue;
+    }
+    if (cudaLaunchKernelEx(&cfg, k_chol_inv_cluster, G, r, shift, W, status) == cudaSuccess) return true;
+    cudaGetLastError();
+  }
+  return false;
+}
+
 int cholesky_inv_launches(lne_ctx* ctx, int r) {
+  if (r <= kCholClusterMax) return 1;
   return (r <= kCholSmemMax && sizeof(double) * ((size_t)r * r + r) <= ctx->smem_optin) ? 1 : 2;
 }
 
@@ -341,7 +506,9 @@ int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W) {
   if ((rc = dalloc(ctx, (void**)&X, sizeof(double) * r * r + 16, "triangular inverse"))) return rc;
   status = (int*)(X + (int64_t)r * r);
   const size_t csmem = sizeof(double) * ((size_t)r * r + r);
-  if (r <= kCholSmemMax && csmem <= ctx->smem_optin) {
+  if (r <= kCholClusterMax && chol_inv_cluster_launch(ctx, G, r, shift, W, status)) {
+    // done on the cluster
+  } else if (r <= kCholSmemMax && csmem <= ctx->smem_optin) {
     cudaFuncSetAttribute(k_chol_inv_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
     k_chol_inv_smem<<<1, 1024, csmem, ctx->stream>>>(G, r, shift, W, status);
   } else {
@@ -388,10 +555,6 @@ __global__ void k_jacobi_init(const double* __restrict__ C, int r, double* __res
     Wc[(int64_t)j * r + i] = C[t];
   }
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < max_sweeps; t += gridDim.x * blockDim.x) rotated[t] = 0;
-}
-
-__device__ __forceinline__ void cluster_barrier() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
 __global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict__ Wc, int* __restrict__ rotated,
@@ -451,30 +614,6 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict
 
 constexpr int kJacobiPer = 5;  // column elements per lane held in registers (r <= 160)
 constexpr int kJacobiMaxSweeps = 60;
-
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ uint32_t dsmem_map(uint32_t saddr, uint32_t rank) {
-  uint32_t a;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(saddr), "r"(rank));
-  return a;
-}
-__device__ __forceinline__ double dsmem_ld(uint32_t a) {
-  double v;
-  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
-  return v;
-}
-__device__ __forceinline__ int dsmem_ld32(uint32_t a) {
-  int v;
-  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
-  return v;
-}
-__device__ __forceinline__ void dsmem_st(uint32_t a, double v) {
-  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
-}
 
 // Same sweeps, same arithmetic, with the columns in distributed shared
 // memory (r <= 32 * kJacobiPer).
