@@ -263,9 +263,10 @@ def time_form(ctx, g, w, precision, seed, steps, warmup, stream, flush):
 
 
 # lne_dense_embed: CholeskyQR3 (3 x (Gram + reduction, Cholesky/inverse,
-# update GEMM) + one trace), Gram, Jacobi (init, sweeps, finish), column
+# update GEMM) + one trace), Gram, Jacobi (FP32 preconditioning, two
+# Newton-Schulz steps of two launches each, FP64 sweeps, finish), column
 # scaling, GEMM, row normalisation
-DENSE_EMBED_LAUNCHES = 3 * 4 + 1 + 2 + 3 + 1 + 1 + 1
+DENSE_EMBED_LAUNCHES = 3 * 4 + 1 + 2 + 7 + 1 + 1 + 1
 
 
 def launches_of(st):

@@ -23,6 +23,8 @@
  *                       (LightNE/SpectralPropagation.h:16-43)
  *   lne_spmm            mkl_sparse_s_mm on a CSR (the SpMM of
  *                       LightNE/mklredsvd/mklredsvd.cc:235-245)
+ *   lne_core_svd        LAPACKE_gesvd(jobu 'S', jobvt 'N') of the rank x rank
+ *                       core C = Z^T B (LightNE/mklredsvd/mklredsvd.cc:357-371)
  */
 #ifndef LIGHTNE_GB300_H
 #define LIGHTNE_GB300_H
@@ -159,9 +161,11 @@ typedef struct lne_randsvd_params {
 
 typedef struct lne_randsvd_stats {
   float ms_sketch, ms_qr, ms_spmm2, ms_core, ms_total; /* device time per stage */
-  int32_t jacobi_sweeps;
+  int32_t jacobi_sweeps;        /* FP64 sweeps of the core SVD */
   int32_t kernel_launches;
   double spmm_nnz;
+  int32_t jacobi_sweeps_fp32;   /* FP32 preconditioning sweeps before them (0: none) */
+  int32_t reserved;
 } lne_randsvd_stats;
 
 /*
@@ -259,6 +263,19 @@ int lne_propagate_adjoint(lne_ctx* ctx, const lne_graph* g, const lne_propagate_
  * h_S (host float[dim]) may be NULL.
  */
 int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_t dim, float* d_emb, float* h_S);
+
+/*
+ * SVD of a small dense matrix, the core step of the randomized SVD:
+ * d_C (device r x r FP64, row-major, not modified) = U diag(S) V^T with
+ * d_U (device r x r FP64, row-major, column j = left singular vector j) and
+ * d_S (device r FP64), singular values descending; V is not formed, as
+ * LAPACKE_gesvd(jobu 'S', jobvt 'N') at LightNE/mklredsvd/mklredsvd.cc:357-371
+ * (which the reference runs in FP32).  One-sided Jacobi in FP64 (r <= 160:
+ * FP32 sweeps first, then FP64 sweeps from the FP64-orthogonalised FP32
+ * basis); r <= 1024.  h_sweeps (host int[2], may be NULL): FP64 sweeps,
+ * FP32 sweeps.
+ */
+int lne_core_svd(lne_ctx* ctx, const double* d_C, int32_t r, double* d_U, double* d_S, int32_t* h_sweeps);
 
 /*
  * Dense building blocks of the randomized SVD (device pointers, FP32 in):

@@ -99,6 +99,8 @@ class RandsvdStats(ctypes.Structure):
         ("jacobi_sweeps", ctypes.c_int32),
         ("kernel_launches", ctypes.c_int32),
         ("spmm_nnz", ctypes.c_double),
+        ("jacobi_sweeps_fp32", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -160,6 +162,7 @@ SIGNATURES = {
                                              ctypes.POINTER(PropagateStats)]),
     "lne_chebyshev_coefficients": (ctypes.c_int, [ctypes.c_int32, ctypes.c_double, VP]),
     "lne_dense_embed": (ctypes.c_int, [VP, VP, I64, I64, VP, VP]),
+    "lne_core_svd": (ctypes.c_int, [VP, VP, ctypes.c_int32, VP, VP, VP]),
     "lne_gram": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, I64, VP]),
     "lne_gemm_tall": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, VP, I64]),
     "lne_gram_noalloc": (ctypes.c_int, [VP, VP, I64, I64, VP, I64, I64, I64, VP]),

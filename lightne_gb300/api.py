@@ -250,6 +250,24 @@ def get_embedding_dense(ctx: Context, x, dim: int):
     return emb, S
 
 
+def core_svd(ctx: Context, C):
+    """SVD of a small dense r x r matrix on the device, the core step of the
+    randomized SVD (LAPACKE_gesvd at LightNE/mklredsvd/mklredsvd.cc:357-371):
+    returns (U torch float64 r x r, S torch float64 r, (fp64 sweeps, fp32
+    sweeps)); C = U diag(S) V^T, S descending."""
+    torch = _torch()
+    dc = torch.as_tensor(C, dtype=torch.float64).to(f"cuda:{ctx.device}").contiguous()
+    r = dc.shape[0]
+    if dc.dim() != 2 or dc.shape[1] != r:
+        raise ValueError("core_svd: C must be square")
+    U = torch.empty(r, r, dtype=torch.float64, device=dc.device)
+    S = torch.empty(r, dtype=torch.float64, device=dc.device)
+    sw = np.zeros(2, dtype=np.int32)
+    check(_lib.load().lne_core_svd(ctx.handle, ctypes.c_void_p(dc.data_ptr()), r, ctypes.c_void_p(U.data_ptr()),
+                                   ctypes.c_void_p(S.data_ptr()), _ptr(sw)))
+    return U, S, (int(sw[0]), int(sw[1]))
+
+
 def chebyshev_coefficients(order: int, s: float = 0.5) -> np.ndarray:
     out = np.zeros(max(order, 2), dtype=np.float32)
     check(_lib.load().lne_chebyshev_coefficients(order, s, _ptr(out)))

@@ -565,6 +565,8 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict
   // every SM's FP64 units share the step's work
   const int gw = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
   const int rp = (r + 1) & ~1;  // even number of players (index r is a dummy when r is odd)
+  // below sqrt(r) eps a rotation only chases the rounding of the dot product
+  const double tol = fmax(1e-15, 2.220446049250313e-16 * sqrt((double)r));
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     for (int s = 0; s < rp - 1; ++s) {
@@ -593,7 +595,7 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict
           b += __shfl_xor_sync(0xffffffffu, b, o);
           g += __shfl_xor_sync(0xffffffffu, g, o);
         }
-        if (fabs(g) > 1e-15 * sqrt(a * b) && g != 0.0) {
+        if (fabs(g) > tol * sqrt(a * b) && g != 0.0) {
           const double zeta = (b - a) / (2.0 * g);
           const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
           const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
@@ -626,12 +628,35 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
   const int csize = gridDim.x;  // the grid is one cluster (8 or 16 CTAs)
   const uint32_t rank = cluster_rank();
   const int nslots = (r + csize - 1) / csize;
+  __shared__ double wsum[8], csum;  // this CTA's sum of squares (rotations keep the total)
+  double sq = 0.0;
   for (int s = 0; s < nslots; ++s) {
     const int c = s * csize + (int)rank;
     if (c < r)
-      for (int i = threadIdx.x; i < r; i += blockDim.x) jcols[(int64_t)s * r + i] = Wc[(int64_t)c * r + i];
+      for (int i = threadIdx.x; i < r; i += blockDim.x) {
+        const double v = Wc[(int64_t)c * r + i];
+        jcols[(int64_t)s * r + i] = v;
+        sq = fma(v, v, sq);
+      }
+  }
+  for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  if (lane == 0) wsum[threadIdx.x >> 5] = sq;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+    csum = t;
   }
   cluster_barrier();
+  // A column below about r eps of the Frobenius norm is rounding noise of
+  // its partners (each rotation leaves eps |x| in it): it is not rotated,
+  // or noise pairs would rotate forever on a rank-deficient matrix.
+  double fro2 = 0.0;
+  {
+    const uint32_t ca = (uint32_t)__cvta_generic_to_shared(&csum);
+    for (int c = 0; c < csize; ++c) fro2 += dsmem_ld(dsmem_map(ca, (uint32_t)c));
+  }
+  const double tiny = fro2 * 1.9721522630525295e-31 * (double)r * (double)r;  // fro2 (2 r 2^-52)^2
   double* cnorm = jcols + (int64_t)nslots * r;
   const uint32_t base = (uint32_t)__cvta_generic_to_shared(jcols);
   const uint32_t nbase = (uint32_t)__cvta_generic_to_shared(cnorm);
@@ -642,6 +667,7 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
   const int rp = (r + 1) & ~1;
   const int m = rp - 1;
   const int cshift = __ffs(csize) - 1;  // csize is a power of two
+  const double tol2 = fmax(1e-30, 4.930380657631324e-32 * r);  // (2^-52)^2 r
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     // squared column norms, fresh every sweep; within the sweep each
@@ -686,8 +712,10 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
         for (int k = 0; k < kJacobiPer; ++k)
           if (lane + 32 * k < r) g = fma(x[k], y[k], g);
         for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
-        // |g| > 1e-15 sqrt(ab), without the square root
-        if (g != 0.0 && g * g > 1e-30 * (a * b)) {
+        // |g| > tol sqrt(ab), without the square root; tol = max(1e-15,
+        // sqrt(r) eps): the rounding of a length-r FP64 dot product, below
+        // which a rotation would only chase noise
+        if (g != 0.0 && a > tiny && b > tiny && g * g > tol2 * (a * b)) {
           // Rotation angle in FP32 (the FP64 units are scarce on this part;
           // an angle accurate to 2^-24 leaves a residual of that size in
           // g, which the next sweep removes), then (c, s) made orthogonal
@@ -736,6 +764,213 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
   if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep + 1;
 }
 
+// FP32 preconditioning of the FP64 sweeps (r <= 32 * kJacobiPer, one CTA):
+// one-sided Jacobi on an FP32 copy of C (scaled to unit largest entry), the
+// rotations accumulated in V from I, until no pair has |x.y| > kJacobiTol32
+// |x| |y| (or kJacobi32MaxSweeps).  FP32 runs at many times the FP64 rate
+// on this part, so these early sweeps are cheap; the FP64 sweeps then start
+// from W = C V', V' = V re-orthogonalised in FP64 (k_jacobi_pm,
+// k_jacobi_ns), whose columns are orthogonal to about the FP32 tolerance,
+// and finish in a few sweeps.  The result is the same FP64-accurate
+// one-sided Jacobi SVD: only the starting basis of the FP64 sweeps differs.
+//
+// Layout: columns of W and V at a stride of rq = r rounded up to 32 floats
+// (zero padded).  A pair is handled by 8 lanes (4 pairs per warp), lane l
+// holding the float4 vectors l, l + 8, ... of the two columns, so that one
+// 8-lane group reads 128 contiguous bytes per load.
+constexpr float kJacobiTol32 = 4e-6f;
+constexpr int kJacobi32MaxSweeps = 30;
+constexpr int kJacobi32Vec = 5;  // float4 vectors per lane: r <= 8 * 4 * 5 = 160
+
+__host__ __device__ inline int jacobi32_stride(int r) { return (r + 31) & ~31; }
+
+__global__ void __launch_bounds__(1024) k_jacobi_precond32(const double* __restrict__ C, int r,
+                                                           double* __restrict__ Vout, int* __restrict__ sweeps_out) {
+  extern __shared__ float4 jw4[];
+  const int rq = jacobi32_stride(r);
+  float* W = reinterpret_cast<float*>(jw4);  // column j at j * rq
+  float* V = W + (size_t)r * rq;
+  __shared__ double red[32];
+  __shared__ int rot_flag[kJacobi32MaxSweeps];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int gl = lane & 7, grp = lane >> 3;
+  for (int k = tid; k < kJacobi32MaxSweeps; k += blockDim.x) rot_flag[k] = 0;
+  double mx = 0.0;
+  for (int t = tid; t < r * r; t += blockDim.x) mx = fmax(mx, fabs(C[t]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) red[warp] = mx;
+  __syncthreads();
+  mx = 0.0;
+  for (int w = 0; w < nw; ++w) mx = fmax(mx, red[w]);
+  const double sc = (mx > 0.0 && isfinite(mx)) ? 1.0 / mx : 1.0;
+  double sq = 0.0;
+  for (int t = tid; t < r * rq; t += blockDim.x) {
+    const int j = t / rq, i = t - (t / rq) * rq;  // column j, row i
+    const float w = i < r ? (float)(C[(int64_t)i * r + j] * sc) : 0.0f;
+    W[t] = w;
+    V[t] = i == j ? 1.0f : 0.0f;
+    sq = fma((double)w, (double)w, sq);
+  }
+  for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  __syncthreads();  // every thread has read red[] above
+  if (lane == 0) red[warp] = sq;
+  __syncthreads();
+  double fro2 = 0.0;
+  for (int w = 0; w < nw; ++w) fro2 += red[w];
+  // columns below about r eps32 of the Frobenius norm are left to the FP64
+  // sweeps (in FP32 they are rounding noise of their partners)
+  const float tiny = (float)(fro2 * 1.4210854715202004e-14 * (double)r * (double)r);  // fro2 (2 r 2^-24)^2
+  const int rp = (r + 1) & ~1;
+  const int m = rp - 1;
+  const int nv = rq / 32;  // float4 vectors per lane actually used
+  const float tol2 = kJacobiTol32 * kJacobiTol32;
+  int sweep = 0;
+  for (; sweep < kJacobi32MaxSweeps; ++sweep) {
+    for (int s = 0; s < m; ++s) {
+      for (int pk0 = warp * 4; pk0 < rp / 2; pk0 += nw * 4) {
+        const int pk = pk0 + grp;
+        int p = 0, q = 0;
+        bool live = pk < rp / 2;
+        if (live) {
+          if (pk == 0) {
+            p = m;
+            q = s;
+          } else {
+            p = s + pk;
+            if (p >= m) p -= m;
+            q = s - pk;
+            if (q < 0) q += m;
+          }
+          if (p >= r || q >= r) live = false;
+          if (p > q) { const int t = p; p = q; q = t; }
+        }
+        float4 x[kJacobi32Vec], y[kJacobi32Vec];
+        float a = 0.f, b = 0.f, g = 0.f;
+        const float4* wp = reinterpret_cast<const float4*>(W + (size_t)p * rq);
+        const float4* wq = reinterpret_cast<const float4*>(W + (size_t)q * rq);
+#pragma unroll
+        for (int k = 0; k < kJacobi32Vec; ++k) {
+          if (live && k < nv) {
+            x[k] = wp[gl + 8 * k];
+            y[k] = wq[gl + 8 * k];
+          } else {
+            x[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            y[k] = x[k];
+          }
+          a = fmaf(x[k].x, x[k].x, fmaf(x[k].y, x[k].y, fmaf(x[k].z, x[k].z, fmaf(x[k].w, x[k].w, a))));
+          b = fmaf(y[k].x, y[k].x, fmaf(y[k].y, y[k].y, fmaf(y[k].z, y[k].z, fmaf(y[k].w, y[k].w, b))));
+          g = fmaf(x[k].x, y[k].x, fmaf(x[k].y, y[k].y, fmaf(x[k].z, y[k].z, fmaf(x[k].w, y[k].w, g))));
+        }
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+          a += __shfl_xor_sync(0xffffffffu, a, o);
+          b += __shfl_xor_sync(0xffffffffu, b, o);
+          g += __shfl_xor_sync(0xffffffffu, g, o);
+        }
+        if (live && g != 0.f && a > tiny && b > tiny && g * g > tol2 * (a * b)) {
+          // the rotation need not be exact here: V is re-orthogonalised
+          // in FP64 before the FP64 sweeps
+          const float zeta = __fdividef(b - a, 2.0f * g);
+          const float az = fabsf(zeta);
+          const float t = az < 1e18f ? copysignf(1.0f, zeta) / (az + sqrtf(fmaf(az, az, 1.0f))) : 0.5f / zeta;
+          const float c = rsqrtf(fmaf(t, t, 1.0f)), sn = c * t;
+          float4* vp = reinterpret_cast<float4*>(V + (size_t)p * rq);
+          float4* vq = reinterpret_cast<float4*>(V + (size_t)q * rq);
+          float4* wpw = reinterpret_cast<float4*>(W + (size_t)p * rq);
+          float4* wqw = reinterpret_cast<float4*>(W + (size_t)q * rq);
+#pragma unroll
+          for (int k = 0; k < kJacobi32Vec; ++k) {
+            if (k < nv) {
+              const int e = gl + 8 * k;
+              wpw[e] = make_float4(c * x[k].x - sn * y[k].x, c * x[k].y - sn * y[k].y, c * x[k].z - sn * y[k].z,
+                                   c * x[k].w - sn * y[k].w);
+              wqw[e] = make_float4(sn * x[k].x + c * y[k].x, sn * x[k].y + c * y[k].y, sn * x[k].z + c * y[k].z,
+                                   sn * x[k].w + c * y[k].w);
+              const float4 u = vp[e], v = vq[e];
+              vp[e] = make_float4(c * u.x - sn * v.x, c * u.y - sn * v.y, c * u.z - sn * v.z, c * u.w - sn * v.w);
+              vq[e] = make_float4(sn * u.x + c * v.x, sn * u.y + c * v.y, sn * u.z + c * v.z, sn * u.w + c * v.w);
+            }
+          }
+          if (gl == 0) rot_flag[sweep] = 1;
+        }
+      }
+      __syncthreads();
+    }
+    if (!rot_flag[sweep]) break;
+  }
+  for (int t = tid; t < r * r; t += blockDim.x) {
+    const int j = t / r, i = t - (t / r) * r;
+    Vout[t] = (double)V[(size_t)j * rq + i];  // column-major r x r
+  }
+  if (tid == 0) *sweeps_out = sweep < kJacobi32MaxSweeps ? sweep + 1 : sweep;
+}
+
+// M = V^T V and, when C is given, P = C V (column-major: P[j * r + i]),
+// FP64; V column-major.  One 16 x 16 output tile per CTA: tiles [0, nt^2)
+// are M, [nt^2, 2 nt^2) are P.
+__global__ void __launch_bounds__(256) k_jacobi_pm(const double* __restrict__ C, const double* __restrict__ Vc, int r,
+                                                   double* __restrict__ Pc, double* __restrict__ M) {
+  extern __shared__ double mt[];
+  const int ldk = r + 1;  // odd: the 16 rows of a tile fall in distinct banks
+  double* As = mt;
+  double* Bs = mt + 16 * ldk;
+  const int nt = (r + 15) / 16;
+  int t = blockIdx.x;
+  const bool isP = t >= nt * nt;
+  if (isP) t -= nt * nt;
+  const int i0 = (t / nt) * 16, j0 = (t % nt) * 16;
+  for (int e = threadIdx.x; e < 16 * r; e += blockDim.x) {
+    const int a = e / r, k = e - (e / r) * r;
+    const int i = i0 + a, j = j0 + a;
+    As[a * ldk + k] = i < r ? (isP ? C[(int64_t)i * r + k] : Vc[(int64_t)i * r + k]) : 0.0;
+    Bs[a * ldk + k] = j < r ? Vc[(int64_t)j * r + k] : 0.0;
+  }
+  __syncthreads();
+  const int ti = threadIdx.x >> 4, tj = threadIdx.x & 15;
+  double acc = 0.0;
+  for (int k = 0; k < r; ++k) acc = fma(As[ti * ldk + k], Bs[tj * ldk + k], acc);
+  const int i = i0 + ti, j = j0 + tj;
+  if (i < r && j < r) {
+    if (isP)
+      Pc[(int64_t)j * r + i] = acc;
+    else
+      M[(int64_t)i * r + j] = acc;
+  }
+}
+
+// Y = X (3 I - M) / 2 for X = X1 and, when given, X2 (column-major r x r,
+// M symmetric): one Newton-Schulz step towards orthogonality when
+// M = V^T V (V^T V = I + E becomes I + O(E^2)).  Tiles [nt^2, 2 nt^2) do X2.
+__global__ void __launch_bounds__(256) k_jacobi_ns(const double* __restrict__ X1, const double* __restrict__ X2,
+                                                   const double* __restrict__ M, int r, double* __restrict__ Y1,
+                                                   double* __restrict__ Y2) {
+  extern __shared__ double mt[];
+  const int ldk = r + 1;
+  double* As = mt;  // As[a][k] = X[i0 + a][k] = Xc[k * r + i0 + a]
+  double* Bs = mt + 16 * ldk;
+  const int nt = (r + 15) / 16;
+  int t = blockIdx.x;
+  const bool second = t >= nt * nt;
+  if (second) t -= nt * nt;
+  const double* X = second ? X2 : X1;
+  double* Y = second ? Y2 : Y1;
+  const int i0 = (t / nt) * 16, j0 = (t % nt) * 16;
+  for (int e = threadIdx.x; e < 16 * r; e += blockDim.x) {
+    const int a = e & 15, k = e >> 4;
+    As[a * ldk + k] = i0 + a < r ? X[(int64_t)k * r + i0 + a] : 0.0;
+  }
+  for (int e = threadIdx.x; e < 16 * r; e += blockDim.x) {
+    const int b = e / r, k = e - (e / r) * r;
+    Bs[b * ldk + k] = j0 + b < r ? M[(int64_t)(j0 + b) * r + k] : 0.0;
+  }
+  __syncthreads();
+  const int ti = threadIdx.x >> 4, tj = threadIdx.x & 15;
+  double acc = 0.0;
+  for (int k = 0; k < r; ++k) acc = fma(As[ti * ldk + k], Bs[tj * ldk + k], acc);
+  const int i = i0 + ti, j = j0 + tj;
+  if (i < r && j < r) Y[(int64_t)j * r + i] = fma(1.5, X[(int64_t)j * r + i], -0.5 * acc);
+}
+
 __global__ void k_jacobi_finish(int r, const double* __restrict__ Wc, double* __restrict__ U,
                                 double* __restrict__ S) {
   __shared__ int order[1024];
@@ -761,19 +996,50 @@ __global__ void k_jacobi_finish(int r, const double* __restrict__ Wc, double* __
   for (int jn = threadIdx.x; jn < r; jn += blockDim.x) S[jn] = norms[order[jn]];
 }
 
-int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out) {
+static size_t jacobi_precond_smem(int r) { return sizeof(float) * 2 * (size_t)r * jacobi32_stride(r); }
+
+static bool jacobi_precond_applies(lne_ctx* ctx, int r) {
+  return r <= 32 * kJacobi32Vec && jacobi_precond_smem(r) + 1024 <= ctx->smem_optin;
+}
+
+int jacobi_svd_launches(lne_ctx* ctx, int r) { return jacobi_precond_applies(ctx, r) ? 7 : 3; }
+
+int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out, int* sweeps32_out) {
   if (r > 1024) {
     set_error("jacobi_svd: rank above 1024 is not supported");
     return LNE_ERR_UNSUPPORTED;
   }
   const int kMaxSweeps = kJacobiMaxSweeps;
+  const bool pre = jacobi_precond_applies(ctx, r);
+  const size_t rr = (size_t)r * r;
   double* Wc = nullptr;
   int rc;
-  if ((rc = dalloc(ctx, (void**)&Wc, sizeof(double) * r * r + sizeof(int) * (kMaxSweeps + 4), "jacobi work")))
-    return rc;
-  int* rotated = (int*)(Wc + (int64_t)r * r);
-  int* d_sw = rotated + kMaxSweeps;
-  k_jacobi_init<<<64, 256, 0, ctx->stream>>>(C, r, Wc, rotated, kMaxSweeps);
+  // Wc, then (preconditioned) V, P, M, V1, P1 (FP64 r x r each)
+  const size_t bytes = sizeof(double) * rr * (pre ? 6 : 1) + sizeof(int) * (kMaxSweeps + 4);
+  if ((rc = dalloc(ctx, (void**)&Wc, bytes, "jacobi work"))) return rc;
+  double* Vd = Wc + rr;
+  double* Pc = Vd + rr;
+  double* M = Pc + rr;
+  double* V1 = M + rr;
+  double* P1 = V1 + rr;
+  int* rotated = (int*)(Wc + rr * (pre ? 6 : 1));
+  int* d_sw = rotated + kMaxSweeps;  // [0]: FP64 sweeps, [1]: FP32 sweeps
+  LNE_CUDA_TRY(cudaMemsetAsync(d_sw + 1, 0, sizeof(int), ctx->stream));
+  if (pre) {
+    // FP32 sweeps give V; two Newton-Schulz steps make it orthogonal to
+    // FP64 precision (V^T V - I: about 1e-5 -> 1e-10 -> 1e-16); W = C V
+    const size_t psmem = jacobi_precond_smem(r);
+    cudaFuncSetAttribute(k_jacobi_precond32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+    k_jacobi_precond32<<<1, 1024, psmem, ctx->stream>>>(C, r, Vd, d_sw + 1);
+    const int nt = (r + 15) / 16;
+    const size_t msmem = sizeof(double) * 32 * (size_t)(r + 1);
+    k_jacobi_pm<<<2 * nt * nt, 256, msmem, ctx->stream>>>(C, Vd, r, Pc, M);              // M = V^T V, P = C V
+    k_jacobi_ns<<<2 * nt * nt, 256, msmem, ctx->stream>>>(Vd, Pc, M, r, V1, P1);         // V1, P1 = (V, P)(3I - M)/2
+    k_jacobi_pm<<<nt * nt, 256, msmem, ctx->stream>>>(nullptr, V1, r, nullptr, M);       // M = V1^T V1
+    k_jacobi_ns<<<nt * nt, 256, msmem, ctx->stream>>>(P1, nullptr, M, r, Wc, nullptr);   // W = P1 (3I - M)/2
+  } else {
+    k_jacobi_init<<<64, 256, 0, ctx->stream>>>(C, r, Wc, rotated, kMaxSweeps);
+  }
   // one cluster: 16 CTAs if the device accepts that (non-portable) size
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -811,12 +1077,13 @@ int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps
     return LNE_ERR_CUDA;
   }
   k_jacobi_finish<<<1, 1024, 0, ctx->stream>>>(r, Wc, U, S);
-  int h = 0;
-  LNE_CUDA_TRY(cudaMemcpyAsync(&h, d_sw, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  int h[2] = {0, 0};
+  LNE_CUDA_TRY(cudaMemcpyAsync(h, d_sw, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->stream));
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   dfree(ctx, Wc);
   LNE_CUDA_TRY(cudaGetLastError());
-  if (sweeps_out) *sweeps_out = h;
+  if (sweeps_out) *sweeps_out = h[0];
+  if (sweeps32_out) *sweeps32_out = h[1];
   return LNE_OK;
 }
 

@@ -39,8 +39,12 @@ int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W);
 
 // One-sided Jacobi SVD of C (r x r, FP64 row-major, device; overwritten):
 // U (r x r FP64, columns = left singular vectors, sorted by singular value,
-// descending), S (r, FP64).
-int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out);
+// descending), S (r, FP64).  For r <= 160 the FP64 sweeps start from an
+// FP32 Jacobi preconditioning; *sweeps32_out (may be NULL) gets its sweeps
+// (0 without it), *sweeps_out the FP64 sweeps.
+int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out, int* sweeps32_out = nullptr);
+// Kernel launches of one jacobi_svd call.
+int jacobi_svd_launches(lne_ctx* ctx, int r);
 
 // tcgen05 tensor-core versions (3xTF32, FP32-level accuracy) of gram and
 // gemm_tall for up to 256 columns; gram/gemm_tall use them when they apply.

@@ -234,9 +234,9 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
       (rc = B.get(&S, (size_t)r, "S")))
     return rc;
   if ((rc = gram(ctx, Y, ld, r, Bm, ld, r, n, C))) return rc;
-  int sweeps = 0;
-  if ((rc = jacobi_svd(ctx, C, r, U, S, &sweeps))) return rc;
-  launches += 2 + 3;  // Gram + reduction, Jacobi init / sweeps / finish
+  int sweeps = 0, sweeps32 = 0;
+  if ((rc = jacobi_svd(ctx, C, r, U, S, &sweeps, &sweeps32))) return rc;
+  launches += 2 + jacobi_svd_launches(ctx, r);  // Gram + reduction, Jacobi
   // emb = Z * (U_C[:, :dim] * diag(sqrt(S[:dim])))
   if ((rc = B.get(&Wf, (size_t)r * dim, "U sqrt(S)"))) return rc;
   k_scale_cols<<<(r * dim + 255) / 256, 256, 0, st>>>(U, S, r, dim, Wf);
@@ -270,8 +270,28 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
     cudaEventElapsedTime(&stats->ms_core, ev[3], ev[5]);
     cudaEventElapsedTime(&stats->ms_total, ev[0], ev[5]);
     stats->jacobi_sweeps = sweeps;
+    stats->jacobi_sweeps_fp32 = sweeps32;
     stats->kernel_launches = launches;
     stats->spmm_nnz = (double)A->nnz;
+  }
+  return LNE_OK;
+}
+
+extern "C" int lne_core_svd(lne_ctx* ctx, const double* d_C, int32_t r, double* d_U, double* d_S,
+                            int32_t* h_sweeps) {
+  LNE_CHECK_ARG(ctx && d_C && d_U && d_S && r >= 1, "lne_core_svd: bad argument");
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  Buf B(ctx);
+  double* C = nullptr;
+  int rc;
+  if ((rc = B.get(&C, (size_t)r * r, "core copy"))) return rc;
+  LNE_CUDA_TRY(cudaMemcpyAsync(C, d_C, sizeof(double) * r * r, cudaMemcpyDeviceToDevice, ctx->stream));
+  int sw = 0, sw32 = 0;
+  if ((rc = jacobi_svd(ctx, C, r, d_U, d_S, &sw, &sw32))) return rc;
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (h_sweeps) {
+    h_sweeps[0] = sw;
+    h_sweeps[1] = sw32;
   }
   return LNE_OK;
 }
