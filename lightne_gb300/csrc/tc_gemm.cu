@@ -424,6 +424,220 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
   stream_finish(sh, tmem, 256, ok, last_commit, flags);
 }
 
+// Warp-specialised form of the update GEMM (same operands, layouts and
+// MMAs as k_tc_gemm_stream), for W of at most kWsMaxCols columns:
+//   warp 8 (loader)      cp.async of raw 16-K slices of In into a ring of
+//                        `ring` slots; raw_full[s] completes when they land
+//   warps 0-3 (split)    raw slot -> TF32 hi/lo operand stage (2 stages),
+//                        releases the raw slot, publishes the stage
+//   warp 9 lane 0 (MMA)  6 MMAs per slice into one of two TMEM accumulators;
+//                        its commits release the stage and, after a tile's
+//                        last slice, hand the accumulator to the epilogue
+//   warps 4-7 (store)    TMEM -> registers -> Out (and OutB), then release
+//                        the accumulator
+// so that loads, splitting, MMAs and stores of successive slices and tiles
+// overlap instead of meeting at block-wide barriers.  Every wait is bounded;
+// a timeout sets the context's numeric flag to 2, which ends every other
+// wait within 64 polls.
+constexpr int kWsThreads = 320;
+constexpr int kWsLoadWarp = 8;
+constexpr int kWsMmaWarp = 9;
+constexpr int kWsMaxRing = 8;
+constexpr int kWsMaxCols = 256;  // two accumulators of up to 256 TMEM columns
+
+struct WsShared {
+  unsigned long long raw_full[kWsMaxRing], raw_empty[kWsMaxRing];
+  unsigned long long conv_full[2], conv_empty[2], acc_full[2], acc_empty[2];
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const float* __restrict__ In, int64_t ldi, int K,
+                                                             const float* __restrict__ W, int c2, int nmma, int ring,
+                                                             int64_t n, float* __restrict__ Out, int64_t ldo,
+                                                             __nv_bfloat16* __restrict__ OutB, int* flags) {
+  extern __shared__ __align__(1024) uint8_t stream_smem[];
+  const int nsl = (K + kSlice - 1) / kSlice;
+  const uint32_t wslice = (uint32_t)nmma * kSliceRowBytes;
+  uint8_t* w_hi = stream_smem;
+  uint8_t* w_lo = stream_smem + (size_t)nsl * wslice;
+  uint8_t* raw = w_lo + (size_t)nsl * wslice;
+  uint8_t* conv = raw + (size_t)ring * kASlice;  // 2 stages x (hi, lo)
+  WsShared* sh = reinterpret_cast<WsShared*>(conv + 4 * kASlice);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+
+  for (int idx = t; idx < nsl * 4 * nmma; idx += kWsThreads) {
+    const int j = idx % nmma, sq = idx / nmma, sl = sq >> 2, q = sq & 3;
+    float4 x;
+    float* xv = reinterpret_cast<float*>(&x);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int k = sl * kSlice + 4 * q + e;
+      xv[e] = (j < c2 && k < K) ? W[(int64_t)k * c2 + j] : 0.0f;
+    }
+    float4 h, l;
+    split4(x, h, l);
+    const uint32_t off = (uint32_t)sl * wslice + tc::kmajor_off((uint32_t)j, (uint32_t)(4 * q), kSlice);
+    *reinterpret_cast<float4*>(w_hi + off) = h;
+    *reinterpret_cast<float4*>(w_lo + off) = l;
+  }
+  if (t == 0) {
+    for (int s = 0; s < ring; ++s) {
+      tc::mbar_init(tc::smem_addr(&sh->raw_full[s]), 32);
+      tc::mbar_init(tc::smem_addr(&sh->raw_empty[s]), 4);
+    }
+    for (int c = 0; c < 2; ++c) {
+      tc::mbar_init(tc::smem_addr(&sh->conv_full[c]), 4);
+      tc::mbar_init(tc::smem_addr(&sh->conv_empty[c]), 1);
+      tc::mbar_init(tc::smem_addr(&sh->acc_full[c]), 1);
+      tc::mbar_init(tc::smem_addr(&sh->acc_empty[c]), 4);
+    }
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(&sh->tmem_base), 512);
+  tc::fence_proxy_async_smem();  // W, written by every thread, is read by the tensor core
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = sh->tmem_base;
+  const int64_t ntiles = (n + 127) / 128;
+  const int64_t my_tiles = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int64_t total = my_tiles * nsl;
+  int* abortf = flags + kFlagNumeric;
+  auto fail = [&]() { atomicExch(abortf, 2); };
+  int64_t last_commit = -1;  // MMA thread: slice of its last commit
+
+  if (warp == kWsLoadWarp) {
+    for (int64_t g = 0; g < total; ++g) {
+      const int s = (int)(g % ring);
+      if (g >= ring &&
+          !tc::mbar_wait(tc::smem_addr(&sh->raw_empty[s]), (uint32_t)((g / ring - 1) & 1), kWaitCycles, abortf)) {
+        if (lane == 0) fail();
+        break;
+      }
+      const int64_t tile = blockIdx.x + (g / nsl) * gridDim.x;
+      const int k0 = (int)(g % nsl) * kSlice;
+      const uint32_t dst0 = tc::smem_addr(raw + (size_t)s * kASlice);
+      for (int idx = lane; idx < 128 * 4; idx += 32) {
+        const int r = idx >> 2, q = idx & 3;
+        const int64_t row = tile * 128 + r;
+        const int k = k0 + 4 * q;
+        const int kb = K - k;
+        const uint32_t bytes = (row < n && kb > 0) ? (uint32_t)(kb >= 4 ? 16 : 4 * kb) : 0u;
+        const float* src = bytes ? In + row * ldi + k : In;
+        tc::cp_async16(dst0 + tc::kmajor_off((uint32_t)r, (uint32_t)(4 * q), kSlice), src, bytes);
+      }
+      tc::cp_async_mbar_arrive(tc::smem_addr(&sh->raw_full[s]));
+    }
+    tc::cp_async_wait_all();
+  } else if (warp < 4) {
+    for (int64_t g = 0; g < total; ++g) {
+      const int s = (int)(g % ring), c = (int)(g & 1);
+      if (!tc::mbar_wait(tc::smem_addr(&sh->raw_full[s]), (uint32_t)((g / ring) & 1), kWaitCycles, abortf) ||
+          (g >= 2 &&
+           !tc::mbar_wait(tc::smem_addr(&sh->conv_empty[c]), (uint32_t)(((g >> 1) - 1) & 1), kWaitCycles, abortf))) {
+        if (lane == 0) fail();
+        break;
+      }
+      const float4* src = reinterpret_cast<const float4*>(raw + (size_t)s * kASlice);
+      float4* hi = reinterpret_cast<float4*>(conv + (size_t)c * 2 * kASlice);
+      float4* lo = reinterpret_cast<float4*>(conv + (size_t)c * 2 * kASlice + kASlice);
+#pragma unroll
+      for (int idx = t; idx < (int)(kASlice / 16); idx += 128) {
+        float4 h, l;
+        split4(src[idx], h, l);
+        hi[idx] = h;
+        lo[idx] = l;
+      }
+      tc::fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        tc::mbar_arrive(tc::smem_addr(&sh->raw_empty[s]));
+        tc::mbar_arrive(tc::smem_addr(&sh->conv_full[c]));
+      }
+    }
+  } else if (warp == kWsMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_tf32(128, nmma);
+      for (int64_t g = 0; g < total; ++g) {
+        const int c = (int)(g & 1);
+        const int sl = (int)(g % nsl);
+        const int64_t j = g / nsl;
+        const int b = (int)(j & 1);
+        if (sl == 0 && j >= 2 &&
+            !tc::mbar_wait(tc::smem_addr(&sh->acc_empty[b]), (uint32_t)(((j >> 1) - 1) & 1), kWaitCycles, abortf)) {
+          fail();
+          break;
+        }
+        if (!tc::mbar_wait(tc::smem_addr(&sh->conv_full[c]), (uint32_t)((g >> 1) & 1), kWaitCycles, abortf)) {
+          fail();
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t a_hi = tc::smem_addr(conv + (size_t)c * 2 * kASlice);
+        issue_slice(tmem + (uint32_t)(b * kWsMaxCols), slice_desc(a_hi), slice_desc(a_hi + kASlice),
+                    slice_desc(tc::smem_addr(w_hi) + sl * wslice), slice_desc(tc::smem_addr(w_lo) + sl * wslice),
+                    idesc, sl == 0);
+        tc::commit(tc::smem_addr(&sh->conv_empty[c]));
+        if (sl == nsl - 1) tc::commit(tc::smem_addr(&sh->acc_full[b]));
+        last_commit = g;
+      }
+      // nothing may still write TMEM when it is released: wait (bounded,
+      // not abortable) for the last commit
+      if (last_commit >= 0)
+        tc::mbar_wait(tc::smem_addr(&sh->conv_empty[last_commit & 1]), (uint32_t)((last_commit >> 1) & 1),
+                      kWaitCycles, flags + kFlagTimeoutGuard);
+    }
+    __syncwarp();
+  } else {
+    const int lg = warp & 3;  // TMEM lanes 32 lg ..
+    const bool vec = ((ldo & 3) == 0) && ((reinterpret_cast<uintptr_t>(Out) & 15) == 0);
+    for (int64_t j = 0; j < my_tiles; ++j) {
+      const int b = (int)(j & 1);
+      if (!tc::mbar_wait(tc::smem_addr(&sh->acc_full[b]), (uint32_t)((j >> 1) & 1), kWaitCycles, abortf)) {
+        if (lane == 0) fail();
+        break;
+      }
+      tc::fence_after_sync();
+      const int64_t tile = blockIdx.x + j * gridDim.x;
+      const int64_t row = tile * 128 + 32 * lg + lane;
+      for (int cg = 0; cg * 16 < nmma; ++cg) {
+        float v[16];
+        tc::tmem_ld16(tmem + (uint32_t)(b * kWsMaxCols) + ((uint32_t)(32 * lg) << 16) + (uint32_t)(cg * 16), v);
+        if (row < n) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (cg * 16 + i >= c2) v[i] = 0.0f;
+          float* orow = Out + row * ldo + cg * 16;
+          if (vec && cg * 16 + 16 <= ldo) {
+#pragma unroll
+            for (int i = 0; i < 16; i += 4)
+              *reinterpret_cast<float4*>(orow + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+          } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (cg * 16 + i < ldo) orow[i] = v[i];
+          }
+          if (OutB) {
+            __nv_bfloat16* brow = OutB + row * ldo + cg * 16;
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (cg * 16 + i < ldo) brow[i] = __float2bfloat16_rn(v[i]);
+          }
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tc::smem_addr(&sh->acc_empty[b]));
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
 // Partial Gram of one contiguous range of SL-row slices per CTA (SL = 32
 // where the stages fit in shared memory, else 16):
 // partial[b] (c1 x c2) = A[rows]^T B[rows].  Both 128-column tiles of A are
@@ -700,6 +914,26 @@ int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float*
   if (nmma > 256) {
     set_error("tc_gemm_tall: more than 256 output columns");
     return LNE_ERR_UNSUPPORTED;
+  }
+  // warp-specialised kernel: the deepest raw ring (up to kWsMaxRing, at
+  // least 2) that fits beside W and the two operand stages
+  const size_t ws_fixed = gemm_stream_smem(k, nmma) - (size_t)kGemmRing * kASlice - sizeof(StreamShared) +
+                          sizeof(WsShared);
+  const int ws_ring = ctx->smem_optin > ws_fixed
+                          ? (int)std::min<size_t>(kWsMaxRing, (ctx->smem_optin - ws_fixed) / kASlice)
+                          : 0;
+  if (aligned16(In, ldi) && k >= 1 && nmma <= kWsMaxCols && ws_ring >= 2) {
+    const int64_t ntiles = (n + 127) / 128;
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, ctx->num_sms);
+    const size_t wsmem = ws_fixed + (size_t)ws_ring * kASlice;
+    // a CTA allocates all 512 TMEM columns: one CTA per SM, which the
+    // shared memory request also ensures
+    const size_t lsmem = std::max(wsmem, ctx->smem_optin / 2 + 1);
+    cudaFuncSetAttribute(k_tc_gemm_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
+    k_tc_gemm_ws<<<grid, kWsThreads, lsmem, ctx->stream>>>(In, ldi, k, W, c2, nmma, ws_ring, n, Out, ldo, OutB,
+                                                           ctx->d_flags);
+    LNE_CUDA_TRY(cudaGetLastError());
+    return LNE_OK;
   }
   const size_t ssmem = gemm_stream_smem(k, nmma);
   if (aligned16(In, ldi) && ssmem <= ctx->smem_optin && k >= 1) {

@@ -130,6 +130,15 @@ __device__ __forceinline__ void cp_async16(uint32_t dst_saddr, const void* src, 
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// The mbarrier gets one arrival (counted in its expected count) once every
+// cp.async this thread issued before has landed.
+__device__ __forceinline__ void cp_async_mbar_arrive(uint32_t mbar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
 // Waits until at most N of this thread's committed copy groups are pending.
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
