@@ -10,9 +10,11 @@
 // tells the stagers when a stage may be refilled.  Every wait is bounded:
 // on a timeout the kernel sets the context's numeric flag to 2, waits once
 // more (bounded), frees its TMEM and returns.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <string>
 
 #include "dense.h"
@@ -250,6 +252,18 @@ __device__ __forceinline__ void issue_slice(uint32_t tmem_d, uint64_t ah, uint64
     tc::mma_tf32(tmem_d, al + ko, bh + ko, idesc, 1u);
   }
 }
+// The same with the A descriptors advanced by `a_step` (in 16-byte units)
+// per K = 8 step and the B descriptors by 16.
+__device__ __forceinline__ void issue_slice_a(uint32_t tmem_d, uint64_t ah, uint64_t al, uint32_t a_step, uint64_t bh,
+                                              uint64_t bl, uint32_t idesc, bool first) {
+#pragma unroll
+  for (int ks = 0; ks < kSlice / 8; ++ks) {
+    const uint64_t ka = (uint64_t)(ks * a_step), kb = (uint64_t)(ks * 16);
+    tc::mma_tf32(tmem_d, ah + ka, bh + kb, idesc, (first && ks == 0) ? 0u : 1u);
+    tc::mma_tf32(tmem_d, ah + ka, bl + kb, idesc, 1u);
+    tc::mma_tf32(tmem_d, al + ka, bh + kb, idesc, 1u);
+  }
+}
 template <int SL = kSlice>
 __device__ __forceinline__ uint64_t slice_desc(uint32_t saddr) {
   return tc::smem_desc(saddr, 128, (SL / 4) * 128);
@@ -426,11 +440,11 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
 
 // Warp-specialised form of the update GEMM (same operands, layouts and
 // MMAs as k_tc_gemm_stream), for W of at most kWsMaxCols columns:
-//   warp 8 (loader)      cp.async of raw 16-K slices of In into a ring of
+//   warps 8-9 (loaders)  cp.async of raw 16-K slices of In into a ring of
 //                        `ring` slots; raw_full[s] completes when they land
 //   warps 0-3 (split)    raw slot -> TF32 hi/lo operand stage (2 stages),
 //                        releases the raw slot, publishes the stage
-//   warp 9 lane 0 (MMA)  6 MMAs per slice into one of two TMEM accumulators;
+//   warp 10 lane 0 (MMA) 6 MMAs per slice into one of two TMEM accumulators;
 //                        its commits release the stage and, after a tile's
 //                        last slice, hand the accumulator to the epilogue
 //   warps 4-7 (store)    TMEM -> registers -> Out (and OutB), then release
@@ -439,9 +453,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
 // overlap instead of meeting at block-wide barriers.  Every wait is bounded;
 // a timeout sets the context's numeric flag to 2, which ends every other
 // wait within 64 polls.
-constexpr int kWsThreads = 320;
+constexpr int kWsLoadWarps = 4;  // warps 8 .. 8 + kWsLoadWarps - 1
+constexpr int kWsThreads = 32 * (9 + kWsLoadWarps);
 constexpr int kWsLoadWarp = 8;
-constexpr int kWsMmaWarp = 9;
+constexpr int kWsMmaWarp = 8 + kWsLoadWarps;
 constexpr int kWsMaxRing = 8;
 constexpr int kWsMaxCols = 256;  // two accumulators of up to 256 TMEM columns
 
@@ -451,7 +466,9 @@ struct WsShared {
   uint32_t tmem_base;
 };
 
-__global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const float* __restrict__ In, int64_t ldi, int K,
+template <bool TMA>
+__global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const __grid_constant__ CUtensorMap tmap,
+                                                             const float* __restrict__ In, int64_t ldi, int K,
                                                              const float* __restrict__ W, int c2, int nmma, int ring,
                                                              int64_t n, float* __restrict__ Out, int64_t ldo,
                                                              __nv_bfloat16* __restrict__ OutB, int* flags) {
@@ -482,7 +499,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const float* __res
   }
   if (t == 0) {
     for (int s = 0; s < ring; ++s) {
-      tc::mbar_init(tc::smem_addr(&sh->raw_full[s]), 32);
+      tc::mbar_init(tc::smem_addr(&sh->raw_full[s]), TMA ? 1 : 32 * kWsLoadWarps);
       tc::mbar_init(tc::smem_addr(&sh->raw_empty[s]), 4);
     }
     for (int c = 0; c < 2; ++c) {
@@ -506,7 +523,28 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const float* __res
   auto fail = [&]() { atomicExch(abortf, 2); };
   int64_t last_commit = -1;  // MMA thread: slice of its last commit
 
-  if (warp == kWsLoadWarp) {
+  if (TMA && warp == kWsLoadWarp) {
+    // one thread: a 16 x 128 box (8 KB, 64-byte swizzle) per slice
+    if (lane == 0) {
+      for (int64_t g = 0; g < total; ++g) {
+        const int s = (int)(g % ring);
+        if (g >= ring &&
+            !tc::mbar_wait(tc::smem_addr(&sh->raw_empty[s]), (uint32_t)((g / ring - 1) & 1), kWaitCycles, abortf)) {
+          fail();
+          break;
+        }
+        const int64_t tile = blockIdx.x + (g / nsl) * gridDim.x;
+        const uint32_t mb = tc::smem_addr(&sh->raw_full[s]);
+        tc::mbar_arrive_expect_tx(mb, kASlice);
+        tc::tma_load_2d(tc::smem_addr(raw + (size_t)s * kASlice), &tmap, (int)(g % nsl) * kSlice, (int)(tile * 128),
+                        mb);
+      }
+    }
+    __syncwarp();
+  } else if (TMA && warp > kWsLoadWarp && warp < kWsLoadWarp + kWsLoadWarps) {
+    // idle loader warps of the TMA form
+  } else if (warp >= kWsLoadWarp && warp < kWsLoadWarp + kWsLoadWarps) {
+    const int ll = t - 32 * kWsLoadWarp;  // loader lane
     for (int64_t g = 0; g < total; ++g) {
       const int s = (int)(g % ring);
       if (g >= ring &&
@@ -517,7 +555,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const float* __res
       const int64_t tile = blockIdx.x + (g / nsl) * gridDim.x;
       const int k0 = (int)(g % nsl) * kSlice;
       const uint32_t dst0 = tc::smem_addr(raw + (size_t)s * kASlice);
-      for (int idx = lane; idx < 128 * 4; idx += 32) {
+      for (int idx = ll; idx < 128 * 4; idx += 32 * kWsLoadWarps) {
         const int r = idx >> 2, q = idx & 3;
         const int64_t row = tile * 128 + r;
         const int k = k0 + 4 * q;
@@ -574,9 +612,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const float* __res
         }
         tc::fence_after_sync();
         const uint32_t a_hi = tc::smem_addr(conv + (size_t)c * 2 * kASlice);
-        issue_slice(tmem + (uint32_t)(b * kWsMaxCols), slice_desc(a_hi), slice_desc(a_hi + kASlice),
-                    slice_desc(tc::smem_addr(w_hi) + sl * wslice), slice_desc(tc::smem_addr(w_lo) + sl * wslice),
-                    idesc, sl == 0);
+        // A: the TMA's 64-byte swizzle (8-row atoms 512 bytes apart; the
+        // second K = 8 step 32 bytes into the atom) or the no-swizzle
+        // core-matrix layout of the cp.async form
+        const uint64_t ah = TMA ? tc::smem_desc_sw64(a_hi, 512) : slice_desc(a_hi);
+        const uint64_t al = TMA ? tc::smem_desc_sw64(a_hi + kASlice, 512) : slice_desc(a_hi + kASlice);
+        issue_slice_a(tmem + (uint32_t)(b * kWsMaxCols), ah, al, TMA ? 2u : 16u,
+                      slice_desc(tc::smem_addr(w_hi) + sl * wslice), slice_desc(tc::smem_addr(w_lo) + sl * wslice),
+                      idesc, sl == 0);
         tc::commit(tc::smem_addr(&sh->conv_empty[c]));
         if (sl == nsl - 1) tc::commit(tc::smem_addr(&sh->acc_full[b]));
         last_commit = g;
@@ -907,6 +950,39 @@ static bool aligned16(const void* p, int64_t ld) {
   return (reinterpret_cast<uintptr_t>(p) & 15) == 0 && (ld & 3) == 0;
 }
 
+// cuTensorMapEncodeTiled, from the driver (no link against libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of a row-major FP32 matrix (rows x cols, ld elements between
+// rows) read in 16-column x 128-row boxes with the 64-byte swizzle; columns
+// and rows past the matrix read as zeros.
+static bool tmap_rows16x128(CUtensorMap* m, const float* base, int64_t rows, int cols, int64_t ld) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn || rows < 1 || cols < 1 || rows > 0x7fffffffLL) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)kSlice, 128};
+  const cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
                  int64_t ldo, __nv_bfloat16* OutB) {
   if (n <= 0) return LNE_OK;
@@ -929,9 +1005,17 @@ int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float*
     // a CTA allocates all 512 TMEM columns: one CTA per SM, which the
     // shared memory request also ensures
     const size_t lsmem = std::max(wsmem, ctx->smem_optin / 2 + 1);
-    cudaFuncSetAttribute(k_tc_gemm_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
-    k_tc_gemm_ws<<<grid, kWsThreads, lsmem, ctx->stream>>>(In, ldi, k, W, c2, nmma, ws_ring, n, Out, ldo, OutB,
-                                                           ctx->d_flags);
+    CUtensorMap tmap;
+    memset(&tmap, 0, sizeof(tmap));
+    if (tmap_rows16x128(&tmap, In, n, k, ldi)) {
+      cudaFuncSetAttribute(k_tc_gemm_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
+      k_tc_gemm_ws<true><<<grid, kWsThreads, lsmem, ctx->stream>>>(tmap, In, ldi, k, W, c2, nmma, ws_ring, n, Out, ldo,
+                                                                  OutB, ctx->d_flags);
+    } else {
+      cudaFuncSetAttribute(k_tc_gemm_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
+      k_tc_gemm_ws<false><<<grid, kWsThreads, lsmem, ctx->stream>>>(tmap, In, ldi, k, W, c2, nmma, ws_ring, n, Out,
+                                                                   ldo, OutB, ctx->d_flags);
+    }
     LNE_CUDA_TRY(cudaGetLastError());
     return LNE_OK;
   }

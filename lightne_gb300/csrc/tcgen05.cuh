@@ -136,6 +136,33 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint32_t mbar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mbar) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Arrive and add `bytes` to the transaction count the phase waits for.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes)
+               : "memory");
+}
+// 2-D tiled TMA load of the box at (x, y) (x: innermost, in elements) into
+// shared memory; completes `bytes` of the mbarrier's transaction count.
+// Out-of-range elements land as zeros.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst_saddr, const void* tmap, int x, int y, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst_saddr),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(mbar)
+      : "memory");
+}
+// Shared memory descriptor of a K-major operand in the 64-byte swizzle
+// layout (what a TMA box with a 64-byte inner extent and SWIZZLE_64B
+// writes): 8-row atoms of 64-byte rows, `sbo_bytes` between atoms.
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr, uint32_t sbo_bytes) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;  // leading byte offset: unused within one swizzle atom
+  d |= (uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;  // layout: 64-byte swizzle
+  return d;
+}
 __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
   asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
