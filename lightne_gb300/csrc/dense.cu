@@ -360,49 +360,77 @@ __device__ __forceinline__ void dsmem_st(uint32_t a, double v) {
 }
 
 // The same factorisation on one thread-block cluster (16 CTAs where the
-// device allows that size, else 8), r <= kCholClusterMax: column j in CTA
-// j % size.  Step k: the owner of column k takes the pivot and scales the
-// column, a cluster barrier publishes it, every CTA copies it (distributed
-// shared memory) and updates its own later columns, element by element in
-// the same operations and order as k_cholesky.  Then every CTA gathers L and
-// the cluster's warps solve L x = e_j for their columns j (each entry a
+// device allows that size, else 8), r <= kCholClusterMax, blocked by panels
+// of kCholPanel columns: panel q (columns 8q .. 8q + 7) lives in CTA
+// q % size.  Step q: the owner factors the panel in its shared memory
+// (pivot, scale, update of the panel's later columns, column by column), a
+// cluster barrier publishes it, every CTA copies it (distributed shared
+// memory) and applies it to its own later columns (rank-8 update).  One
+// cluster barrier per panel instead of one per pivot; the sums of a trailing
+// update run in panel order (not bit-identical to the one-CTA form, the
+// same FP64 arithmetic otherwise).  Then every CTA gathers L and the
+// cluster's warps solve L x = e_j for their columns j (each entry a
 // lane-parallel dot product), writing row j of W = L^-T.
 constexpr int kCholClusterMax = 144;
+constexpr int kCholPanel = 8;
 
 __global__ void __launch_bounds__(256) k_chol_inv_cluster(const double* __restrict__ G, int r, double shift,
                                                           float* __restrict__ W, int* __restrict__ status) {
   extern __shared__ double chs[];
   __shared__ int bad;
+  __shared__ double prcp;  // 1 / pivot
   const int csize = gridDim.x;
   const int rank = (int)cluster_rank();
-  const int nslots = (r + csize - 1) / csize;
+  const int npan = (r + kCholPanel - 1) / kCholPanel;
+  const int nps = (npan + csize - 1) / csize;  // panel slots per CTA
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  double* col = chs;                          // [nslots][r]: my columns
-  double* colk = col + (size_t)nslots * r;    // [r]: column k of this step
-  double* Lf = colk + r;                      // [r][r]: all of L (inverse phase)
-  double* xw = Lf + (size_t)r * r;            // [nw][r]: a warp's solution column
-  for (int s = 0; s < nslots; ++s) {
-    const int j = s * csize + rank;
+  double* col = chs;                                       // [nps * 8][r]: my columns
+  double* pan = col + (size_t)nps * kCholPanel * r;        // [8][r]: the panel of this step
+  double* Lf = pan + (size_t)kCholPanel * r;               // [r][r]: all of L (inverse phase)
+  double* xw = Lf + (size_t)r * r;                         // [nw][r]: a warp's solution column; then r reciprocals
+  // local column c (slot c / 8, offset c % 8) is global column j_of(c)
+  auto j_of = [&](int c) { return ((c / kCholPanel) * csize + rank) * kCholPanel + (c % kCholPanel); };
+  const int ncols = nps * kCholPanel;
+  for (int c = 0; c < ncols; ++c) {
+    const int j = j_of(c);
     if (j < r)
-      for (int i = tid; i < r; i += blockDim.x) col[(size_t)s * r + i] = G[(size_t)j * r + i] + (i == j ? shift : 0.0);
+      for (int i = tid; i < r; i += blockDim.x) col[(size_t)c * r + i] = G[(size_t)j * r + i] + (i == j ? shift : 0.0);
   }
   if (tid == 0) bad = 0;
   const uint32_t col_s = (uint32_t)__cvta_generic_to_shared(col);
   const uint32_t bad_s = (uint32_t)__cvta_generic_to_shared(&bad);
   cluster_barrier();
   bool failed = false;
-  for (int k = 0; k < r; ++k) {
-    const int own = k % csize, ks = k / csize;
-    if (rank == own && warp == 0) {
-      double* c = col + (size_t)ks * r;
-      const double d = c[k];
-      const bool ok = d > 0.0 && isfinite(d);
-      const double piv = ok ? sqrt(d) : 1.0;
-      for (int i = k + 1 + lane; i < r; i += 32) c[i] /= piv;
-      __syncwarp();
-      if (lane == 0) {
-        c[k] = piv;
-        if (!ok) bad = 1;
+  for (int q = 0; q < npan; ++q) {
+    const int own = q % csize, qs = q / csize;
+    const int k0 = q * kCholPanel, k1 = min(k0 + kCholPanel, r);
+    if (rank == own) {
+      for (int k = k0; k < k1; ++k) {
+        double* ck = col + (size_t)(qs * kCholPanel + (k - k0)) * r;
+        // FP64 division and square root are long instruction sequences on
+        // this part: one square root and one reciprocal per pivot, then
+        // the column is scaled by multiplications spread over all warps
+        if (warp == 0) {  // one warp evaluates the pivot
+          const double d = ck[k];
+          const bool ok = d > 0.0 && isfinite(d);
+          const double piv = ok ? sqrt(d) : 1.0;
+          if (lane == 0) {
+            prcp = 1.0 / piv;
+            ck[k] = piv;
+            if (!ok) bad = 1;
+          }
+        }
+        __syncthreads();
+        if (bad) break;
+        const double rp = prcp;
+        for (int i = k + 1 + tid; i < r; i += blockDim.x) ck[i] *= rp;
+        __syncthreads();
+        for (int j = k + 1 + warp; j < k1; j += nw) {
+          double* cj = col + (size_t)(qs * kCholPanel + (j - k0)) * r;
+          const double ljk = ck[j];
+          for (int i = j + lane; i < r; i += 32) cj[i] -= ck[i] * ljk;
+        }
+        __syncthreads();
       }
     }
     cluster_barrier();
@@ -410,36 +438,57 @@ __global__ void __launch_bounds__(256) k_chol_inv_cluster(const double* __restri
       failed = true;
       break;
     }
-    const uint32_t src = dsmem_map(col_s + (uint32_t)(ks * r) * 8u, (uint32_t)own);
-    for (int i = k + tid; i < r; i += blockDim.x) colk[i] = dsmem_ld(src + 8u * (uint32_t)i);
+    // the panel's rows k0.. into pan (column t of the panel at pan + t r)
+    const uint32_t src = dsmem_map(col_s + (uint32_t)(qs * kCholPanel * r) * 8u, (uint32_t)own);
+    for (int e = tid; e < (k1 - k0) * r; e += blockDim.x)
+      if (e - (e / r) * r >= k0) pan[e] = dsmem_ld(src + 8u * (uint32_t)e);
     __syncthreads();
-    for (int s = warp; s < nslots; s += nw) {
-      const int j = s * csize + rank;
-      if (j > k && j < r) {
-        const double ljk = colk[j];
-        double* c = col + (size_t)s * r;
-        for (int i = j + lane; i < r; i += 32) c[i] -= colk[i] * ljk;
+    // rank-(k1 - k0) update of my columns after the panel
+    for (int c = warp; c < ncols; c += nw) {
+      const int j = j_of(c);
+      if (j < k1 || j >= r) continue;
+      double lj[kCholPanel];
+#pragma unroll
+      for (int t = 0; t < kCholPanel; ++t) lj[t] = k0 + t < k1 ? pan[(size_t)t * r + j] : 0.0;
+      double* cj = col + (size_t)c * r;
+      for (int i = j + lane; i < r; i += 32) {
+        double v = cj[i];
+#pragma unroll
+        for (int t = 0; t < kCholPanel; ++t)
+          if (k0 + t < k1) v -= pan[(size_t)t * r + i] * lj[t];
+        cj[i] = v;
       }
     }
     __syncthreads();
   }
   cluster_barrier();
   if (!failed) {
-    // L row-major in every CTA: Lf[i][k] = column k, row i (i >= k)
+    // L column-major in every CTA (Lc[k][i] = column k, row i >= k) and
+    // the reciprocals of its diagonal
+    double* Lc = Lf;
+    double* idg = xw + (size_t)nw * r;
     for (int k = warp; k < r; k += nw) {
-      const uint32_t src = dsmem_map(col_s + (uint32_t)((k / csize) * r) * 8u, (uint32_t)(k % csize));
-      for (int i = k + lane; i < r; i += 32) Lf[(size_t)i * r + k] = dsmem_ld(src + 8u * (uint32_t)i);
+      const int qk = k / kCholPanel;
+      const uint32_t src =
+          dsmem_map(col_s + (uint32_t)(((qk / csize) * kCholPanel + (k % kCholPanel)) * r) * 8u, (uint32_t)(qk % csize));
+      for (int i = k + lane; i < r; i += 32) Lc[(size_t)k * r + i] = dsmem_ld(src + 8u * (uint32_t)i);
     }
     __syncthreads();
+    for (int i = tid; i < r; i += blockDim.x) idg[i] = 1.0 / Lc[(size_t)i * r + i];
+    __syncthreads();
+    // column j of X = L^-1 by column-oriented forward substitution:
+    // x_k = b_k / L_kk, then b_i -= L_ik x_k for i > k (lane-parallel, no
+    // reductions); row j of W = X^T
     double* x = xw + (size_t)warp * r;
     for (int j = warp * csize + rank; j < r; j += nw * csize) {
-      if (lane == 0) x[j] = 1.0 / Lf[(size_t)j * r + j];
+      for (int i = lane; i < r; i += 32) x[i] = i == j ? 1.0 : 0.0;
       __syncwarp();
-      for (int i = j + 1; i < r; ++i) {
-        double sacc = 0.0;
-        for (int k = j + lane; k < i; k += 32) sacc = fma(Lf[(size_t)i * r + k], x[k], sacc);
-        for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
-        if (lane == 0) x[i] = -sacc / Lf[(size_t)i * r + i];
+      for (int k = j; k < r; ++k) {
+        const double xk = x[k] * idg[k];
+        __syncwarp();
+        if (lane == 0) x[k] = xk;
+        const double* lk = Lc + (size_t)k * r;
+        for (int i = k + 1 + lane; i < r; i += 32) x[i] = fma(-lk[i], xk, x[i]);
         __syncwarp();
       }
       for (int i = lane; i < r; i += 32) W[(size_t)j * r + i] = i < j ? 0.0f : (float)x[i];
@@ -451,8 +500,9 @@ __global__ void __launch_bounds__(256) k_chol_inv_cluster(const double* __restri
 }
 
 static size_t chol_cluster_smem(int r, int csize) {
-  const size_t nslots = (size_t)(r + csize - 1) / csize;
-  return sizeof(double) * (nslots * r + r + (size_t)r * r + 8 * (size_t)r);
+  const size_t npan = (size_t)(r + kCholPanel - 1) / kCholPanel;
+  const size_t nps = (npan + csize - 1) / csize;
+  return sizeof(double) * (nps * kCholPanel * r + (size_t)kCholPanel * r + (size_t)r * r + 9 * (size_t)r);
 }
 
 // Launches k_chol_inv_cluster on a 16- or 8-CTA cluster; false if neither
