@@ -66,6 +66,15 @@ int lne_ctx_destroy(lne_ctx* ctx);
 /* L2 tuning: the bytes of L2 one column panel of an SpMM
  * dense operand may occupy (default 64 MiB; 0 disables column panels). */
 int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes);
+/* Aggregation of the sparsifier's pair samples (no reference counterpart:
+ * the reference always inserts into par_table, LightNE/par_table.h:86-109).
+ * With counts (-sample 0) and one batch of samples, lne_sparsify counts the
+ * pairs slice by slice in shared-memory tables of `slots` entries (a power
+ * of two in [64, 16384]; default 16384) over 2^slice_bits slices of the
+ * hash space (-1, the default: chosen from the sample count; at most 16),
+ * and falls back to the pair table in HBM when a slice overflows.
+ * slots = 0 always uses the pair table.  The output is the same either way. */
+int lne_ctx_set_sparsify_slices(lne_ctx* ctx, int32_t slots, int32_t slice_bits);
 /* Wait for all work queued on the context's stream. */
 int lne_ctx_synchronize(lne_ctx* ctx);
 
@@ -112,6 +121,7 @@ typedef struct lne_sparsify_stats {
   int64_t exp_rv_rounded, table_size, capacity, samples_emitted, distinct, nnz_upper, nnz;
   float ms_sample, ms_trunclog, ms_csr; /* device time per stage (CUDA events) */
   int32_t kernel_launches;              /* kernels this call launched */
+  int32_t sliced;                       /* 1: pairs counted by the sliced aggregation, 0: pair table */
 } lne_sparsify_stats;
 
 /*

@@ -70,6 +70,7 @@ class SparsifyStats(ctypes.Structure):
         ("ms_trunclog", ctypes.c_float),
         ("ms_csr", ctypes.c_float),
         ("kernel_launches", ctypes.c_int32),
+        ("sliced", ctypes.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -141,6 +142,7 @@ SIGNATURES = {
     "lne_ctx_destroy": (ctypes.c_int, [VP]),
     "lne_ctx_synchronize": (ctypes.c_int, [VP]),
     "lne_ctx_set_spmm_panel_bytes": (ctypes.c_int, [VP, I64]),
+    "lne_ctx_set_sparsify_slices": (ctypes.c_int, [VP, I32, I32]),
     "lne_device_alloc": (ctypes.c_int, [VP, I64, PVP]),
     "lne_device_free": (ctypes.c_int, [VP, VP]),
     "lne_copy_to_host": (ctypes.c_int, [VP, VP, VP, I64]),

@@ -20,6 +20,7 @@ enum FlagIndex : int {
   kFlagSortOverflow = 2,  // a device buffer sized from host counts was too small (internal)
   kFlagNumeric = 3,     // 2: a tensor-core kernel's wait timed out (the other CTAs stop waiting)
   kFlagTimeoutGuard = 4,  // always 0: the no-abort flag of the final bounded wait
+  kFlagSliceOverflow = 5,  // a slice of the sliced aggregation had more pairs than its shared table
   kFlagWords = 8,
 };
 
@@ -61,6 +62,11 @@ struct lne_ctx {
   // panels, the default: with full-width lane layouts the gathers run as
   // fast from HBM as from L2-sized panels at 1.1M x 144)
   int64_t spmm_panel_bytes = 0;
+  // Sliced aggregation of the sparsifier's samples (counts, one batch):
+  // shared-memory table size per slice (0: always the pair table in HBM)
+  // and the number of slice bits (-1: chosen from the sample count).
+  int sparsify_slice_slots = 16384;
+  int sparsify_slice_bits = -1;
 };
 
 struct lne_graph {

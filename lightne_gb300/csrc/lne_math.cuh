@@ -25,6 +25,17 @@ LNE_HD uint64_t hash64_2(uint64_t x) {
   x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
   return x ^ (x >> 31);
 }
+// hash64_2 is a bijection of the 64-bit words: x ^= x >> s is undone by
+// xoring in the shifts by s, 2s, ... below 64, and a multiply by an odd
+// constant by a multiply by its inverse mod 2^64.  So a pair key can travel
+// as its hash and be recovered exactly.
+LNE_HD uint64_t hash64_2_inv(uint64_t y) {
+  y ^= (y >> 31) ^ (y >> 62);
+  y *= 0x319642b2d24d8ec3ULL;  // 0x94d049bb133111eb^-1 mod 2^64
+  y ^= (y >> 27) ^ (y >> 54);
+  y *= 0x96de1b173f119089ULL;  // 0xbf58476d1ce4e5b9^-1 mod 2^64
+  return y ^ (y >> 30) ^ (y >> 60);
+}
 LNE_HD uint64_t rng_rand(uint64_t s) { return hash64_2(s); }
 LNE_HD uint64_t rng_next(uint64_t s) { return hash64_2(hash64_2(s)); }
 LNE_HD uint64_t rng_fork(uint64_t s, uint64_t i) { return hash64_2(hash64_2(i + s)); }

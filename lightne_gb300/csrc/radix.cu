@@ -331,4 +331,53 @@ int partition_by_slot(lne_ctx* ctx, const unsigned long long* keys, unsigned lon
   return LNE_OK;
 }
 
+int partition_by_top_bits(lne_ctx* ctx, unsigned long long* keys, unsigned long long* tmp, int64_t count,
+                          int top_bits, unsigned long long** result, int* launches) {
+  *result = keys;
+  if (count <= 0 || top_bits <= 0) return LNE_OK;
+  if (top_bits > 16) {
+    set_error("partition: at most 16 top bits");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  const int passes = (top_bits + 7) / 8;
+  const int dbits = (top_bits + passes - 1) / passes;
+  const int bins = 1 << dbits;
+  const int64_t ntiles = (count + kRadixTile - 1) / kRadixTile;
+  if (ntiles > 0x7fffffffLL) {
+    set_error("partition: too many keys");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  const int64_t cells = (int64_t)bins * ntiles;
+  char* mem = nullptr;
+  const size_t hist_bytes = (sizeof(int64_t) * (size_t)(cells + 1) + 255) & ~(size_t)255;
+  int rc = dalloc(ctx, (void**)&mem, 2 * hist_bytes + scan_tmp_bytes(cells), "partition histograms");
+  if (rc) return rc;
+  int64_t* hist = (int64_t*)mem;
+  int64_t* offs = (int64_t*)(mem + hist_bytes);
+  void* scan_tmp = mem + 2 * hist_bytes;
+  cudaStream_t st = ctx->stream;
+  cudaFuncSetAttribute(k_radix_scatter<false, kDigitKey, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kScatterSmem);
+  unsigned long long *src = keys, *dst = tmp;
+  for (int p = 0; p < passes; ++p) {
+    // digits from the least significant of the top bits up; the last digit
+    // may extend past bit 63, where the shifted word is zero
+    const int shift = 64 - top_bits + p * dbits;
+    k_radix_hist<kDigitKey><<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src, count, shift, dbits, ntiles, hist, 0);
+    scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
+    k_radix_scatter<false, kDigitKey, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+        src, nullptr, count, shift, dbits, ntiles, offs, dst, nullptr, nullptr, nullptr, 0, 0);
+    std::swap(src, dst);
+    if (launches) *launches += 5;
+  }
+  *result = src;
+  dfree(ctx, mem);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("partition: kernel launch failed: ") + cudaGetErrorString(e));
+    return LNE_ERR_CUDA;
+  }
+  return LNE_OK;
+}
+
 }  // namespace lne

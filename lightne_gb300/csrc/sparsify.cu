@@ -98,7 +98,7 @@ static constexpr int kMaxRMagic = 64;  // multipliers of r = 1..64 kept in share
 
 enum WalkPhase : int { kPhEff = 0, kPhR = 1, kPhK = 2, kPhW1 = 3, kPhW2 = 4 };
 
-template <bool SAMPLE>
+template <bool SAMPLE, bool HASHED>
 __global__ void __launch_bounds__(kWalkThreads, 6) k_walk(const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs,
                                                       const uint32_t* __restrict__ src, int64_t e0, int64_t e1,
                                                       SampleArgs a, unsigned long long* __restrict__ out_keys,
@@ -209,6 +209,7 @@ __global__ void __launch_bounds__(kWalkThreads, 6) k_walk(const Vertex* __restri
           if (end_walk) {
             const uint32_t lo = x < cur ? x : cur, hi = x < cur ? cur : x;
             key = ((uint64_t)lo << 32) + (uint64_t)hi;
+            if (HASHED) key = hash64_2(key);
             emit = true;
             sample_done = true;
           }
@@ -287,6 +288,178 @@ __global__ void k_insert(const unsigned long long* __restrict__ keys, const doub
       if (leader && !table_insert_add<false>(table, mask, key, 1.0, flags, (unsigned long long)__popc(same))) return;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Sliced aggregation (counts, one batch of samples).  The insert-add of
+// par_table only has to produce the multiset of (pair, count); where the
+// slot of a pair lies does not show in the output, which is sorted.  So the
+// sampler writes every key as h = hash64_2(key) (a bijection), the batch is
+// sorted by the top `sbits` bits of h (a few radix passes), and each slice
+// of 2^-sbits of the hash space -- a few thousand samples -- is counted by
+// one CTA in a shared-memory open-addressing table (linear probing on the
+// low bits of h, the same insert-or-add as par_table).  The occupied slots
+// are appended, with the key recovered by hash64_2_inv, as a dense
+// Slot[distinct] array that the trunc-log reads in place of the table.
+// No pair table is written or read in HBM.  If a slice has more distinct
+// pairs than its shared table holds, the slice kernel raises
+// kFlagSliceOverflow and the host reruns the batch through the pair table.
+// The all-ones word marks an empty shared slot: its hash preimage is a pair
+// with a vertex id above 2^31, which no graph here has.
+// ---------------------------------------------------------------------------
+static constexpr int kSliceThreads = 1024;
+static constexpr int kSliceSlotsMax = 16384;  // 192 KB of shared memory
+static constexpr int kSliceBitsMax = 16;
+
+__device__ __forceinline__ int64_t slice_of(unsigned long long h, int sbits) {
+  return sbits == 0 ? 0 : (int64_t)(h >> (64 - sbits));
+}
+
+// start[s] = first index of slice s in the sorted hashed keys, s = 0..nslices
+// (start[nslices] = count).
+__global__ void k_slice_bounds(const unsigned long long* __restrict__ hk, int64_t count, int sbits, int64_t nslices,
+                               int64_t* __restrict__ start) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s_cur = i < count ? slice_of(hk[i], sbits) : nslices;
+    const int64_t s_prev = i > 0 ? slice_of(hk[i - 1], sbits) : -1;
+    for (int64_t s = s_prev + 1; s <= s_cur; ++s) start[s] = i;
+  }
+}
+
+// One CTA per slice at a time (slices round-robin over the grid); adds the
+// slices' distinct pairs to *n_distinct and the samples counted to
+// *n_samples.  A slice's keys are loaded into registers (kSliceRegs per
+// thread, in chunks for larger slices) before the table is cleared, so the
+// global loads overlap the clearing; the occupied slots are found in
+// 32-slot chunks (one per warp in turn, conflict-free) whose occupancy
+// masks stay in registers between the count and the write.
+static constexpr int kSliceRegs = 8;
+static constexpr int kSliceMaskRegs = kSliceSlotsMax / 32 / (kSliceThreads / 32);  // 16
+
+__global__ void __launch_bounds__(kSliceThreads, 1) k_slice_count(const unsigned long long* __restrict__ hk,
+                                                                  const int64_t* __restrict__ start, int64_t nslices,
+                                                                  int slots_max, Slot* __restrict__ uniq,
+                                                                  unsigned long long* __restrict__ n_distinct,
+                                                                  unsigned long long* __restrict__ n_samples,
+                                                                  int* __restrict__ flags) {
+  extern __shared__ __align__(16) unsigned char slice_smem[];
+  unsigned long long* sk = reinterpret_cast<unsigned long long*>(slice_smem);
+  unsigned* sc = reinterpret_cast<unsigned*>(slice_smem + sizeof(unsigned long long) * slots_max);
+  __shared__ unsigned warp_tot[kSliceThreads / 32];
+  __shared__ unsigned long long blk_base;
+  __shared__ int blk_ovf;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nthr = blockDim.x, nwarps = nthr >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned long long my_samples = 0;
+  int64_t s = blockIdx.x;
+  int64_t b = s < nslices ? start[s] : 0, e = s < nslices ? start[s + 1] : 0;
+  for (; s < nslices; s += gridDim.x) {
+    // bounds of this CTA's next slice, loaded while this one is counted
+    const int64_t sn = s + gridDim.x;
+    const int64_t bn = sn < nslices ? start[sn] : 0, en = sn < nslices ? start[sn + 1] : 0;
+    if (e > b) {  // the same for every thread of the CTA
+      int slots = 64;
+      while (slots < slots_max && (int64_t)slots < (e - b) + (e - b) / 2) slots <<= 1;
+      const unsigned smask = (unsigned)slots - 1u;
+      unsigned long long reg[kSliceRegs];
+      int64_t c0 = b;
+      {
+        const int64_t i0 = c0 + (threadIdx.x & ~31) + lane;
+#pragma unroll
+        for (int k = 0; k < kSliceRegs; ++k) {
+          const int64_t i = i0 + (int64_t)k * nthr;
+          reg[k] = i < e ? hk[i] : kEmptyKey;
+        }
+      }
+      for (int i = threadIdx.x; i < slots; i += nthr) {
+        sk[i] = kEmptyKey;
+        sc[i] = 0u;
+      }
+      if (threadIdx.x == 0) blk_ovf = 0;
+      __syncthreads();
+      // insert-or-add; lanes holding the same pair are merged first
+      for (;;) {
+#pragma unroll
+        for (int k = 0; k < kSliceRegs; ++k) {
+          const unsigned long long h = reg[k];
+          const unsigned same = __match_any_sync(kFullMask, h);
+          if (h != kEmptyKey && (__ffs(same) - 1) == lane) {
+            const unsigned add = (unsigned)__popc(same);
+            unsigned pos = (unsigned)h & smask;
+            bool placed = false;
+            for (int p = 0; p < slots; ++p) {
+              unsigned long long kk = *reinterpret_cast<volatile unsigned long long*>(&sk[pos]);
+              if (kk == kEmptyKey) kk = atomicCAS(&sk[pos], kEmptyKey, h);
+              if (kk == kEmptyKey || kk == h) {
+                atomicAdd(&sc[pos], add);
+                placed = true;
+                break;
+              }
+              pos = (pos + 1u) & smask;
+            }
+            if (placed)
+              my_samples += add;
+            else
+              blk_ovf = 1;
+          }
+        }
+        c0 += (int64_t)kSliceRegs * nthr;
+        if (c0 >= e) break;  // the same for every thread
+        const int64_t i0 = c0 + (threadIdx.x & ~31) + lane;
+#pragma unroll
+        for (int k = 0; k < kSliceRegs; ++k) {
+          const int64_t i = i0 + (int64_t)k * nthr;
+          reg[k] = i < e ? hk[i] : kEmptyKey;
+        }
+      }
+      __syncthreads();
+      // occupied slots: 32-slot chunks, chunk c by warp c % nwarps
+      const int nchunk = slots >> 5;
+      unsigned mask[kSliceMaskRegs];
+      unsigned occ = 0;
+#pragma unroll
+      for (int q = 0; q < kSliceMaskRegs; ++q) {
+        const int c = wid + q * nwarps;
+        const bool in = c < nchunk;
+        mask[q] = __ballot_sync(kFullMask, in && sk[(in ? c : 0) * 32 + lane] != kEmptyKey);
+        occ += __popc(mask[q]);
+      }
+      if (lane == 0) warp_tot[wid] = occ;
+      __syncthreads();
+      unsigned before = 0, total = 0;
+      for (int w = 0; w < nwarps; ++w) {
+        const unsigned t = warp_tot[w];
+        if (w < wid) before += t;
+        total += t;
+      }
+      if (threadIdx.x == 0) {
+        blk_base = atomicAdd(n_distinct, (unsigned long long)total);
+        if (blk_ovf) atomicExch(flags + kFlagSliceOverflow, 1);
+      }
+      __syncthreads();
+      uint64_t pos = blk_base + before;
+#pragma unroll
+      for (int q = 0; q < kSliceMaskRegs; ++q) {
+        const int j = (wid + q * nwarps) * 32 + lane;
+        if ((mask[q] >> lane) & 1u)
+          uniq[pos + __popc(mask[q] & lt)] = Slot{hash64_2_inv(sk[j]), (unsigned long long)sc[j]};
+        pos += __popc(mask[q]);
+      }
+      __syncthreads();  // the table is cleared for the next slice
+    }
+    b = bn;
+    e = en;
+  }
+  for (int o = 16; o > 0; o >>= 1) my_samples += __shfl_down_sync(kFullMask, my_samples, o);
+  if (lane == 0 && my_samples) atomicAdd(n_samples, my_samples);
+}
+
+// Hashed keys back to pair keys, in place (the pair-table fallback).
+__global__ void k_unhash(unsigned long long* __restrict__ k, int64_t count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    k[i] = hash64_2_inv(k[i]);
 }
 
 // Sum of weights and number of occupied slots (PathEmbed.h:175-188).  Counts
@@ -518,11 +691,11 @@ namespace {
 
 struct Scratch {
   lne_ctx* ctx;
-  void* p[12] = {};
+  void* p[16] = {};
   int k = 0;
   explicit Scratch(lne_ctx* c) : ctx(c) {}
   int get(void** out, size_t bytes, const char* what) {
-    if (k == 12) {
+    if (k == 16) {
       set_error("lne_sparsify: scratch list full (internal)");
       return LNE_ERR_UNSUPPORTED;
     }
@@ -574,15 +747,14 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
 
   Scratch S(ctx);
   Events ev;
-  Slot* table = nullptr;
-  unsigned long long* counters = nullptr;  // [0] emitted [1] count sum [2] distinct [3] kept
+  Slot* table = nullptr;  // the pair table in HBM (allocated and cleared on first use)
+  Slot* uniq = nullptr;   // sliced aggregation: the distinct pairs with their counts
+  unsigned long long* counters = nullptr;  // [0] emitted [1] count sum [2] distinct [3] kept [4] items
   double* wsum = nullptr;
   int rc;
-  if ((rc = S.get((void**)&table, sizeof(Slot) * cap, "pair table"))) return rc;
   const int sum_blocks = 1024;
   if ((rc = S.get((void**)&counters, 64 + sizeof(double) * (sum_blocks + 1), "counters"))) return rc;
   wsum = (double*)((char*)counters + 64);
-  k_table_init<<<grid_for((int64_t)cap, 256, (int64_t)ctx->num_sms * 32), 256, 0, st>>>(table, cap);
   LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 64, st));
   LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, st));
 
@@ -605,42 +777,127 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   const uint64_t buf_keys = want_keys < max_keys ? want_keys : max_keys;
   const int64_t edges_per_batch = (int64_t)std::max<uint64_t>(1, buf_keys / per_edge);
   unsigned long long* keys = nullptr;
-  unsigned long long* keys2 = nullptr;  // counts: the batch reordered by table slice
+  unsigned long long* keys2 = nullptr;  // counts: the batch reordered by slice
   double* wts = nullptr;
   if ((rc = S.get((void**)&keys, sizeof(unsigned long long) * buf_keys, "sample buffer"))) return rc;
   if (p->sample && (rc = S.get((void**)&wts, sizeof(double) * buf_keys, "sample weights"))) return rc;
   if (!p->sample && (rc = S.get((void**)&keys2, sizeof(unsigned long long) * buf_keys, "partitioned samples")))
     return rc;
   int launches_sample = 0;
+  auto ensure_table = [&]() -> int {
+    if (table) return LNE_OK;
+    const int r = S.get((void**)&table, sizeof(Slot) * cap, "pair table");
+    if (r) return r;
+    k_table_init<<<grid_for((int64_t)cap, 256, (int64_t)ctx->num_sms * 32), 256, 0, st>>>(table, cap);
+    ++launches_sample;
+    return LNE_OK;
+  };
+  // Counts commute, so a batch is first grouped by the top 8 bits of its
+  // table slot: the inserts then sweep the table one slice (1/256 of it) at
+  // a time, and a slice's slots stay in L2 while its atomics land.  A
+  // smaller grid keeps the warps within a slice or two.
+  auto insert_counts = [&](const unsigned long long* in, unsigned long long* tmp, unsigned long long got) -> int {
+    int r = ensure_table();
+    if (r) return r;
+    if ((r = partition_by_slot(ctx, in, tmp, (int64_t)got, (int)bits, &launches_sample))) return r;
+    const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 8);
+    k_insert<false><<<iblocks, 256, 0, st>>>(tmp, nullptr, got, table, cap - 1, ctx->d_flags);
+    ++launches_sample;
+    return LNE_OK;
+  };
+
+  // Sliced aggregation (see k_slice_count) for counts when the samples fit
+  // one batch and the shared-memory table fits the device.
+  const int slots_max = std::min(ctx->sparsify_slice_slots, kSliceSlotsMax);
+  const size_t slice_smem = (size_t)slots_max * (sizeof(unsigned long long) + sizeof(unsigned));
+  const bool sliced_try = !p->sample && slots_max > 0 && want_keys <= max_keys && slice_smem + 1024 <= ctx->smem_optin;
+  bool sliced = false;
   unsigned long long emitted_total = 0;
-  for (int64_t eb = 0; eb < m_dir; eb += edges_per_batch) {
-    const int64_t ee = std::min<int64_t>(m_dir, eb + edges_per_batch);
-    LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 8, st));
-    const unsigned wblocks = (unsigned)((ee - eb + kWalkThreads - 1) / kWalkThreads);
-    if (p->sample)
-      k_walk<true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts, counters,
-                                                     buf_keys, ctx->d_flags);
-    else
-      k_walk<false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts, counters,
-                                                      buf_keys, ctx->d_flags);
+  if (sliced_try) {
+    const unsigned wblocks = (unsigned)((m_dir + kWalkThreads - 1) / kWalkThreads);
+    k_walk<false, true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, 0, m_dir, a, keys, nullptr,
+                                                          counters, buf_keys, ctx->d_flags);
+    ++launches_sample;
     unsigned long long got = 0;
     LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));
     LNE_CUDA_TRY(cudaStreamSynchronize(st));
     if (got > buf_keys) got = buf_keys;  // overflow is flagged and reported below
-    if (p->sample) {
-      const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 32);
-      k_insert<true><<<iblocks, 256, 0, st>>>(keys, wts, got, table, cap - 1, ctx->d_flags);
-    } else {
-      // Counts commute, so the batch is first grouped by the top 8 bits of
-      // its table slot: the inserts then sweep the table one slice (1/256
-      // of it) at a time, and a slice's slots stay in L2 while its atomics
-      // land.  A smaller grid keeps the warps within a slice or two.
-      if ((rc = partition_by_slot(ctx, keys, keys2, (int64_t)got, (int)bits, &launches_sample))) return rc;
-      const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 8);
-      k_insert<false><<<iblocks, 256, 0, st>>>(keys2, wts, got, table, cap - 1, ctx->d_flags);
+    emitted_total = got;
+    // slices of at most a quarter (half, with 2^16 slices) of the shared table
+    int sbits = ctx->sparsify_slice_bits;
+    if (sbits < 0) {
+      sbits = 0;
+      while (sbits < kSliceBitsMax && (got >> sbits) > (uint64_t)slots_max / 4) ++sbits;
     }
-    emitted_total += got;
-    launches_sample += 2;
+    const bool fits = ctx->sparsify_slice_bits >= 0 || (got >> sbits) <= (uint64_t)slots_max / 2;
+    unsigned long long* hk = keys;
+    if (fits) {
+      if ((rc = partition_by_top_bits(ctx, keys, keys2, (int64_t)got, sbits, &hk, &launches_sample))) return rc;
+      const int64_t nslices = (int64_t)1 << sbits;
+      int64_t* starts = nullptr;
+      if ((rc = S.get((void**)&starts, sizeof(int64_t) * (nslices + 1), "slice starts"))) return rc;
+      if ((rc = S.get((void**)&uniq, sizeof(Slot) * std::max<unsigned long long>(got, 1), "distinct pairs")))
+        return rc;
+      k_slice_bounds<<<grid_for((int64_t)got + 1, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(hk, (int64_t)got,
+                                                                                                  sbits, nslices,
+                                                                                                  starts);
+      LNE_CUDA_TRY(cudaFuncSetAttribute(k_slice_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)slice_smem));
+      const unsigned sgrid = (unsigned)std::min<int64_t>(nslices, ctx->num_sms);
+      k_slice_count<<<sgrid, kSliceThreads, slice_smem, st>>>(hk, starts, nslices, slots_max, uniq, counters + 2,
+                                                              counters + 1, ctx->d_flags);
+      launches_sample += 2;
+      unsigned long long sc[2] = {0, 0};  // samples counted, distinct pairs
+      int fl[kFlagWords];
+      LNE_CUDA_TRY(cudaMemcpyAsync(sc, counters + 1, sizeof(sc), cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaStreamSynchronize(st));
+      LNE_CUDA_TRY(cudaGetLastError());
+      S.release(starts);
+      if (!fl[kFlagSliceOverflow] && sc[0] != got) {
+        set_error("lne_sparsify: sliced aggregation lost samples (internal error)");
+        return LNE_ERR_UNSUPPORTED;
+      }
+      // Above 90% of the pair table's capacity the table decides whether
+      // the reference's table would fill: rerun through it.
+      sliced = !fl[kFlagSliceOverflow] && sc[1] * 10 <= (unsigned long long)cap * 9;
+      if (!sliced) {
+        S.release(uniq);
+        uniq = nullptr;
+        LNE_CUDA_TRY(cudaMemsetAsync(counters + 1, 0, 16, st));
+        LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags + kFlagSliceOverflow, 0, sizeof(int), st));
+      }
+    }
+    if (!sliced) {
+      k_unhash<<<grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(hk, (int64_t)got);
+      ++launches_sample;
+      if ((rc = insert_counts(hk, hk == keys ? keys2 : keys, got))) return rc;
+    }
+  } else {
+    if ((rc = ensure_table())) return rc;
+    for (int64_t eb = 0; eb < m_dir; eb += edges_per_batch) {
+      const int64_t ee = std::min<int64_t>(m_dir, eb + edges_per_batch);
+      LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 8, st));
+      const unsigned wblocks = (unsigned)((ee - eb + kWalkThreads - 1) / kWalkThreads);
+      if (p->sample)
+        k_walk<true, false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts,
+                                                              counters, buf_keys, ctx->d_flags);
+      else
+        k_walk<false, false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts,
+                                                               counters, buf_keys, ctx->d_flags);
+      ++launches_sample;
+      unsigned long long got = 0;
+      LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaStreamSynchronize(st));
+      if (got > buf_keys) got = buf_keys;  // overflow is flagged and reported below
+      if (p->sample) {
+        const unsigned iblocks = grid_for((int64_t)got, 256, (int64_t)ctx->num_sms * 32);
+        k_insert<true><<<iblocks, 256, 0, st>>>(keys, wts, got, table, cap - 1, ctx->d_flags);
+        ++launches_sample;
+      } else if ((rc = insert_counts(keys, keys2, got))) {
+        return rc;
+      }
+      emitted_total += got;
+    }
   }
   LNE_CUDA_TRY(cudaGetLastError());
   S.release(keys);
@@ -648,13 +905,14 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   if (wts) S.release(wts);
   cudaEventRecord(ev.e[1], st);
 
-  const unsigned tgrid = grid_for((int64_t)cap, 256, (int64_t)ctx->num_sms * 16);
   const int sgrid = sum_blocks;
-  if (p->sample)
-    k_table_sum<true><<<sgrid, 256, 0, st>>>(table, cap, counters + 1, counters + 2, wsum);
-  else
-    k_table_sum<false><<<sgrid, 256, 0, st>>>(table, cap, counters + 1, counters + 2, wsum);
-  k_sum_blocks<<<1, 32, 0, st>>>(wsum, sgrid, wsum + sum_blocks);
+  if (!sliced) {
+    if (p->sample)
+      k_table_sum<true><<<sgrid, 256, 0, st>>>(table, cap, counters + 1, counters + 2, wsum);
+    else
+      k_table_sum<false><<<sgrid, 256, 0, st>>>(table, cap, counters + 1, counters + 2, wsum);
+    k_sum_blocks<<<1, 32, 0, st>>>(wsum, sgrid, wsum + sum_blocks);
+  }
   unsigned long long h_cnt[3] = {0, 0, 0};
   LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 8, st));
   double h_w = 0.0;
@@ -698,15 +956,21 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   if ((rc = S.get((void**)&ivals, sizeof(uint32_t) * max_items, "csr item values"))) return rc;
   if ((rc = dalloc(ctx, (void**)&row_ptr, sizeof(int64_t) * (n + 1), "row_ptr"))) return rc;
   LNE_CUDA_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(unsigned long long) * n, st));
+  // the trunc-log reads the pair table, or the dense distinct pairs of the
+  // sliced aggregation (every slot occupied)
+  const Slot* tsrc = sliced ? uniq : table;
+  const uint64_t tcap = sliced ? (uint64_t)h_cnt[2] : cap;
+  const unsigned tgrid = grid_for((int64_t)tcap, 256, (int64_t)ctx->num_sms * 16);
   if (p->sample)
-    k_trunclog<true><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper,
+    k_trunclog<true><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
                                             (const LogTable*)ctx->log_table, rowcnt, counters + 3, counters + 4,
                                             cbits, max_items, ikeys, ivals, ctx->d_flags);
   else
-    k_trunclog<false><<<tgrid, 256, 0, st>>>(table, cap, g->vdata, factor, p->upper,
+    k_trunclog<false><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
                                              (const LogTable*)ctx->log_table, rowcnt, counters + 3, counters + 4,
                                              cbits, max_items, ikeys, ivals, ctx->d_flags);
-  S.release(table);
+  if (table) S.release(table);
+  if (uniq) S.release(uniq);
   cudaEventRecord(ev.e[2], st);
   scan_exclusive_i64((const int64_t*)rowcnt, row_ptr, n, scan_tmp, st);
   int64_t nnz = 0;
@@ -739,7 +1003,8 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     dfree(ctx, val);
     return rc;
   }
-  int launches = 7 + launches_sample;  // init, table sum, block sum, trunc-log, 3 scan + walk/insert
+  // sampling and aggregation, [table sum, block sum,] trunc-log, 3 scan
+  int launches = launches_sample + (sliced ? 0 : 2) + 4;
   if ((rc = radix_sort_pairs_to_csr(ctx, ikeys, ivals, tkeys, tvals, nnz, 2 * cbits, ((1ULL << cbits) - 1), col,
                                     val, &launches))) {
     dfree(ctx, row_ptr);
@@ -775,6 +1040,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     cudaEventElapsedTime(&stats->ms_trunclog, ev.e[1], ev.e[2]);
     cudaEventElapsedTime(&stats->ms_csr, ev.e[2], ev.e[3]);
     stats->kernel_launches = launches;
+    stats->sliced = sliced ? 1 : 0;
   }
   lne_csr* c = new lne_csr();
   c->n = n;

@@ -22,11 +22,30 @@ static void spmm_launch(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X,
                                                                           epi);
 }
 
+// Copies columns [v0, v0 + C) (16-byte vectors) of the x_rows rows of X
+// into a dense x_rows x C array.
+static __global__ void k_slab_copy(const uint4* __restrict__ X, int64_t ldv, int64_t v0, int64_t x_rows, int C,
+                            uint4* __restrict__ out) {
+  const int64_t total = x_rows * C;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / C;
+    const int c = (int)(i - r * C);
+    out[i] = __ldg(X + r * ldv + v0 + c);
+  }
+}
+
+// A narrow slab after the first (the tail columns of a 144-wide operand)
+// is gathered from a dense copy of its columns when that copy is at most
+// this size: rows of the copy are 32-64 bytes instead of one 128-byte line
+// per row of X, so the copy stays in L2 while the slab's gathers run.
+static constexpr int64_t kSlabCopyMaxBytes = (int64_t)96 << 20;
+
 // Runs Y-epilogue(A * X) over all rows.  X rows: ldx elements, 16-byte
 // aligned; d columns are produced (the epilogue sees element offsets).
+// x_rows (the rows of X; 0 if unknown) enables the tail-slab copies.
 template <typename XT, class Rows, class Epi>
 static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int64_t ldx, int64_t d, const Epi& epi,
-                    int* launches = nullptr) {
+                    int* launches = nullptr, int64_t x_rows = 0) {
   constexpr int E = Vec16<XT>::E;
   const int64_t c_total = (d + E - 1) / E;
   float* partial = nullptr;
@@ -46,21 +65,37 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
       if ((rc = dalloc(ctx, (void**)&partial, sizeof(float) * plan.n_chunks * w, "spmm partials"))) return rc;
     }
     const XT* Xs = X + c_off * E;
+    int64_t ldxs = ldx;
+    XT* slab = nullptr;
+    if (c_off > 0 && x_rows > 0 && x_rows * C * 16 <= kSlabCopyMaxBytes) {
+      if ((rc = dalloc(ctx, (void**)&slab, (size_t)(x_rows * C * 16), "spmm slab copy"))) {
+        if (partial) dfree(ctx, partial);
+        return rc;
+      }
+      const int64_t nv = x_rows * C;
+      int64_t blocks = (nv + 255) / 256;
+      if (blocks > (int64_t)ctx->num_sms * 16) blocks = (int64_t)ctx->num_sms * 16;
+      k_slab_copy<<<(unsigned)blocks, 256, 0, ctx->stream>>>(reinterpret_cast<const uint4*>(X), ldx / E, c_off, x_rows,
+                                                             C, reinterpret_cast<uint4*>(slab));
+      ++nl;
+      Xs = slab;
+      ldxs = (int64_t)C * E;
+    }
     const int e_base = (int)(c_off * E);
     if (C <= 2)
-      spmm_launch<XT, 2, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+      spmm_launch<XT, 2, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else if (C <= 4)
-      spmm_launch<XT, 4, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+      spmm_launch<XT, 4, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else if (C <= 8)
-      spmm_launch<XT, 8, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+      spmm_launch<XT, 8, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else if (C <= 16)
-      spmm_launch<XT, 16, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+      spmm_launch<XT, 16, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else if (C <= 32)
-      spmm_launch<XT, 32, 1>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+      spmm_launch<XT, 32, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else if (C <= 64)
-      spmm_launch<XT, 32, 2>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+      spmm_launch<XT, 32, 2>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else
-      spmm_launch<XT, 32, 4>(ctx, R, plan, Xs, ldx, C, partial, ldp, e_base, epi);
+      spmm_launch<XT, 32, 4>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     ++nl;
     if (plan.n_long > 0) {
       int64_t blocks = (plan.n_long + 7) / 8;
@@ -68,6 +103,7 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
       k_spmm_finish<Epi><<<(unsigned)blocks, 256, 0, ctx->stream>>>(plan, partial, ldp, (int)ldp, e_base, epi);
       ++nl;
     }
+    if (slab) dfree(ctx, slab);
     c_off += C;
   }
   if (partial) dfree(ctx, partial);
@@ -96,7 +132,7 @@ static int spmm_csr_panels(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ldx, i
     if ((rc = build_plan_csr(ctx, A))) return rc;
     CsrRows R{A->row_ptr, A->col, A->val};
     epi.add = false;
-    return spmm_run<XT>(ctx, R, A->plan, X, ldx, d, epi, launches);
+    return spmm_run<XT>(ctx, R, A->plan, X, ldx, d, epi, launches, A->n);
   }
   const int64_t pw = std::max<int64_t>(1, ctx->spmm_panel_bytes / row_bytes);
   if ((rc = build_panels(ctx, A, pw))) return rc;

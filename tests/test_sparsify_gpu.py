@@ -52,6 +52,48 @@ def test_device_matches_reference_golden(ctx, path):
     assert st["nnz"] == z["row_ptr"][-1]
 
 
+# Aggregation of the samples: the sliced shared-memory count (default), the
+# pair table in HBM (slots = 0), a single 64-slot slice that overflows and
+# reruns through the pair table, and forced slice counts.
+AGGREGATION = {"table": (0, -1), "overflow64": (64, 0), "bits1": (256, 1), "bits9": (16384, 9)}
+
+
+@pytest.mark.parametrize("mode", sorted(AGGREGATION))
+def test_aggregation_paths_match_reference_golden(ctx, mode):
+    slots, bits = AGGREGATION[mode]
+    ctx.set_sparsify_slices(slots, bits)
+    try:
+        for path in CASES:
+            z = np.load(path)
+            prm = json.loads(str(z["params"]))
+            if prm["sample"] != 0:
+                continue
+            got, st = device_sparsify(ctx, z["offsets"], z["nbrs"], prm)
+            assert_csr_equal(got, (z["row_ptr"], z["col"], z["val"]))
+            if mode == "table":
+                assert st["sliced"] == 0
+            elif mode == "overflow64":  # one slice of 64 slots
+                assert st["sliced"] == (1 if st["distinct"] <= 64 else 0), (path, st["distinct"])
+            elif mode == "bits1":  # two slices of 256 slots
+                if st["distinct"] > 512:
+                    assert st["sliced"] == 0
+            else:
+                assert st["sliced"] == 1
+    finally:
+        ctx.set_sparsify_slices()
+
+
+def test_default_aggregation_is_sliced_for_counts(ctx):
+    z = np.load(os.path.join(GOLDEN, "sparsify_chunglu300.npz"))
+    prm = json.loads(str(z["params"]))
+    _, st = device_sparsify(ctx, z["offsets"], z["nbrs"], prm)
+    assert st["sliced"] == 1
+    z = np.load(os.path.join(GOLDEN, "sparsify_chunglu300_sample1.npz"))
+    prm = json.loads(str(z["params"]))
+    _, st = device_sparsify(ctx, z["offsets"], z["nbrs"], prm)
+    assert st["sliced"] == 0  # weights (-sample 1) always go through the pair table
+
+
 def test_device_matches_oracle_config1(ctx):
     # config 1: Chung-Lu n=10,312, m=333,983, T=10, samples = 20*T*m (ratio as float)
     off, nbrs = graphs.chung_lu(10312, 333983, 2.1, seed=1)
@@ -59,11 +101,20 @@ def test_device_matches_oracle_config1(ctx):
     prm = dict(seed=1, walk_len=10, tablesz=13_500_000, negative=1, sample=0, sample_ratio=ratio, mem_ratio=1.0,
                upper=0)
     got, st = device_sparsify(ctx, off, nbrs, prm)
+    assert st["sliced"] == 1
     ref, pst = port.sparsify(off, nbrs, 1, walk_len=10, tablesz=13_500_000, sample_ratio=ratio)
     assert st["samples_emitted"] == pst["samples"]
     assert st["distinct"] == pst["distinct"]
     assert st["m_exact"] == pst["M_exact"] and st["factor"] == pst["factor"]
     assert_csr_equal(got, ref)
+    # the same matrix through the pair table in HBM
+    ctx.set_sparsify_slices(0)
+    try:
+        got2, st2 = device_sparsify(ctx, off, nbrs, prm)
+    finally:
+        ctx.set_sparsify_slices()
+    assert st2["sliced"] == 0 and st2["distinct"] == st["distinct"]
+    assert_csr_equal(got2, ref)
 
 
 def test_device_matches_oracle_midsize_variants(ctx):
