@@ -70,7 +70,7 @@ int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes);
  * the reference always inserts into par_table, LightNE/par_table.h:86-109).
  * With counts (-sample 0) and one batch of samples, lne_sparsify counts the
  * pairs slice by slice in shared-memory tables of `slots` entries (a power
- * of two in [64, 16384]; default 16384) over 2^slice_bits slices of the
+ * of two in [64, 8192]; default 8192) over 2^slice_bits slices of the
  * hash space (-1, the default: chosen from the sample count; at most 16),
  * and falls back to the pair table in HBM when a slice overflows.
  * slots = 0 always uses the pair table.  The output is the same either way. */

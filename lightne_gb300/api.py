@@ -43,7 +43,7 @@ class Context:
     def synchronize(self) -> None:
         check(_lib.load().lne_ctx_synchronize(self.handle))
 
-    def set_sparsify_slices(self, slots: int = 16384, slice_bits: int = -1) -> None:
+    def set_sparsify_slices(self, slots: int = 8192, slice_bits: int = -1) -> None:
         """Shared-memory table size per slice of the sliced pair aggregation
         (0: always the pair table in HBM) and its slice bits (-1: automatic)."""
         check(_lib.load().lne_ctx_set_sparsify_slices(self.handle, slots, slice_bits))

@@ -257,8 +257,8 @@ int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes) {
 
 int lne_ctx_set_sparsify_slices(lne_ctx* ctx, int32_t slots, int32_t slice_bits) {
   LNE_CHECK_ARG(ctx != nullptr, "lne_ctx_set_sparsify_slices: ctx is NULL");
-  LNE_CHECK_ARG(slots == 0 || (slots >= 64 && slots <= 16384 && (slots & (slots - 1)) == 0),
-                "lne_ctx_set_sparsify_slices: slots must be 0 or a power of two in [64, 16384]");
+  LNE_CHECK_ARG(slots == 0 || (slots >= 64 && slots <= 8192 && (slots & (slots - 1)) == 0),
+                "lne_ctx_set_sparsify_slices: slots must be 0 or a power of two in [64, 8192]");
   LNE_CHECK_ARG(slice_bits >= -1 && slice_bits <= 16, "lne_ctx_set_sparsify_slices: slice_bits must be in [-1, 16]");
   ctx->sparsify_slice_slots = slots;
   ctx->sparsify_slice_bits = slice_bits;

@@ -65,7 +65,7 @@ struct lne_ctx {
   // Sliced aggregation of the sparsifier's samples (counts, one batch):
   // shared-memory table size per slice (0: always the pair table in HBM)
   // and the number of slice bits (-1: chosen from the sample count).
-  int sparsify_slice_slots = 16384;
+  int sparsify_slice_slots = 8192;
   int sparsify_slice_bits = -1;
 };
 

@@ -307,8 +307,8 @@ __global__ void k_insert(const unsigned long long* __restrict__ keys, const doub
 // The all-ones word marks an empty shared slot: its hash preimage is a pair
 // with a vertex id above 2^31, which no graph here has.
 // ---------------------------------------------------------------------------
-static constexpr int kSliceThreads = 1024;
-static constexpr int kSliceSlotsMax = 16384;  // 192 KB of shared memory
+static constexpr int kSliceThreads = 512;
+static constexpr int kSliceSlotsMax = 8192;  // 96 KB of shared memory: two CTAs per SM
 static constexpr int kSliceBitsMax = 16;
 
 __device__ __forceinline__ int64_t slice_of(unsigned long long h, int sbits) {
@@ -327,17 +327,19 @@ __global__ void k_slice_bounds(const unsigned long long* __restrict__ hk, int64_
   }
 }
 
-// One CTA per slice at a time (slices round-robin over the grid); adds the
-// slices' distinct pairs to *n_distinct and the samples counted to
-// *n_samples.  A slice's keys are loaded into registers (kSliceRegs per
-// thread, in chunks for larger slices) before the table is cleared, so the
-// global loads overlap the clearing; the occupied slots are found in
-// 32-slot chunks (one per warp in turn, conflict-free) whose occupancy
-// masks stay in registers between the count and the write.
-static constexpr int kSliceRegs = 8;
+// One CTA per slice at a time (slices round-robin over the grid, two CTAs
+// per SM so that one counts while the other waits); adds the slices'
+// distinct pairs to *n_distinct and the samples counted to *n_samples.  A
+// slice's keys are loaded into registers (kSliceRegs per thread, in chunks
+// for larger slices) before the table is cleared, so the global loads
+// overlap the clearing; every lane inserts its own key (equal keys meet in
+// the table: the CAS admits one, the others add).  The occupied slots are
+// found in 32-slot chunks (one per warp in turn, conflict-free) whose
+// occupancy masks stay in registers between the count and the write.
+static constexpr int kSliceRegs = 12;
 static constexpr int kSliceMaskRegs = kSliceSlotsMax / 32 / (kSliceThreads / 32);  // 16
 
-__global__ void __launch_bounds__(kSliceThreads, 1) k_slice_count(const unsigned long long* __restrict__ hk,
+__global__ void __launch_bounds__(kSliceThreads, 2) k_slice_count(const unsigned long long* __restrict__ hk,
                                                                   const int64_t* __restrict__ start, int64_t nslices,
                                                                   int slots_max, Slot* __restrict__ uniq,
                                                                   unsigned long long* __restrict__ n_distinct,
@@ -384,9 +386,8 @@ __global__ void __launch_bounds__(kSliceThreads, 1) k_slice_count(const unsigned
 #pragma unroll
         for (int k = 0; k < kSliceRegs; ++k) {
           const unsigned long long h = reg[k];
-          const unsigned same = __match_any_sync(kFullMask, h);
-          if (h != kEmptyKey && (__ffs(same) - 1) == lane) {
-            const unsigned add = (unsigned)__popc(same);
+          if (h != kEmptyKey) {
+            const unsigned add = 1u;
             unsigned pos = (unsigned)h & smask;
             bool placed = false;
             for (int p = 0; p < slots; ++p) {
@@ -823,13 +824,13 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     LNE_CUDA_TRY(cudaStreamSynchronize(st));
     if (got > buf_keys) got = buf_keys;  // overflow is flagged and reported below
     emitted_total = got;
-    // slices of at most a quarter (half, with 2^16 slices) of the shared table
+    // slices of at most a quarter (5/8, with 2^16 slices) of the shared table
     int sbits = ctx->sparsify_slice_bits;
     if (sbits < 0) {
       sbits = 0;
       while (sbits < kSliceBitsMax && (got >> sbits) > (uint64_t)slots_max / 4) ++sbits;
     }
-    const bool fits = ctx->sparsify_slice_bits >= 0 || (got >> sbits) <= (uint64_t)slots_max / 2;
+    const bool fits = ctx->sparsify_slice_bits >= 0 || (got >> sbits) <= (uint64_t)slots_max * 5 / 8;
     unsigned long long* hk = keys;
     if (fits) {
       if ((rc = partition_by_top_bits(ctx, keys, keys2, (int64_t)got, sbits, &hk, &launches_sample))) return rc;
@@ -842,7 +843,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
                                                                                                   sbits, nslices,
                                                                                                   starts);
       LNE_CUDA_TRY(cudaFuncSetAttribute(k_slice_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)slice_smem));
-      const unsigned sgrid = (unsigned)std::min<int64_t>(nslices, ctx->num_sms);
+      const unsigned sgrid = (unsigned)std::min<int64_t>(nslices, 2 * (int64_t)ctx->num_sms);
       k_slice_count<<<sgrid, kSliceThreads, slice_smem, st>>>(hk, starts, nslices, slots_max, uniq, counters + 2,
                                                               counters + 1, ctx->d_flags);
       launches_sample += 2;

@@ -55,7 +55,7 @@ def test_device_matches_reference_golden(ctx, path):
 # Aggregation of the samples: the sliced shared-memory count (default), the
 # pair table in HBM (slots = 0), a single 64-slot slice that overflows and
 # reruns through the pair table, and forced slice counts.
-AGGREGATION = {"table": (0, -1), "overflow64": (64, 0), "bits1": (256, 1), "bits9": (16384, 9)}
+AGGREGATION = {"table": (0, -1), "overflow64": (64, 0), "bits1": (256, 1), "bits9": (8192, 9)}
 
 
 @pytest.mark.parametrize("mode", sorted(AGGREGATION))
