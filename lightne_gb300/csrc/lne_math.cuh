@@ -93,12 +93,22 @@ LNE_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
   return (uint64_t)(((unsigned __int128)a * b) >> 64);
 #endif
 }
+// The remainder x - q d is below d < 2^32, so it is exact modulo 2^32 and
+// only the low 32 bits of q = y >> sh2 (sh2 <= 31) are needed: one funnel
+// shift instead of a 64-bit variable shift, one 32-bit multiply-add.
+LNE_HD uint32_t shr64_lo32(uint64_t y, uint32_t sh) {
+#ifdef __CUDA_ARCH__
+  return __funnelshift_r((uint32_t)y, (uint32_t)(y >> 32), sh);
+#else
+  return (uint32_t)(y >> sh);
+#endif
+}
 LNE_HD uint32_t gm_mod(uint64_t x, uint32_t d, uint64_t magic) {
   const uint32_t l = ceil_log2_u32(d);
   const uint32_t sh1 = l < 1 ? l : 1u, sh2 = l > 0 ? l - 1 : 0u;
   const uint64_t t1 = umulhi64(magic, x);
-  const uint64_t q = (t1 + ((x - t1) >> sh1)) >> sh2;
-  return (uint32_t)(x - q * (uint64_t)d);
+  const uint64_t y = t1 + ((x - t1) >> sh1);
+  return (uint32_t)x - shr64_lo32(y, sh2) * d;
 }
 
 // ---------------------------------------------------------------------------

@@ -98,7 +98,7 @@ static constexpr int kMaxRMagic = 64;  // multipliers of r = 1..64 kept in share
 
 enum WalkPhase : int { kPhEff = 0, kPhR = 1, kPhK = 2, kPhW1 = 3, kPhW2 = 4 };
 
-template <bool SAMPLE, bool HASHED>
+template <bool SAMPLE>
 __global__ void __launch_bounds__(kWalkThreads, 6) k_walk(const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs,
                                                       const uint32_t* __restrict__ src, int64_t e0, int64_t e1,
                                                       SampleArgs a, unsigned long long* __restrict__ out_keys,
@@ -209,7 +209,6 @@ __global__ void __launch_bounds__(kWalkThreads, 6) k_walk(const Vertex* __restri
           if (end_walk) {
             const uint32_t lo = x < cur ? x : cur, hi = x < cur ? cur : x;
             key = ((uint64_t)lo << 32) + (uint64_t)hi;
-            if (HASHED) key = hash64_2(key);
             emit = true;
             sample_done = true;
           }
@@ -264,6 +263,128 @@ __global__ void __launch_bounds__(kWalkThreads, 6) k_walk(const Vertex* __restri
       } else {
         atomicExch(flags + kFlagSortOverflow, 1);
       }
+    }
+  }
+}
+
+// The sampler for counts (-sample 0), the same draws and walks as k_walk
+// with the per-draw state update written as selects rather than branches:
+// the lanes of a warp sit in different phases (r, k, walk on u's side, walk
+// on v's side), and branches per phase ran each phase's code in turn at
+// about half the lanes.  Here every lane runs the same instructions; only
+// the neighbour load (walk phases) and the vertex-record load (a walk that
+// goes on) are predicated.  HASHED writes hash64_2(key) instead of the key.
+template <bool HASHED>
+__global__ void __launch_bounds__(kWalkThreads, 6) k_walk_counts(
+    const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs, const uint32_t* __restrict__ src, int64_t e0,
+    int64_t e1, SampleArgs a, unsigned long long* __restrict__ out_keys, unsigned long long* __restrict__ out_count,
+    uint64_t out_cap, int* flags) {
+  __shared__ unsigned long long qk[kWalkThreads / 32][kQueue];
+  __shared__ unsigned long long rmag[kMaxRMagic + 1];
+  for (int i = threadIdx.x; i <= kMaxRMagic; i += blockDim.x) rmag[i] = gm_magic(i > 0 ? (uint32_t)i : 1u);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t e = e0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool active = e < e1;
+  uint32_t u = 0, v = 0, x = 0, left1 = 0, left2 = 0, r = 1;
+  uint32_t cur_off = 0, div = 1;
+  uint64_t mag = 1;
+  uint4 vu = make_uint4(0, 1, 1, 0), vv = make_uint4(0, 1, 1, 0);
+  uint64_t s = 0, todo = 0;
+  int phase = kPhR;
+  if (active) {
+    u = __ldg(src + e);
+    v = __ldg(nbrs + e);
+    vu = __ldg(reinterpret_cast<const uint4*>(vd + u));
+    vv = __ldg(reinterpret_cast<const uint4*>(vd + v));
+    s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
+    todo = a.exp_rv;
+    if (a.use_frac) todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
+    active = todo > 0;
+    div = (uint32_t)a.walk_len;
+    mag = a.walk_magic;
+  }
+  const uint32_t T = (uint32_t)a.walk_len;
+  int qlen = 0;  // warp-uniform
+  while (__any_sync(kFullMask, active)) {
+    const uint64_t rnd = rng_draw(s);
+    const uint32_t m = gm_mod(rnd, div, mag);
+    const bool isR = phase == kPhR, isK = phase == kPhK, isW1 = phase == kPhW1;
+    const bool isW = phase >= kPhW1;
+    uint32_t nxt = 0;
+    if (active && isW) nxt = __ldg(nbrs + cur_off + m);
+    // position reached by this draw (k: the walk on u's side starts at u)
+    // and the steps left on each side
+    const uint32_t pos = isW ? nxt : u;
+    const uint32_t l1 = isK ? m : (isW1 ? left1 - 1u : left1);
+    const uint32_t l2 = isK ? r - m - 1u : (isW1 || isR ? left2 : left2 - 1u);
+    const bool side_u = isK || isW1;
+    const bool go_u = side_u && l1 > 0;             // walk on from pos, u's side
+    const bool to_v = side_u && l1 == 0 && l2 > 0;  // u's side done: walk from v
+    const bool go_v = !side_u && !isR && l2 > 0;    // walk on from pos, v's side
+    const bool end = !isR && !go_u && !to_v && !go_v;
+    const uint32_t xn = (side_u && l1 == 0) ? pos : x;
+    const uint32_t eb = side_u ? v : pos;
+    uint4 rec = to_v ? vv : vu;
+    if (active && isW && (go_u || go_v)) rec = __ldg(reinterpret_cast<const uint4*>(vd + pos));
+    const uint32_t rn = m + 1u;  // r from the first draw of a sample
+    const bool emit = active && end;
+    unsigned long long key = 0;
+    if (emit) {
+      const uint32_t lo = xn < eb ? xn : eb, hi = xn < eb ? eb : xn;
+      key = ((uint64_t)lo << 32) + (uint64_t)hi;
+      if (HASHED) key = hash64_2(key);
+    }
+    // next state
+    const uint64_t rmg = rmag[rn <= (uint32_t)kMaxRMagic ? rn : 0u];
+    x = xn;
+    left1 = l1;
+    left2 = l2;
+    r = isR ? rn : r;
+    if (isR) {
+      phase = kPhK;
+      div = rn;
+      mag = rn <= (uint32_t)kMaxRMagic ? rmg : gm_magic(rn);
+    } else if (end) {
+      phase = kPhR;
+      div = T;
+      mag = a.walk_magic;
+    } else {
+      phase = go_u ? kPhW1 : kPhW2;
+      cur_off = rec.x;
+      div = rec.y;
+      mag = ((uint64_t)rec.w << 32) | rec.z;
+      if (div == 0) active = false;  // unreachable for a validated (symmetric) graph
+    }
+    if (emit && --todo == 0) active = false;
+    // stage this iteration's keys in the warp queue
+    const unsigned em = __ballot_sync(kFullMask, emit);
+    if (emit) qk[wid][qlen + __popc(em & ((1u << lane) - 1))] = key;
+    qlen += __popc(em);
+    __syncwarp();
+    if (qlen >= 32) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(out_count, 32ULL);
+      base = __shfl_sync(kFullMask, base, 0);
+      if (base + 32 <= out_cap)
+        out_keys[base + lane] = qk[wid][lane];
+      else if (lane == 0)
+        atomicExch(flags + kFlagSortOverflow, 1);
+      __syncwarp();
+      if (lane < qlen - 32) qk[wid][lane] = qk[wid][32 + lane];
+      qlen -= 32;
+      __syncwarp();
+    }
+  }
+  if (qlen > 0) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(out_count, (unsigned long long)qlen);
+    base = __shfl_sync(kFullMask, base, 0);
+    if (lane < qlen) {
+      if (base + lane < out_cap)
+        out_keys[base + lane] = qk[wid][lane];
+      else
+        atomicExch(flags + kFlagSortOverflow, 1);
     }
   }
 }
@@ -816,8 +937,8 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   unsigned long long emitted_total = 0;
   if (sliced_try) {
     const unsigned wblocks = (unsigned)((m_dir + kWalkThreads - 1) / kWalkThreads);
-    k_walk<false, true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, 0, m_dir, a, keys, nullptr,
-                                                          counters, buf_keys, ctx->d_flags);
+    k_walk_counts<true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, 0, m_dir, a, keys, counters,
+                                                          buf_keys, ctx->d_flags);
     ++launches_sample;
     unsigned long long got = 0;
     LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));
@@ -880,11 +1001,11 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
       LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 8, st));
       const unsigned wblocks = (unsigned)((ee - eb + kWalkThreads - 1) / kWalkThreads);
       if (p->sample)
-        k_walk<true, false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts,
+        k_walk<true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts,
                                                               counters, buf_keys, ctx->d_flags);
       else
-        k_walk<false, false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts,
-                                                               counters, buf_keys, ctx->d_flags);
+        k_walk_counts<false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, counters,
+                                                               buf_keys, ctx->d_flags);
       ++launches_sample;
       unsigned long long got = 0;
       LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));

@@ -89,3 +89,33 @@ def test_hash_inverse_round_trips(prog):
     # preimage is not a pair key (lo <= hi) of any graph with int32 vertex ids
     pre = int(run(prog, ["%016x" % (2 ** 64 - 1)])[0][3], 16)
     assert (pre & 0xffffffff) >= 2 ** 31 or (pre >> 32) >= 2 ** 31
+
+
+GM_SRC = r'''
+#include "lne_math.cuh"
+#include <cstdio>
+int main() {
+  unsigned long long x; unsigned d;
+  while (scanf("%llx %x", &x, &d) == 2)
+    printf("%u\n", lne::gm_mod(x, d, lne::gm_magic(d)));
+}
+'''
+
+
+def test_gm_mod_matches_64bit_remainder():
+    td = tempfile.mkdtemp()
+    src, exe = os.path.join(td, "g.cc"), os.path.join(td, "g")
+    open(src, "w").write(GM_SRC)
+    subprocess.run(["g++", "-O2", "-I", os.path.join(ROOT, "lightne_gb300", "csrc"), src, "-o", exe], check=True)
+    rng = np.random.default_rng(5)
+    ds = [1, 2, 3, 7, 10, 64, 65, 2 ** 31 - 1, 2 ** 31, 2 ** 31 + 1, 2 ** 32 - 1] + \
+        [int(v) for v in rng.integers(1, 2 ** 32, 300)] + [int(v) for v in rng.integers(1, 5000, 300)]
+    cases = []
+    for d in ds:
+        for x in [0, 1, d - 1, d, 2 ** 64 - 1, 2 ** 63] + [int(v) for v in rng.integers(0, 2 ** 63, 20)] + \
+                [int(v) * 2 + 1 for v in rng.integers(2 ** 62, 2 ** 63, 5)]:
+            cases.append((x % 2 ** 64, d))
+    inp = "\n".join("%x %x" % (x, d) for x, d in cases)
+    out = subprocess.run([exe], input=inp, capture_output=True, text=True, check=True).stdout.split()
+    bad = [(x, d, int(o)) for (x, d), o in zip(cases, out) if int(o) != x % d]
+    assert not bad, bad[:5]
