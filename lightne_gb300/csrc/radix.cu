@@ -2,7 +2,7 @@
 // order the sparsifier's kept entries by (row, column).
 //
 // Each pass sorts by one digit of at most 8 bits (reduce-then-scan):
-//   k_radix_hist     per-tile digit counts (tile = 4096 consecutive items),
+//   k_radix_hist     per-tile digit counts (tile = 2048 consecutive items),
 //                    stored digit-major, so that one exclusive scan over
 //                    [digit][tile] gives every tile the output start of each
 //                    of its digits;
@@ -30,9 +30,9 @@ namespace {
 
 constexpr int kRadixThreads = 256;
 constexpr int kRadixWarps = kRadixThreads / 32;
-constexpr int kRadixItems = 16;                            // per thread
-constexpr int kRadixTile = kRadixThreads * kRadixItems;    // 4096 items
-constexpr int kWarpItems = 32 * kRadixItems;               // 512 items per warp
+constexpr int kRadixItems = 8;                             // per thread
+constexpr int kRadixTile = kRadixThreads * kRadixItems;    // 2048 items
+constexpr int kWarpItems = 32 * kRadixItems;               // 256 items per warp
 constexpr int kMaxBins = 256;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr size_t kTileBytes = (size_t)kRadixTile * (sizeof(unsigned long long) + sizeof(uint32_t));
@@ -115,11 +115,11 @@ __device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned* wa
 
 // FINAL: write column = key & col_mask and the value (as float) to the CSR
 // arrays; otherwise write key and value to the next pass's buffers.  The
-// tile is first copied to shared memory with cp.async (48 KB in flight per
+// tile is first copied to shared memory with cp.async (24 KB in flight per
 // CTA, no registers held), ranked from there, reordered into a second
 // shared buffer and written out.
 template <bool FINAL, int MODE, bool VALS>
-__global__ void __launch_bounds__(kRadixThreads, 2) k_radix_scatter(
+__global__ void __launch_bounds__(kRadixThreads, 4) k_radix_scatter(
     const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t count, int shift, int dbits,
     int64_t ntiles, const int64_t* __restrict__ offs, unsigned long long* __restrict__ okeys,
     uint32_t* __restrict__ ovals, int32_t* __restrict__ ocol, float* __restrict__ oval, unsigned long long col_mask,

@@ -701,7 +701,7 @@ __device__ __forceinline__ TruncLogOut<WEIGHTED> trunclog_entry(unsigned long lo
   return o;
 }
 
-template <bool WEIGHTED>
+template <bool WEIGHTED, bool DENSE>
 __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, uint64_t cap,
                                                   const Vertex* __restrict__ vd, double factor, int upper,
                                                   const LogTable* __restrict__ ltab,
@@ -727,13 +727,12 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
   unsigned long long kept = 0;
   int qn = 0;  // queued entries (warp-uniform), < 32 between flushes
 
-  // Evaluates the first min(qn, 32) queued entries (one per lane) and
-  // appends their CSR entries.
-  auto flush = [&](int take) {
+  // Evaluates one entry per lane (lanes with have set) and appends their
+  // CSR entries.
+  auto emit = [&](bool have, unsigned long long key, unsigned long long raw) {
     TruncLogOut<WEIGHTED> o;
     o.nitem = 0;
-    if (lane < take) o = trunclog_entry<WEIGHTED>(qk[lane], qr[lane], vd, factor, xf, upper, tab);
-    __syncwarp();
+    if (have) o = trunclog_entry<WEIGHTED>(key, raw, vd, factor, xf, upper, tab);
     if (o.nitem) {
       atomicAdd(&rowcnt[o.u], 1ULL);
       if (o.nitem == 2) atomicAdd(&rowcnt[o.v], 1ULL);
@@ -765,9 +764,25 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
     }
   };
 
+  // Evaluates the first min(qn, 32) queued entries (one per lane).
+  auto flush = [&](int take) {
+    const bool have = lane < take;
+    const unsigned long long key = have ? qk[lane] : 0ULL, raw = have ? qr[lane] : 0ULL;
+    __syncwarp();
+    emit(have, key, raw);
+  };
+
   // warp-uniform loop: the lanes of a warp read 32 consecutive slots
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < cap; b += stride) {
+  if (DENSE) {  // every slot occupied (the distinct pairs of the sliced aggregation)
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < cap; b += stride) {
+      const uint64_t i = b + lane;
+      const bool have = i < cap;
+      const Slot sl = have ? T[i] : Slot{kEmptyKey, 0ULL};
+      emit(have, sl.key, sl.val);
+    }
+  }
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); !DENSE && b < cap; b += stride) {
     const uint64_t i = b + lane;
     const unsigned long long key = i < cap ? T[i].key : kEmptyKey;
     const bool occ = key != kEmptyKey;
@@ -1084,13 +1099,17 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   const uint64_t tcap = sliced ? (uint64_t)h_cnt[2] : cap;
   const unsigned tgrid = grid_for((int64_t)tcap, 256, (int64_t)ctx->num_sms * 16);
   if (p->sample)
-    k_trunclog<true><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
+    k_trunclog<true, false><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
                                             (const LogTable*)ctx->log_table, rowcnt, counters + 3, counters + 4,
                                             cbits, max_items, ikeys, ivals, ctx->d_flags);
+  else if (sliced)
+    k_trunclog<false, true><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
+                                                   (const LogTable*)ctx->log_table, rowcnt, counters + 3,
+                                                   counters + 4, cbits, max_items, ikeys, ivals, ctx->d_flags);
   else
-    k_trunclog<false><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
-                                             (const LogTable*)ctx->log_table, rowcnt, counters + 3, counters + 4,
-                                             cbits, max_items, ikeys, ivals, ctx->d_flags);
+    k_trunclog<false, false><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
+                                                    (const LogTable*)ctx->log_table, rowcnt, counters + 3,
+                                                    counters + 4, cbits, max_items, ikeys, ivals, ctx->d_flags);
   if (table) S.release(table);
   if (uniq) S.release(uniq);
   cudaEventRecord(ev.e[2], st);
