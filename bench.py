@@ -534,8 +534,11 @@ def run_micro(args, local):
     """One C-ABI call timed alone at the workload's sizes (CUDA events on the
     context's stream, 512 MiB L2 flush before every launch): the Gram
     (lne_gram, A = B, n x rank), the tall update GEMM (lne_gemm_tall,
-    n x rank times rank x rank) or the randomized SVD's SpMM B = A Q
-    (lne_spmm, FP32 Q, n x ld).  Prints ms per launch and the bytes model."""
+    n x rank times rank x rank), the randomized SVD's SpMM B = A Q
+    (lne_spmm, FP32 Q, n x ld) or the whole spectral propagation (prop:
+    lne_propagate, BF16 form, n x dim, order K on the graph; its bytes model
+    is the compulsory traffic of its 2K - 1 SpMM half-steps and recursion
+    streams).  Prints ms per launch and the bytes model."""
     import ctypes
 
     import torch
@@ -568,6 +571,23 @@ def run_micro(args, local):
                                          vp(Out.data_ptr()), ld)
         model = 2 * n * ld * 4
         bytes_text = "2 n ld 4 (In read, Out written)"
+    elif args.micro == "prop":
+        from lightne_gb300.api import PropagateParams
+        off, nbrs = load_graph(args.workload)
+        g = Graph.from_numpy(ctx, off, nbrs)
+        d, K = w["dim"], w["order"]
+        del X
+        A0 = torch.randn((n, d), dtype=torch.float32, device="cuda", generator=torch.Generator("cuda").manual_seed(4))
+        Yp = torch.empty_like(A0)
+        prm = _lib.PropagateParams(dim=d, order=K, precision=_lib.LNE_PREC_BF16, mu=0.2, s=0.5)
+        call = lambda: lib.lne_propagate(ctx.handle, g.handle, ctypes.byref(prm), vp(A0.data_ptr()),  # noqa: E731
+                                         vp(Yp.data_ptr()), vp(0), None)
+        m_dir = int(off[-1])
+        # per SpMM (2K - 1 of them): vertex records (16 n) and neighbours
+        # (4 m_dir) once, the BF16 operand once (2 n d), its FP32 result
+        # written once (4 n d); the fused recursion streams are not counted
+        model = (2 * K - 1) * (16 * n + 4 * m_dir + 6 * n * d)
+        bytes_text = "(2K-1) (16 n + 4 m_dir + 2 n d + 4 n d): graph, BF16 operand once, FP32 result"
     else:
         off, nbrs = load_graph(args.workload)
         g = Graph.from_numpy(ctx, off, nbrs)
@@ -599,6 +619,8 @@ def run_micro(args, local):
                       "frac": model / (ms / 1e3) / 1e9 / hbm}))
     if csr:
         csr.free()
+    if args.micro == "prop":
+        g.free()
     ctx.close()
 
 
@@ -798,7 +820,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy", action="store_true")
     ap.add_argument("--quick", action="store_true", help="BF16 form only, no e2e / CPU legs (for profiling)")
-    ap.add_argument("--micro", choices=["gram", "gemm", "spmm"], help="time one C-ABI call alone (for profiling)")
+    ap.add_argument("--micro", choices=["gram", "gemm", "spmm", "prop"],
+                    help="time one C-ABI call alone (for profiling)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 GPU form (library calls) leg")
     args = ap.parse_args()
     ws, rank, local = dist_setup()

@@ -2,11 +2,11 @@
 // order the sparsifier's kept entries by (row, column).
 //
 // Each pass sorts by one digit of at most 8 bits (reduce-then-scan):
-//   k_radix_hist     per-tile digit counts (tile = 2048 consecutive items),
-//                    stored digit-major, so that one exclusive scan over
-//                    [digit][tile] gives every tile the output start of each
-//                    of its digits;
-//   k_radix_scatter  each warp ranks its 512 items of the tile by warp
+//   k_radix_hist     per-tile digit counts (tile = 2048 consecutive items,
+//                    one warp each), stored digit-major, so that one
+//                    exclusive scan over [digit][tile] gives every tile the
+//                    output start of each of its digits;
+//   k_radix_scatter  each warp ranks its 256 items of the tile by warp
 //                    multisplit (lanes with equal digits found by one ballot
 //                    per digit bit; rounds in index order), the warps'
 //                    counts are combined into tile-local digit offsets, the
@@ -69,31 +69,33 @@ __device__ __forceinline__ unsigned digit_of(unsigned long long key, int shift, 
   return (unsigned)((key >> shift) & mask);
 }
 
-// Per-warp sub-histograms in shared memory (plain shared atomics: the
-// counting is issue-bound otherwise), summed per tile.
+// One warp per tile: the warp counts its tile's digits into its own
+// shared histogram (plain shared atomics) and writes the tile's column of
+// the [digit][tile] table, so the per-tile work outside the counting is one
+// pass over the bins.  No block-wide barrier.
+static unsigned hist_grid(int64_t ntiles) { return (unsigned)((ntiles + kRadixWarps - 1) / kRadixWarps); }
+
 template <int MODE>
 __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const unsigned long long* __restrict__ keys,
                                                                int64_t count, int shift, int dbits, int64_t ntiles,
                                                                int64_t* __restrict__ hist, unsigned long long hmask) {
   const int bins = 1 << dbits;
   __shared__ unsigned int h[kRadixWarps][kMaxBins];
-  for (int i = threadIdx.x; i < kRadixWarps * kMaxBins; i += blockDim.x) (&h[0][0])[i] = 0;
-  __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * kRadixTile;
-  const unsigned long long mask = (unsigned long long)(bins - 1);
+  const int lane = threadIdx.x & 31;
+  const int64_t tile = (int64_t)blockIdx.x * kRadixWarps + (threadIdx.x >> 5);
+  if (tile >= ntiles) return;  // the same for the whole warp
   unsigned int* my = h[threadIdx.x >> 5];
+  for (int d = lane; d < bins; d += 32) my[d] = 0;
+  __syncwarp();
+  const int64_t base = tile * kRadixTile;
+  const unsigned long long mask = (unsigned long long)(bins - 1);
 #pragma unroll 8
-  for (int r = 0; r < kRadixItems; ++r) {
-    const int64_t i = base + (int64_t)r * kRadixThreads + threadIdx.x;
+  for (int r = 0; r < kRadixTile / 32; ++r) {
+    const int64_t i = base + (int64_t)r * 32 + lane;
     if (i < count) atomicAdd(&my[digit_of<MODE>(keys[i], shift, mask, hmask)], 1u);
   }
-  __syncthreads();
-  for (int d = threadIdx.x; d < bins; d += blockDim.x) {
-    unsigned s = 0;
-#pragma unroll
-    for (int w = 0; w < kRadixWarps; ++w) s += h[w][d];
-    hist[(int64_t)d * ntiles + blockIdx.x] = s;
-  }
+  __syncwarp();
+  for (int d = lane; d < bins; d += 32) hist[(int64_t)d * ntiles + tile] = my[d];
 }
 
 // Exclusive scan of v over the block's threads (kRadixThreads); returns the
@@ -271,7 +273,7 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
   uint32_t *src_v = vals, *dst_v = vals_tmp;
   for (int p = 0; p < passes; ++p) {
     const int shift = p * dbits;
-    k_radix_hist<kDigitKey><<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist, 0);
+    k_radix_hist<kDigitKey><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist, 0);
     scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
     if (p == passes - 1) {
       k_radix_scatter<true, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
@@ -316,7 +318,7 @@ int partition_by_slot(lne_ctx* ctx, const unsigned long long* keys, unsigned lon
   cudaStream_t st = ctx->stream;
   cudaFuncSetAttribute(k_radix_scatter<false, kDigitSlot, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kScatterSmem);
-  k_radix_hist<kDigitSlot><<<(unsigned)ntiles, kRadixThreads, 0, st>>>(keys, count, shift, dbits, ntiles, hist,
+  k_radix_hist<kDigitSlot><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(keys, count, shift, dbits, ntiles, hist,
                                                                        hmask);
   scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
   k_radix_scatter<false, kDigitSlot, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
@@ -363,7 +365,7 @@ int partition_by_top_bits(lne_ctx* ctx, unsigned long long* keys, unsigned long 
     // digits from the least significant of the top bits up; the last digit
     // may extend past bit 63, where the shifted word is zero
     const int shift = 64 - top_bits + p * dbits;
-    k_radix_hist<kDigitKey><<<(unsigned)ntiles, kRadixThreads, 0, st>>>(src, count, shift, dbits, ntiles, hist, 0);
+    k_radix_hist<kDigitKey><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(src, count, shift, dbits, ntiles, hist, 0);
     scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
     k_radix_scatter<false, kDigitKey, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
         src, nullptr, count, shift, dbits, ntiles, offs, dst, nullptr, nullptr, nullptr, 0, 0);
