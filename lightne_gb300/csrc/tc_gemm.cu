@@ -904,6 +904,234 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __
   stream_finish(sh, tmem, 512, ok, last_commit, flags);
 }
 
+// Warp-specialised form of the symmetric Gram (A = B, c1 = c2 <= 192), with
+// the slices, operand layout, MMAs, TMEM sets and 64-row drains of
+// k_tc_gram_stream<32, R>:
+//   warps 12-13 (load)   cp.async of raw 32-row slices into a ring of
+//                        `ring` slots; raw_full[s] completes when they land
+//   warps 8-11 (split)   raw slot -> TF32 hi/lo operand stage (2 stages),
+//                        releases the raw slot, publishes the stage
+//   warp 14 lane 0 (MMA) D0 (and D1) MMAs of a slice into the TMEM set of
+//                        its 64-row group; its commits release the stage and,
+//                        after the group's last slice, hand the set over
+//   warps 0-7 (drain)    TMEM set -> FP32 registers (rounded to nearest),
+//                        release the set; the sums go to partial[b] at the end
+// The block-synchronous form met at two block barriers per slice and kept
+// the tensor pipe about a quarter busy.  Every wait is bounded; a timeout
+// sets the context's numeric flag to 2, which ends every other wait within
+// 64 polls.
+constexpr int kGwsSL = 32;
+constexpr int kGwsGroup = kGroupRows / kGwsSL;  // slices per TMEM set fill
+constexpr int kGwsDrainWarps = 8;
+constexpr int kGwsSplitWarp = 8, kGwsLoadWarp = 12, kGwsMmaWarp = 14;
+constexpr int kGwsThreads = 32 * 15;
+constexpr int kGwsChunks = 6;      // 16-column chunks per drain thread: sets up to 192 columns
+constexpr int kGwsMaxRing = 8;
+
+struct GwsShared {
+  unsigned long long raw_full[kGwsMaxRing], raw_empty[kGwsMaxRing];
+  unsigned long long conv_full[2], conv_empty[2], set_full[2], set_empty[2];
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kGwsThreads, 1) k_tc_gram_ws(const float* __restrict__ A, int64_t lda, int c1,
+                                                              int nmma, int ring, int64_t n, int64_t per,
+                                                              float* __restrict__ partial, int* flags) {
+  extern __shared__ __align__(1024) uint8_t stream_smem[];
+  constexpr uint32_t kRowBytes = kGwsSL * 4;
+  constexpr int kQ = kGwsSL / 4;
+  const int mt = c1 > 128 ? 2 : 1;
+  const uint32_t a_part = (uint32_t)(128 * mt) * kRowBytes;
+  const uint32_t stage = 2 * a_part;
+  const int c1p = (c1 + 3) & ~3;
+  const uint32_t raw_slot = (uint32_t)(kGwsSL * c1p * 4);
+  uint8_t* conv = stream_smem;
+  uint8_t* raw = stream_smem + 2 * (size_t)stage;
+  GwsShared* sh = reinterpret_cast<GwsShared*>(raw + (size_t)ring * raw_slot);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int n1 = mt == 2 ? nmma - 128 : 0;  // N of D1 (columns >= 128 only)
+  const int set_cols = nmma + n1;
+  const int nchunks = set_cols / 16;
+  const int64_t nslices = (n + kGwsSL - 1) / kGwsSL;
+  const int64_t s0 = (int64_t)blockIdx.x * per;
+  const int64_t left = nslices - s0;
+  const int64_t total = left <= 0 ? 0 : (left < per ? left : per);
+  const int64_t ngroups = (total + kGwsGroup - 1) / kGwsGroup;
+
+  if (t == 0) {
+    for (int s = 0; s < ring; ++s) {
+      tc::mbar_init(tc::smem_addr(&sh->raw_full[s]), 64);
+      tc::mbar_init(tc::smem_addr(&sh->raw_empty[s]), 4);
+    }
+    for (int c = 0; c < 2; ++c) {
+      tc::mbar_init(tc::smem_addr(&sh->conv_full[c]), 4);
+      tc::mbar_init(tc::smem_addr(&sh->conv_empty[c]), 1);
+      tc::mbar_init(tc::smem_addr(&sh->set_full[c]), 1);
+      tc::mbar_init(tc::smem_addr(&sh->set_empty[c]), kGwsDrainWarps);
+    }
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(&sh->tmem_base), 512);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = sh->tmem_base;
+  int* abortf = flags + kFlagNumeric;
+  auto fail = [&]() { atomicExch(abortf, 2); };
+  bool ok = true;
+
+  if (warp >= kGwsLoadWarp && warp < kGwsMmaWarp) {
+    const int ll = t - 32 * kGwsLoadWarp;  // 0..63
+    const int qa = c1p >> 2;
+    for (int64_t g = 0; g < total; ++g) {
+      const int s = (int)(g % ring);
+      if (g >= ring &&
+          !tc::mbar_wait(tc::smem_addr(&sh->raw_empty[s]), (uint32_t)((g / ring - 1) & 1), kWaitCycles, abortf)) {
+        if (lane == 0) fail();
+        break;
+      }
+      const uint32_t dst0 = tc::smem_addr(raw + (size_t)s * raw_slot);
+      for (int idx = ll; idx < kGwsSL * qa; idx += 64) {
+        const int r = idx / qa, q = idx - r * qa;
+        const int64_t row = (s0 + g) * kGwsSL + r;
+        const int cb = c1 - 4 * q;
+        const uint32_t bytes = row < n ? (uint32_t)(cb >= 4 ? 16 : 4 * cb) : 0u;
+        tc::cp_async16(dst0 + (uint32_t)((r * c1p + 4 * q) * 4), bytes ? (const void*)(A + row * lda + 4 * q) : A,
+                       bytes);
+      }
+      tc::cp_async_mbar_arrive(tc::smem_addr(&sh->raw_full[s]));
+    }
+    tc::cp_async_wait_all();
+  } else if (warp >= kGwsSplitWarp && warp < kGwsLoadWarp) {
+    const int ct = t - 32 * kGwsSplitWarp;  // 0..127
+    for (int64_t g = 0; g < total; ++g) {
+      const int s = (int)(g % ring), c = (int)(g & 1);
+      if (!tc::mbar_wait(tc::smem_addr(&sh->raw_full[s]), (uint32_t)((g / ring) & 1), kWaitCycles, abortf) ||
+          (g >= 2 &&
+           !tc::mbar_wait(tc::smem_addr(&sh->conv_empty[c]), (uint32_t)(((g >> 1) - 1) & 1), kWaitCycles, abortf))) {
+        if (lane == 0) fail();
+        break;
+      }
+      const float* rs = reinterpret_cast<const float*>(raw + (size_t)s * raw_slot);
+      uint8_t* hi = conv + (size_t)c * stage;
+      // operand row j (a column of A), K group q (slice rows 4q .. 4q + 3)
+      auto one = [&](int j, int q) {
+        const float* col = rs + (4 * q) * c1p + j;
+        const float4 x = make_float4(col[0], col[c1p], col[2 * c1p], col[3 * c1p]);
+        float4 h, l;
+        split4(x, h, l);
+        const uint32_t off = tc::kmajor_off((uint32_t)j, (uint32_t)(4 * q), kGwsSL);
+        *reinterpret_cast<float4*>(hi + off) = h;
+        *reinterpret_cast<float4*>(hi + a_part + off) = l;
+      };
+      if (ct < c1) {
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) one(ct, q);
+      }
+      for (int e = ct; e < kQ * (c1 - 128); e += 128) one(128 + e / kQ, e % kQ);
+      tc::fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        tc::mbar_arrive(tc::smem_addr(&sh->raw_empty[s]));
+        tc::mbar_arrive(tc::smem_addr(&sh->conv_full[c]));
+      }
+    }
+  } else if (warp == kGwsMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc0 = tc::idesc_tf32(128, nmma);
+      const uint32_t idesc1 = tc::idesc_tf32(128, n1 > 0 ? n1 : 16);
+      int64_t last_commit = -1;
+      for (int64_t g = 0; g < total; ++g) {
+        const int c = (int)(g & 1);
+        const int64_t gi = g / kGwsGroup;
+        const int b = (int)(gi & 1);
+        const bool first = g % kGwsGroup == 0;
+        if (first && gi >= 2 &&
+            !tc::mbar_wait(tc::smem_addr(&sh->set_empty[b]), (uint32_t)(((gi >> 1) - 1) & 1), kWaitCycles, abortf)) {
+          fail();
+          break;
+        }
+        if (!tc::mbar_wait(tc::smem_addr(&sh->conv_full[c]), (uint32_t)((g >> 1) & 1), kWaitCycles, abortf)) {
+          fail();
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t a_hi = tc::smem_addr(conv + (size_t)c * stage);
+        const uint32_t a_lo = a_hi + a_part;
+        const uint32_t d = tmem + (uint32_t)(b * 256);
+        issue_slice<kGwsSL>(d, slice_desc<kGwsSL>(a_hi), slice_desc<kGwsSL>(a_lo), slice_desc<kGwsSL>(a_hi),
+                            slice_desc<kGwsSL>(a_lo), idesc0, first);
+        if (n1 > 0) {
+          const uint32_t m1 = 128 * kRowBytes;  // operand row 128
+          issue_slice<kGwsSL>(d + (uint32_t)nmma, slice_desc<kGwsSL>(a_hi + m1), slice_desc<kGwsSL>(a_lo + m1),
+                              slice_desc<kGwsSL>(a_hi + m1), slice_desc<kGwsSL>(a_lo + m1), idesc1, first);
+        }
+        tc::commit(tc::smem_addr(&sh->conv_empty[c]));
+        if (g % kGwsGroup == kGwsGroup - 1 || g == total - 1) tc::commit(tc::smem_addr(&sh->set_full[b]));
+        last_commit = g;
+      }
+      // nothing may still write TMEM when it is released
+      if (last_commit >= 0)
+        tc::mbar_wait(tc::smem_addr(&sh->conv_empty[last_commit & 1]), (uint32_t)((last_commit >> 1) & 1),
+                      kWaitCycles, flags + kFlagTimeoutGuard);
+    }
+    __syncwarp();
+  } else if (warp < kGwsDrainWarps) {
+    const int lg = warp & 3, half = warp >> 2;
+    const uint32_t lane_addr = (uint32_t)(32 * lg) << 16;
+    float acc[kGwsChunks][16];
+#pragma unroll
+    for (int i = 0; i < kGwsChunks; ++i)
+#pragma unroll
+      for (int e = 0; e < 16; ++e) acc[i][e] = 0.0f;
+    for (int64_t gi = 0; gi < ngroups; ++gi) {
+      const int b = (int)(gi & 1);
+      if (!tc::mbar_wait(tc::smem_addr(&sh->set_full[b]), (uint32_t)((gi >> 1) & 1), kWaitCycles, abortf)) {
+        if (lane == 0) fail();
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+#pragma unroll
+      for (int i = 0; i < kGwsChunks; ++i) {
+        const int ch = half + 2 * i;
+        if (ch < nchunks) {
+          float v[16];
+          tc::tmem_ld16(tmem + lane_addr + (uint32_t)(b * 256 + ch * 16), v);
+#pragma unroll
+          for (int e = 0; e < 16; ++e) acc[i][e] += v[e];
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tc::smem_addr(&sh->set_empty[b]));
+    }
+    if (ok && *reinterpret_cast<volatile int*>(abortf) == 0) {
+      float* out = partial + (int64_t)blockIdx.x * c1 * c1;
+#pragma unroll
+      for (int i = 0; i < kGwsChunks; ++i) {
+        const int ch = half + 2 * i;
+        if (ch < nchunks) {
+          const bool d1 = ch * 16 >= nmma;
+          const int row = (d1 ? 128 : 0) + 32 * lg + lane;
+          const int j0 = d1 ? 128 + ch * 16 - nmma : ch * 16;
+          if (row < c1) {
+#pragma unroll
+            for (int e = 0; e < 16; ++e)
+              if (j0 + e < c1) out[(int64_t)row * c1 + j0 + e] = acc[i][e];
+          }
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
 // G[i][j] = sum over CTAs of partial[b][i][j] in FP64, in CTA order; with
 // sym, the lower triangle is the mirror of the upper one (so G is exactly
 // symmetric; entries i >= 128, j < 128 are not computed by the CTAs).
@@ -939,6 +1167,10 @@ static size_t gram_stream_smem(int c1, int c2, int nmma, bool sym, int sl, int r
   const size_t b_part = sym ? 0 : (size_t)nmma * sl * 4;
   const size_t c1p = (c1 + 3) & ~3, c2p = sym ? 0 : (c2 + 3) & ~3;
   return 2 * (2 * a_part + 2 * b_part) + (size_t)ring * sl * (c1p + c2p) * 4 + sizeof(StreamShared);
+}
+static size_t gram_ws_smem(int c1, int ring) {
+  const size_t a_part = (size_t)(128 * (c1 > 128 ? 2 : 1)) * kGwsSL * 4;
+  return 4 * a_part + (size_t)ring * kGwsSL * ((c1 + 3) & ~3) * 4 + sizeof(GwsShared);
 }
 // Slice rows: 32 (ring of 5) when that fits, else 16 (ring of 6); 0: neither fits.
 static int gram_slice_rows(lne_ctx* ctx, int c1, int c2, int nmma, bool sym) {
@@ -1060,6 +1292,37 @@ int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const floa
   }
   const int nmma = std::max(16, (c2 + 15) / 16 * 16);
   const bool sym = A == B && lda == ldb && c1 == c2;
+  if (sym) {
+    // warp-specialised form: two TMEM sets of at most 2 x kGwsChunks chunks
+    const int set_cols = nmma + (c1 > 128 ? nmma - 128 : 0);
+    const size_t slot = (size_t)kGwsSL * ((c1 + 3) & ~3) * 4;
+    const size_t fixed = gram_ws_smem(c1, 0);
+    const int ring = ctx->smem_optin > fixed ? (int)std::min<size_t>(kGwsMaxRing, (ctx->smem_optin - fixed) / slot)
+                                             : 0;
+    if (set_cols <= 32 * kGwsChunks && ring >= 2) {
+      const int64_t nslices = (n + kGwsSL - 1) / kGwsSL;
+      const int64_t want =
+          std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(nslices, ctx->num_sms), max_blocks));
+      const int64_t per = (nslices + want - 1) / want;
+      const int64_t nb = (nslices + per - 1) / per;  // <= want
+      float* own = nullptr;
+      if (!partial) {
+        int rc = dalloc(ctx, (void**)&own, sizeof(float) * nb * c1 * c2, "gram partials");
+        if (rc) return rc;
+        partial = own;
+      }
+      // the CTA allocates all 512 TMEM columns: one CTA per SM
+      const size_t lsmem = std::max(gram_ws_smem(c1, ring), ctx->smem_optin / 2 + 1);
+      cudaFuncSetAttribute(k_tc_gram_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
+      k_tc_gram_ws<<<(unsigned)nb, kGwsThreads, lsmem, ctx->stream>>>(A, lda, c1, nmma, ring, n, per, partial,
+                                                                      ctx->d_flags);
+      const int64_t cnt = (int64_t)c1 * c2;
+      k_gram_reduce_stream<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, c1, c2, 1, G);
+      if (own) dfree(ctx, own);
+      LNE_CUDA_TRY(cudaGetLastError());
+      return LNE_OK;
+    }
+  }
   const int sl = gram_slice_rows(ctx, c1, c2, nmma, sym);
   const int ring = sl == 32 ? 5 : kGramRing;
   const size_t ssmem = gram_stream_smem(c1, c2, nmma, sym, sl, ring);

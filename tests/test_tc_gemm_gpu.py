@@ -54,7 +54,7 @@ def test_gram(ctx, lib, n, c1, c2):
 
 
 @pytest.mark.parametrize("n,c", [(10000, 138), (4096, 128), (2049, 16), (33, 144), (1, 138), (7001, 250),
-                                 (200003, 144)])
+                                 (200003, 144), (50001, 131), (5000, 160), (3000, 100), (70, 7)])
 def test_gram_symmetric(ctx, lib, n, c):
     """A^T A with the same pointer for both operands (the CholeskyQR case):
     the second 128-column tile only computes columns >= 128 and the rest
