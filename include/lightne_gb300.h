@@ -49,6 +49,7 @@ extern "C" {
 /* Dense operand precision of SpMM / propagation. */
 #define LNE_PREC_FP32 0
 #define LNE_PREC_BF16 1
+#define LNE_PREC_FP8 2 /* e4m3; SpMM dense operand only (lne_spmm x_prec) */
 
 typedef struct lne_ctx lne_ctx;
 typedef struct lne_graph lne_graph;
@@ -144,8 +145,9 @@ int lne_trunc_log_values(lne_ctx* ctx, const double* x, int64_t n, double* out);
 /*
  * SpMM: Y = alpha * A * X + beta * Y (mkl_sparse_s_mm, row-major,
  * non-transposed, as LightNE/mklredsvd/mklredsvd.cc:235-245).  X is n x d
- * with leading dimension ldx (device, FP32 or BF16 per x_prec; rows on
- * 16-byte boundaries: ldx a multiple of 8), Y is n x d FP32 with ldy.
+ * with leading dimension ldx (device, FP32, BF16 or FP8 e4m3 per x_prec;
+ * rows on 16-byte boundaries: ldx a multiple of 8, of 16 for FP8), Y is
+ * n x d FP32 with ldy.
  * beta == 0 does not read Y.  Sums are formed in a fixed order: the result
  * is bitwise reproducible.  The first call on a matrix builds its work list.
  */
@@ -192,8 +194,10 @@ int lne_randsvd(lne_ctx* ctx, const lne_csr* A, const lne_randsvd_params* p, flo
 /*
  * The Gaussian sketch generator lne_randsvd uses: rows x cols N(0,1) values
  * of stream stream_id (0: Omega, 1: P) into device memory with leading
- * dimension ld.  Values are rounded to BF16-representable floats, so the
- * FP32 and BF16 forms share one sketch.  Exposed so that a checker can rebuild the same sketches
+ * dimension ld.  Omega's values are rounded to FP8 (e4m3)-representable
+ * floats, the other streams' to BF16-representable floats, so the FP32 and
+ * BF16 forms share one sketch (the BF16 form gathers Omega from an FP8
+ * copy).  Exposed so that a checker can rebuild the same sketches
  * (the reference's VSL SFMT19937 stream, mklredsvd.cc:141, has no
  * counterpart without MKL).
  */

@@ -21,6 +21,7 @@ LNE_ERR_NUMERIC = 6
 
 LNE_PREC_FP32 = 0
 LNE_PREC_BF16 = 1
+LNE_PREC_FP8 = 2
 
 _STATUS_NAMES = {
     LNE_ERR_INVALID: "LNE_ERR_INVALID",

@@ -16,24 +16,39 @@ namespace lne {
 // ---------------------------------------------------------------------------
 // Gaussian sketch
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float gaussian_at(uint64_t base, uint64_t idx) {
+// FP8 (e4m3) nearest value of x, as a float (and its byte in *b).
+__device__ __forceinline__ float round_e4m3(float x, __nv_fp8_storage_t* b) {
+  *b = __nv_cvt_float_to_fp8(x, __NV_SATFINITE, __NV_E4M3);
+  const __half_raw h = __nv_cvt_fp8_to_halfraw(*b, __NV_E4M3);
+  return __half2float(*reinterpret_cast<const __half*>(&h));
+}
+
+// Box-Muller draw `idx` of the stream, rounded to an FP8 (e4m3)-representable
+// value (e4m3 set) or a BF16-representable one, so that the FP32 and
+// BF16 forms of the randomized SVD use the same sketch.
+__device__ __forceinline__ float gaussian_at(uint64_t base, uint64_t idx, bool e4m3, __nv_fp8_storage_t* b) {
   const uint64_t x1 = hash64_2(base + 2 * idx), x2 = hash64_2(base + 2 * idx + 1);
   const float u1 = (float)((x1 >> 40) + 1) * 5.9604644775390625e-08f;  // (0, 1]
   const float u2 = (float)(x2 >> 40) * 5.9604644775390625e-08f;        // [0, 1)
   float s, c;
   sincospif(2.0f * u2, &s, &c);
-  // rounded to a BF16-representable value, so that the FP32 and BF16 forms
-  // of the randomized SVD use the same sketch
-  return __bfloat162float(__float2bfloat16_rn(sqrtf(-2.0f * logf(u1)) * c));
+  const float z = sqrtf(-2.0f * logf(u1)) * c;
+  if (e4m3) return round_e4m3(z, b);
+  *b = 0;
+  return __bfloat162float(__float2bfloat16_rn(z));
 }
 
 template <typename T>
-__global__ void k_gaussian(uint64_t base, int64_t rows, int64_t cols, T* __restrict__ out, int64_t ld) {
+__global__ void k_gaussian(uint64_t base, int64_t rows, int64_t cols, T* __restrict__ out, int64_t ld, bool e4m3) {
   const int64_t total = rows * ld;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t / ld, j = t - i * ld;
-    const float z = j < cols ? gaussian_at(base, (uint64_t)(i * cols + j)) : 0.0f;
-    out[t] = (T)z;
+    __nv_fp8_storage_t b = 0;
+    const float z = j < cols ? gaussian_at(base, (uint64_t)(i * cols + j), e4m3, &b) : 0.0f;
+    if constexpr (sizeof(T) == 1)
+      reinterpret_cast<__nv_fp8_storage_t*>(out)[t] = b;
+    else
+      out[t] = (T)z;
   }
 }
 
@@ -46,10 +61,11 @@ static unsigned grid1d(int64_t items, int threads, int64_t cap) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, cap));
 }
 
+// Stream 0 (the sketch Omega) is rounded to e4m3, the others to BF16.
 int gaussian_fill_f32(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols, float* out,
                       int64_t ld) {
   k_gaussian<float><<<grid1d(rows * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
-      gaussian_base(seed, stream_id), rows, cols, out, ld);
+      gaussian_base(seed, stream_id), rows, cols, out, ld, stream_id == 0);
   LNE_CUDA_TRY(cudaGetLastError());
   return LNE_OK;
 }
@@ -57,7 +73,15 @@ int gaussian_fill_f32(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t r
 int gaussian_fill_bf16(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
                        __nv_bfloat16* out, int64_t ld) {
   k_gaussian<__nv_bfloat16><<<grid1d(rows * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
-      gaussian_base(seed, stream_id), rows, cols, out, ld);
+      gaussian_base(seed, stream_id), rows, cols, out, ld, stream_id == 0);
+  LNE_CUDA_TRY(cudaGetLastError());
+  return LNE_OK;
+}
+
+int gaussian_fill_fp8(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
+                      __nv_fp8_e4m3* out, int64_t ld) {
+  k_gaussian<__nv_fp8_e4m3><<<grid1d(rows * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
+      gaussian_base(seed, stream_id), rows, cols, out, ld, true);
   LNE_CUDA_TRY(cudaGetLastError());
   return LNE_OK;
 }

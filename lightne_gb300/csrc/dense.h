@@ -5,6 +5,7 @@
 // padding columns kept at zero).  Small r x r matrices are row-major FP64.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <stdint.h>
 
 #include "lne_internal.h"
@@ -12,12 +13,17 @@
 namespace lne {
 
 // N(0,1) entries from a counter-based generator: entry (i, j) of stream
-// `stream_id` is a Box-Muller transform of two 53-bit uniforms hashed from
-// (seed, stream_id, i, j).  Independent of the launch shape.
+// `stream_id` is a Box-Muller transform of two 24-bit uniforms hashed from
+// (seed, stream_id, i, j), rounded to an e4m3-representable value for
+// stream 0 (the sketch) and to a BF16-representable one otherwise.
+// Independent of the launch shape.  The FP8 fill writes the e4m3 bytes of
+// the same values (always e4m3-rounded).
 int gaussian_fill_f32(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols, float* out,
                       int64_t ld);
 int gaussian_fill_bf16(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
                        __nv_bfloat16* out, int64_t ld);
+int gaussian_fill_fp8(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
+                      __nv_fp8_e4m3* out, int64_t ld);
 
 // G (c1 x c2, FP64, row-major, ldg = c2) = A^T B for A (n x c1, lda),
 // B (n x c2, ldb).  FP32 products summed per 2048-row block, blocks summed

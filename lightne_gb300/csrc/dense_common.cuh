@@ -1,6 +1,8 @@
 // Dense-operand helpers shared by the SpMM, propagation and dense kernels.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -52,9 +54,39 @@ struct Vec16<__nv_bfloat16> {
   }
 };
 
+// FP8 (e4m3) operand: 16 elements per 16 bytes, widened exactly to float
+// (every e4m3 value is a half), two at a time.  Read-only (the sketch).
+template <>
+struct Vec16<__nv_fp8_e4m3> {
+  static constexpr int E = 16;
+  __device__ __forceinline__ static void unpack(const uint4 v, float (&o)[16]) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const __half2_raw r = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(w[i] >> (16 * h)), __NV_E4M3);
+        const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&r));
+        o[4 * i + 2 * h] = f.x;
+        o[4 * i + 2 * h + 1] = f.y;
+      }
+  }
+  __device__ __forceinline__ static void load(const __nv_fp8_e4m3* p, float (&o)[16]) {
+    unpack(__ldg(reinterpret_cast<const uint4*>(p)), o);
+  }
+  __device__ __forceinline__ static void load_cg(const __nv_fp8_e4m3* p, float (&o)[16]) {
+    unpack(__ldcg(reinterpret_cast<const uint4*>(p)), o);
+  }
+};
+
 // Padded leading dimension: rows of the dense operands start on 16-byte
 // boundaries and hold a whole number of 16-byte vectors for both FP32 and
 // BF16 copies (multiple of 8 elements).
 __host__ __device__ __forceinline__ int64_t pad_ld(int64_t d) { return (d + 7) / 8 * 8; }
 
+}  // namespace lne
+
+namespace lne {
+// Leading dimension of an FP8 copy: rows of 16-byte multiples.
+__host__ __device__ __forceinline__ int64_t pad_ld_fp8(int64_t d) { return (d + 15) / 16 * 16; }
 }  // namespace lne

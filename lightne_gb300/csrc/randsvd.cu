@@ -47,7 +47,7 @@ struct Buf {
   }
 };
 
-// Y = A * X with FP32 output, X FP32 or BF16; `add` accumulates the later
+// Y = A * X with FP32 output, X FP32, BF16 or FP8; `add` accumulates the later
 // column panels of the cache-blocked SpMM.
 struct EpiStore {
   float* __restrict__ Y;
@@ -170,10 +170,11 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
 
   Buf B(ctx);
   float *Y = nullptr, *T = nullptr, *Bm = nullptr, *P = nullptr, *Wf = nullptr;
-  __nv_bfloat16* Xb = nullptr;
+  __nv_fp8_e4m3* Xq = nullptr;  // the sketch's FP8 copy (BF16 form)
+  const int64_t ldq = pad_ld_fp8(r);
   double *C = nullptr, *U = nullptr, *S = nullptr;
   if ((rc = B.get(&Y, (size_t)n * ld, "Y")) || (rc = B.get(&T, (size_t)n * ld, "QR scratch")) ||
-      (bf16 && (rc = B.get(&Xb, (size_t)n * ld, "BF16 operand"))))
+      (bf16 && (rc = B.get(&Xq, (size_t)n * ldq, "FP8 sketch"))))
     return rc;
 
   cudaEventRecord(ev[0], st);
@@ -186,8 +187,9 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
     if ((rc = sparse_projection_product(ctx, A, O, Y, ld, &launches))) return rc;
     launches -= 1;  // the Gaussian draw counted below does not happen
   } else if (bf16) {
-    if ((rc = gaussian_fill_bf16(ctx, p->seed, 0, n, r, Xb, ld))) return rc;
-    if ((rc = spmm_store<__nv_bfloat16>(ctx, A, Xb, ld, (int)ld, Y, &launches))) return rc;
+    // the sketch's values are e4m3-representable: its FP8 copy is exact
+    if ((rc = gaussian_fill_fp8(ctx, p->seed, 0, n, r, Xq, ldq))) return rc;
+    if ((rc = spmm_store<__nv_fp8_e4m3>(ctx, A, Xq, ldq, (int)ld, Y, &launches))) return rc;
   } else {
     if ((rc = gaussian_fill_f32(ctx, p->seed, 0, n, r, T, ld))) return rc;
     if ((rc = spmm_store<float>(ctx, A, T, ld, (int)ld, Y, &launches))) return rc;

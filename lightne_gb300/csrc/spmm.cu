@@ -185,12 +185,14 @@ extern "C" int lne_spmm(lne_ctx* ctx, const lne_csr* A, int x_prec, const void* 
                         float alpha, float beta, float* Y, int64_t ldy) {
   LNE_CHECK_ARG(ctx && A && X && Y, "lne_spmm: NULL argument");
   LNE_CHECK_ARG(d >= 1 && ldx >= d && ldy >= d, "lne_spmm: need 1 <= d <= ldx, ldy");
-  LNE_CHECK_ARG(x_prec == LNE_PREC_FP32 || x_prec == LNE_PREC_BF16, "lne_spmm: x_prec must be FP32 or BF16");
-  LNE_CHECK_ARG(ldx % 8 == 0 && ((uintptr_t)X % 16) == 0,
-                "lne_spmm: X rows must start on 16-byte boundaries (ldx a multiple of 8)");
+  LNE_CHECK_ARG(x_prec == LNE_PREC_FP32 || x_prec == LNE_PREC_BF16 || x_prec == LNE_PREC_FP8,
+                "lne_spmm: x_prec must be FP32, BF16 or FP8");
+  LNE_CHECK_ARG(ldx % (x_prec == LNE_PREC_FP8 ? 16 : 8) == 0 && ((uintptr_t)X % 16) == 0,
+                "lne_spmm: X rows must start on 16-byte boundaries (ldx a multiple of 8, 16 for FP8)");
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
   lne_csr* Am = const_cast<lne_csr*>(A);
   EpiAxpby epi{alpha, beta, Y, ldy, (int)d, false};
   if (x_prec == LNE_PREC_FP32) return spmm_csr_panels<float>(ctx, Am, (const float*)X, ldx, d, epi);
+  if (x_prec == LNE_PREC_FP8) return spmm_csr_panels<__nv_fp8_e4m3>(ctx, Am, (const __nv_fp8_e4m3*)X, ldx, d, epi);
   return spmm_csr_panels<__nv_bfloat16>(ctx, Am, (const __nv_bfloat16*)X, ldx, d, epi);
 }

@@ -90,6 +90,64 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
   constexpr int kUnroll = kStaged < 1 ? 1 : (kStaged > 4 ? 4 : kStaged);
   const int lane = threadIdx.x & 31;
   const int grp = lane / G, gl = lane % G;
+  if constexpr (E == 16) {
+    // 16 elements per vector (FP8): the gathers of 4 / VPL nonzeros are
+    // staged as raw 16-byte words (4 registers each), widened at the FMAs
+    constexpr int kU = VPL >= 4 ? 1 : 4 / VPL;
+    // G = 9 (a 144-element row: 9 vectors): three groups of 9 lanes, lanes
+    // 27..31 idle
+    const bool in_grp = grp < P;
+    for (int64_t base = j0; base < j1; base += 32) {
+      const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);
+      const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;
+      const float v = Rows::kHasVal ? (lane < cnt ? R.v(base + lane) : 0.f) : 1.f;
+      for (int t0 = 0; t0 < cnt; t0 += P * kU) {
+        uint4 raw[kU][VPL];
+        float vv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int t = t0 + u * P + grp;
+          const uint32_t cc = __shfl_sync(kFull, c, t & 31);
+          vv[u] = Rows::kHasVal ? __shfl_sync(kFull, v, t & 31) : 1.f;
+          const XT* xr = X + (int64_t)cc * ldx;
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            const int ch = gl + G * k;
+            raw[u][k] = (in_grp && t < cnt && ch < C) ? __ldg(reinterpret_cast<const uint4*>(xr + ch * E))
+                                                       : make_uint4(0, 0, 0, 0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u)
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            float x[E];
+            Vec16<XT>::unpack(raw[u][k], x);
+#pragma unroll
+            for (int e = 0; e < E; ++e) acc.a[k][e] = fmaf(vv[u], x[e], acc.a[k][e]);
+          }
+      }
+    }
+    if constexpr ((G & (G - 1)) == 0) {
+#pragma unroll
+      for (int o = G; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < VPL; ++k)
+#pragma unroll
+          for (int e = 0; e < E; ++e) acc.a[k][e] += __shfl_xor_sync(kFull, acc.a[k][e], o);
+    } else {
+      static_assert(P == 3, "non-power-of-two groups: three groups per warp");
+#pragma unroll
+      for (int k = 0; k < VPL; ++k)
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const float g1 = __shfl_down_sync(kFull, acc.a[k][e], G);
+          const float g2 = __shfl_down_sync(kFull, acc.a[k][e], 2 * G);
+          acc.a[k][e] = (acc.a[k][e] + g1) + g2;
+        }
+    }
+    return;
+  }
   for (int64_t base = j0; base < j1; base += 32) {
     const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);
     const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;

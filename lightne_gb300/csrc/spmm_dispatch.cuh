@@ -58,6 +58,9 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
   while (c_off < c_total) {
     int64_t rem = c_total - c_off, C2 = 1;
     while (C2 * 2 <= rem && C2 * 2 <= 128) C2 *= 2;
+    // an FP8 row of 144 elements is one 9-vector slab (three groups of 9
+    // lanes): its tail vector shares the gathers of the row
+    if (E == 16 && rem == 9) C2 = 9;
     const int C = (int)C2;
     const int64_t ldp = (int64_t)C * E;
     if (plan.n_chunks > 0 && partial == nullptr) {
@@ -82,7 +85,18 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
       ldxs = (int64_t)C * E;
     }
     const int e_base = (int)(c_off * E);
-    if (C <= 2)
+    bool launched = false;
+    if constexpr (E == 16) {  // one 16-element vector: one lane per nonzero
+      if (C <= 1) {
+        spmm_launch<XT, 1, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
+        launched = true;
+      } else if (C == 9) {
+        spmm_launch<XT, 9, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
+        launched = true;
+      }
+    }
+    if (launched) {
+    } else if (C <= 2)
       spmm_launch<XT, 2, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else if (C <= 4)
       spmm_launch<XT, 4, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);

@@ -1,4 +1,4 @@
-"""lne_spmm (explicit CSR x dense, FP32 or BF16 dense operand) against an
+"""lne_spmm (explicit CSR x dense, FP32, BF16 or FP8 dense operand) against an
 FP64 numpy product of the same operands.  Tolerance: FP32 accumulation,
 |err| <= 1e-5 * (|A| |X|) elementwise."""
 import ctypes
@@ -8,7 +8,7 @@ import pytest
 import torch
 
 from lightne_gb300 import _lib
-from lightne_gb300._lib import LNE_PREC_BF16, LNE_PREC_FP32
+from lightne_gb300._lib import LNE_PREC_BF16, LNE_PREC_FP8, LNE_PREC_FP32
 from lightne_gb300.api import CSR
 
 pytestmark = pytest.mark.gpu
@@ -31,18 +31,22 @@ def to_bf16_f64(x):
     return torch.from_numpy(x).to(torch.bfloat16).to(torch.float64).numpy()
 
 
+DTYPES = {LNE_PREC_FP32: torch.float32, LNE_PREC_BF16: torch.bfloat16, LNE_PREC_FP8: torch.float8_e4m3fn}
+
+
 @pytest.mark.parametrize("d,prec", [(128, LNE_PREC_FP32), (138, LNE_PREC_FP32), (20, LNE_PREC_FP32),
                                     (600, LNE_PREC_FP32), (128, LNE_PREC_BF16), (138, LNE_PREC_BF16),
-                                    (60, LNE_PREC_BF16), (1100, LNE_PREC_BF16)])
+                                    (60, LNE_PREC_BF16), (1100, LNE_PREC_BF16), (144, LNE_PREC_FP8),
+                                    (138, LNE_PREC_FP8), (16, LNE_PREC_FP8), (700, LNE_PREC_FP8),
+                                    (2100, LNE_PREC_FP8)])
 def test_spmm_matches_fp64(ctx, lib, d, prec):
     n = 3000
     rp, col, val = random_csr(n, 12, long_rows=[(5, 2500), (77, 2049), (2999, 2048)], seed=d)
-    ld = (d + 7) // 8 * 8
+    ld = (d + 15) // 16 * 16 if prec == LNE_PREC_FP8 else (d + 7) // 8 * 8
     rng = np.random.default_rng(1)
     X = np.zeros((n, ld), np.float32)
     X[:, :d] = rng.standard_normal((n, d)).astype(np.float32)
-    dt = torch.float32 if prec == LNE_PREC_FP32 else torch.bfloat16
-    dX = torch.from_numpy(X).to(dt).cuda()
+    dX = torch.from_numpy(X).to(DTYPES[prec]).cuda()
     Y0 = rng.standard_normal((n, ld)).astype(np.float32)
     dY = torch.from_numpy(Y0).cuda()
     d_rp, d_col, d_val = (torch.from_numpy(a).cuda() for a in (rp, col, val))
@@ -54,7 +58,7 @@ def test_spmm_matches_fp64(ctx, lib, d, prec):
     assert rc == 0, lib.lne_last_error()
     ctx.synchronize()
     got = dY.cpu().numpy()
-    Xd = X.astype(np.float64) if prec == LNE_PREC_FP32 else to_bf16_f64(X)
+    Xd = dX.cpu().to(torch.float64).numpy()  # the operand's values as stored
     import scipy.sparse as sp
     Am = sp.csr_matrix((val.astype(np.float64), col, rp), shape=(n, n))
     ref = alpha * (Am @ Xd[:, :d]) + beta * Y0[:, :d].astype(np.float64)
@@ -109,7 +113,7 @@ def test_spmm_column_panels(ctx, lib, prec):
         ctx.synchronize()
         outs.append(dY.cpu().numpy()[:, :d].astype(np.float64))
     lib.lne_ctx_set_spmm_panel_bytes(ctx.handle, 64 << 20)
-    Xd = X.astype(np.float64) if prec == LNE_PREC_FP32 else to_bf16_f64(X)
+    Xd = dX.cpu().to(torch.float64).numpy()  # the operand's values as stored
     import scipy.sparse as sp
     Am = sp.csr_matrix((val.astype(np.float64), col, rp), shape=(n, n))
     ref = Am @ Xd[:, :d]
