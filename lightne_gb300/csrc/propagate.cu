@@ -186,6 +186,8 @@ struct EpiFirst {
 // Order k >= 2: Lx2 = M tmp - Lx0 - 2 Lx1 [- 2 extra];  conv += ck Lx2 (conv
 // may be null);  or the final vector on the last order.  L0 == null means a
 // zero Lx0; `extra` (FP32, may be null) is the tangent pass's M T_k term.
+// The sum is read and written every second order: `skip` leaves conv alone
+// and the next order adds ck_prev Lx1 (the skipped order's vector) as well.
 template <typename XT>
 struct EpiStep {
   const float4* __restrict__ coef;
@@ -199,6 +201,8 @@ struct EpiStep {
   FinalOut fin;
   int64_t ld;
   float ck;
+  float ck_prev = 0.0f;
+  bool skip = false;
   template <int N>
   __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&acc)[N]) const {
     const float4 c = __ldg(coef + r);
@@ -211,8 +215,10 @@ struct EpiStep {
       for (int i = 0; i < N; ++i) l0[i] = 0.0f;
     }
     load_f32<N>(L1, ld, r, e0, l1);
-    if (conv) {
+    if (conv && !skip) {
       load_f32<N>(conv, ld, r, e0, cv);
+#pragma unroll
+      for (int i = 0; i < N; ++i) cv[i] = fmaf(ck_prev, l1[i], cv[i]);
     } else {
 #pragma unroll
       for (int i = 0; i < N; ++i) cv[i] = 0.0f;
@@ -235,7 +241,7 @@ struct EpiStep {
     } else {
       store_f32<N>(L2, ld, r, e0, l2);
       if (L2b) store_bf16<N>(L2b, ld, r, e0, l2);
-      if (conv) store_f32<N>(conv, ld, r, e0, cv);
+      if (conv && !skip) store_f32<N>(conv, ld, r, e0, cv);
     }
   }
 };
@@ -407,7 +413,11 @@ struct Filter {
       if ((rc = apply_m(op(ring[j1], ringb[j1]), kBF16 ? nullptr : Tf, kBF16 ? Tb : nullptr))) return rc;
       const bool last = k == order - 1;
       FinalOut fo{last ? base : nullptr, scale_dt, finf, finb};
-      EpiStep<XT> epi{coef, Tx, l0, ring[j1], nullptr, ring[j2], ringb[j2], conv, fo, ld, c[k]};
+      // conv is updated on odd orders (and on the last): even orders are
+      // added with the next one
+      const bool skip = !last && (k % 2 == 0);
+      const float ck_prev = (k % 2 == 1) ? c[k - 1] : 0.0f;
+      EpiStep<XT> epi{coef, Tx, l0, ring[j1], nullptr, ring[j2], ringb[j2], conv, fo, ld, c[k], ck_prev, skip};
       if ((rc = spmm_run<XT>(ctx, R, g->plan, Tx, ld, ld, epi, launches))) return rc;
       l0 = ring[j1];
       j1 = j2;
