@@ -5,7 +5,12 @@
 // with par_table (LightNE/par_table.h).
 //
 // Layout in HBM during one call:
-//   table   Slot[capacity]       16 B per slot: u64 key, u64 count (or f64 weight)
+//   keys    u64[samples] x 2     the walk's samples (hashed keys on the sliced
+//                                path) and their radix-partitioned copy
+//   uniq    Slot[distinct]       sliced path: the distinct pairs with counts
+//   table   Slot[capacity]       pair table (weights, several batches, or the
+//                                sliced path's fallback): 16 B per slot,
+//                                u64 key, u64 count (or f64 weight)
 //   rowcnt  i64[n]               kept entries per row
 //   row_ptr i64[n+1]             exclusive scan of rowcnt (the output row_ptr)
 //   items   u64[nnz] + u32[nnz]  (row << cbits | col, float bits) per CSR entry,
@@ -88,10 +93,11 @@ __device__ __forceinline__ bool table_insert_add(Slot* __restrict__ T, uint64_t 
 // Granlund-Montgomery multiplier:
 //   [eff test (-sample 1)] -> r = rand % T + 1 -> k = rand % r + 1 ->
 //   k-1 steps from u, then r-k steps from v (rand % degree each)
-// so the lanes of a warp execute the same instructions whatever phase each
-// lane is in.  Emitted pair keys (and weights with -sample 1) are staged per
-// warp in shared memory and written to the sample buffer 32 at a time, so
-// the walk never waits on the pair table; k_insert adds them to the table.
+// so the lanes of a warp draw in step whatever phase each lane is in.
+// Emitted pair keys (and weights with -sample 1) are staged per warp in
+// shared memory and written to the sample buffer 32 at a time, so the walk
+// never waits on the aggregation.  k_walk (below) is the -sample 1 form, with
+// one branch per phase; k_walk_counts is the -sample 0 form with selects.
 static constexpr int kWalkThreads = 256;
 static constexpr int kQueue = 64;    // staged keys per warp
 static constexpr int kMaxRMagic = 64;  // multipliers of r = 1..64 kept in shared memory
