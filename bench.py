@@ -535,7 +535,8 @@ def run_micro(args, local):
     context's stream, 512 MiB L2 flush before every launch): the Gram
     (lne_gram, A = B, n x rank), the tall update GEMM (lne_gemm_tall,
     n x rank times rank x rank), the randomized SVD's SpMM B = A Q
-    (lne_spmm, FP32 Q, n x ld) or the whole spectral propagation (prop:
+    (lne_spmm, FP32 Q, n x ld), its sketch product Y = A Omega from the FP8
+    copy (spmm8) or the whole spectral propagation (prop:
     lne_propagate, BF16 form, n x dim, order K on the graph; its bytes model
     is the compulsory traffic of its 2K - 1 SpMM half-steps and recursion
     streams).  Prints ms per launch and the bytes model."""
@@ -595,10 +596,23 @@ def run_micro(args, local):
                                               sample_ratio=float(np.float32(w["sample_ratio"])))
         g.free()
         Y = torch.empty((n, ld), dtype=torch.float32, device="cuda")
-        call = lambda: lib.lne_spmm(ctx.handle, csr.handle, 0, vp(X.data_ptr()), ld, ld, 1.0, 0.0,  # noqa: E731
-                                    vp(Y.data_ptr()), ld)
-        model = 8 * (n + 1) + 8 * csr.nnz + 2 * n * ld * 4
-        bytes_text = "8(n+1) + 8 nnz + 2 n ld 4 (CSR, Q once, B written)"
+        if args.micro == "spmm8":
+            # the sketch product Y = A Omega of the BF16 form: Omega's values
+            # are e4m3-representable, so its FP8 copy is exact
+            ldq = (r + 15) // 16 * 16
+            om = torch.zeros((n, ldq), dtype=torch.float32, device="cuda")
+            _lib.check(lib.lne_gaussian(ctx.handle, SVD_SEED, 0, n, r, vp(om.data_ptr()), ldq))
+            Xq = om.to(torch.float8_e4m3fn)
+            del om, X
+            call = lambda: lib.lne_spmm(ctx.handle, csr.handle, _lib.LNE_PREC_FP8,  # noqa: E731
+                                        vp(Xq.data_ptr()), ldq, ld, 1.0, 0.0, vp(Y.data_ptr()), ld)
+            model = 8 * (n + 1) + 8 * csr.nnz + n * ldq + n * ld * 4
+            bytes_text = "8(n+1) + 8 nnz + n ldq + n ld 4 (CSR, FP8 Omega once, Y written)"
+        else:
+            call = lambda: lib.lne_spmm(ctx.handle, csr.handle, 0, vp(X.data_ptr()), ld, ld, 1.0, 0.0,  # noqa: E731
+                                        vp(Y.data_ptr()), ld)
+            model = 8 * (n + 1) + 8 * csr.nnz + 2 * n * ld * 4
+            bytes_text = "8(n+1) + 8 nnz + 2 n ld 4 (CSR, Q once, B written)"
     for _ in range(args.warmup):
         _lib.check(call())
     torch.cuda.synchronize()
@@ -820,7 +834,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy", action="store_true")
     ap.add_argument("--quick", action="store_true", help="BF16 form only, no e2e / CPU legs (for profiling)")
-    ap.add_argument("--micro", choices=["gram", "gemm", "spmm", "prop"],
+    ap.add_argument("--micro", choices=["gram", "gemm", "spmm", "spmm8", "prop"],
                     help="time one C-ABI call alone (for profiling)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 GPU form (library calls) leg")
     args = ap.parse_args()
