@@ -70,14 +70,6 @@ int gaussian_fill_f32(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t r
   return LNE_OK;
 }
 
-int gaussian_fill_bf16(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
-                       __nv_bfloat16* out, int64_t ld) {
-  k_gaussian<__nv_bfloat16><<<grid1d(rows * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(
-      gaussian_base(seed, stream_id), rows, cols, out, ld, stream_id == 0);
-  LNE_CUDA_TRY(cudaGetLastError());
-  return LNE_OK;
-}
-
 int gaussian_fill_fp8(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
                       __nv_fp8_e4m3* out, int64_t ld) {
   k_gaussian<__nv_fp8_e4m3><<<grid1d(rows * ld, 256, (int64_t)ctx->num_sms * 32), 256, 0, ctx->stream>>>(

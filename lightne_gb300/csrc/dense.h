@@ -20,8 +20,6 @@ namespace lne {
 // the same values (always e4m3-rounded).
 int gaussian_fill_f32(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols, float* out,
                       int64_t ld);
-int gaussian_fill_bf16(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
-                       __nv_bfloat16* out, int64_t ld);
 int gaussian_fill_fp8(lne_ctx* ctx, uint64_t seed, uint64_t stream_id, int64_t rows, int64_t cols,
                       __nv_fp8_e4m3* out, int64_t ld);
 

@@ -85,17 +85,15 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
       ldxs = (int64_t)C * E;
     }
     const int e_base = (int)(c_off * E);
-    bool launched = false;
-    if constexpr (E == 16) {  // one 16-element vector: one lane per nonzero
-      if (C <= 1) {
-        spmm_launch<XT, 1, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
-        launched = true;
-      } else if (C == 9) {
-        spmm_launch<XT, 9, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
-        launched = true;
+    if (E == 16 && (C == 1 || C == 9)) {
+      // FP8: one lane per nonzero for one vector, three 9-lane groups for a
+      // 144-element row (instantiated for FP8 only)
+      if constexpr (E == 16) {
+        if (C == 1)
+          spmm_launch<XT, 1, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
+        else
+          spmm_launch<XT, 9, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
       }
-    }
-    if (launched) {
     } else if (C <= 2)
       spmm_launch<XT, 2, 1>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
     else if (C <= 4)

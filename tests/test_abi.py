@@ -49,3 +49,13 @@ def test_chebyshev_coefficients_match_scipy(lib):
     c = chebyshev_coefficients(10, 0.5)
     ref = [ss.iv(0, 0.5), -2 * ss.iv(1, 0.5)] + [(-2 if k & 1 else 2) * ss.iv(k, 0.5) for k in range(2, 10)]
     assert np.array_equal(c, np.array(ref, dtype=np.float32))
+
+
+def test_status_and_precision_constants_match_header():
+    from lightne_gb300 import _lib
+    txt = open(os.path.join(ROOT, "include", "lightne_gb300.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"^#define (LNE_[A-Z0-9_]+) (\d+)", txt, re.M)}
+    assert {"LNE_OK", "LNE_ERR_TABLE_FULL", "LNE_PREC_FP32", "LNE_PREC_BF16", "LNE_PREC_FP8"} <= set(defs)
+    for name, value in defs.items():
+        if hasattr(_lib, name):
+            assert getattr(_lib, name) == value, name

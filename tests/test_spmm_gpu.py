@@ -27,10 +27,6 @@ def random_csr(n, avg, long_rows=(), seed=0):
     return rp, col, val
 
 
-def to_bf16_f64(x):
-    return torch.from_numpy(x).to(torch.bfloat16).to(torch.float64).numpy()
-
-
 DTYPES = {LNE_PREC_FP32: torch.float32, LNE_PREC_BF16: torch.bfloat16, LNE_PREC_FP8: torch.float8_e4m3fn}
 
 
