@@ -7,8 +7,8 @@ Workload (default c2): seeded Chung-Lu power-law graph (exponent 2.1) with
 n = 1,138,499 vertices and m = 2,990,443 undirected edges, T = 10, b = 1,
 samples = 100 * m (-sample_ratio 1.883551 as a float), -sample 0, rank 138
 (d = 128 + 10 oversampling), dim 128, order 10, mu = 0.2, s = 0.5.
-A step is one full embedding: NetSMF sparsifier (path sampling into the pair
-table, trunc-log, canonical CSR), randomized SVD and U sqrt(S), spectral
+A step is one full embedding: NetSMF sparsifier (path sampling, pair
+aggregation, trunc-log, canonical CSR), randomized SVD and U sqrt(S), spectral
 propagation, dense SVD embedding.  `value` is samples per second of the
 whole pipeline (samples / step time) with the graph resident in HBM, for
 the BF16 form (BF16 SpMM operands, FP32 accumulation); the FP32 form is
@@ -141,13 +141,21 @@ def barrier(ws):
 
 
 def allmax(ws, x):
+    """Max of x over the ranks (a CUDA tensor under NCCL, a CPU one under gloo)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(units_per_rank, ws, max_ms):
+    """Whole-job throughput of ws independent replicas: the units all ranks
+    processed over the slowest rank's time."""
+    return units_per_rank * ws / (max_ms / 1e3)
 
 
 # ---------------------------------------------------------------------------
@@ -432,7 +440,7 @@ def run_ours(args, ws, rank, local):
     ms_bf = allmax(ws, ms_bf)
     ms_fp = allmax(ws, ms_fp)
     samples = st_bf[-1]["sparsify"]["samples_emitted"]
-    value = samples * ws / (ms_bf / 1e3)
+    value = replica_value(samples, ws, ms_bf)
 
     # e2e through the C ABI with host (pinned) buffers: upload, pipeline, download
     off_p = torch.from_numpy(off).pin_memory().numpy()
@@ -498,7 +506,7 @@ def run_ours(args, ws, rank, local):
                 "workload": w["label"], "samples_per_step": samples, "nnz": nnz,
                 "l2": "512 MiB flush between timed steps",
                 "embed_secs_bf16": ms_bf / 1e3, "embed_secs_fp32": ms_fp / 1e3,
-                "fp32_form_value": samples * ws / (ms_fp / 1e3), "bf16_over_fp32_speedup": ms_fp / ms_bf,
+                "fp32_form_value": replica_value(samples, ws, ms_fp), "bf16_over_fp32_speedup": ms_fp / ms_bf,
                 "stages_ms_bf16": {
                     "sample": ms_sample, "trunclog": stage(st_bf, "sparsify", "ms_trunclog"),
                     "csr": stage(st_bf, "sparsify", "ms_csr"), "randsvd": stage(st_bf, "randsvd", "ms_total"),
