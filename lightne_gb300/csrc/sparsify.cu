@@ -432,7 +432,7 @@ __global__ void k_insert(const unsigned long long* __restrict__ keys, const doub
 // pairs than its shared table holds, the slice kernel raises
 // kFlagSliceOverflow and the host reruns the batch through the pair table.
 // The all-ones word marks an empty shared slot: its hash preimage is a pair
-// with a vertex id above 2^31, which no graph here has.
+// with a vertex id above 2^31, which int32 vertex ids rule out.
 // ---------------------------------------------------------------------------
 static constexpr int kSliceThreads = 512;
 static constexpr int kSliceSlotsMax = 8192;  // 96 KB of shared memory: two CTAs per SM
