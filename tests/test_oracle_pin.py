@@ -85,3 +85,42 @@ def test_port_table_full_status():
     # mem_ratio 0 and tablesz 1: capacity 2 slots, far fewer than the distinct pairs
     with pytest.raises(RuntimeError, match="status 3"):
         port.sparsify(off, nbrs, 1, walk_len=10, tablesz=1, mem_ratio=0.0, sample_ratio=1.0)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="reference build (oracle/_ref) not present")
+def test_port_matches_live_reference_property():
+    """Property check: on random small graphs and parameters (-sample 0),
+    the port's CSR is the reference's, bit for bit."""
+    hypothesis = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from lightne_gb300 import graphs
+
+    @hypothesis.settings(max_examples=60, deadline=None, derandomize=True)
+    @hypothesis.given(n=st.integers(10, 300), deg=st.integers(1, 4), exp=st.sampled_from([2.1, 2.5, 3.0]),
+                      gseed=st.integers(0, 10 ** 6), seed=st.integers(0, 2 ** 63 - 1),
+                      walk_len=st.integers(1, 12), negative=st.integers(1, 5), upper=st.integers(0, 1),
+                      ratio=st.floats(0.2, 3.0))
+    def check(n, deg, exp, gseed, seed, walk_len, negative, upper, ratio):
+        m = min(n * deg, n * (n - 1) // 4)
+        off, nbrs = graphs.chung_lu(n, m, exp, seed=gseed)
+        if off[-1] == 0:
+            return
+        compared.append(int(off[-1]))
+        ratio = float(np.float32(ratio))
+        tablesz = 4 * walk_len * n * 10
+        prm = dict(seed=seed, walk_len=walk_len, tablesz=tablesz, negative=negative, sample=0,
+                   sample_ratio=ratio, mem_ratio=1.0, upper=upper)
+        with tempfile.TemporaryDirectory() as td:
+            g = os.path.join(td, "g.adj")
+            o = os.path.join(td, "g.csr")
+            graphs.write_adjacency_graph(g, off, nbrs)
+            subprocess.run([REF_BIN, g, o, str(seed), str(walk_len), str(tablesz), str(negative), "0", repr(ratio),
+                            "1.0", str(upper)], check=True, stdout=subprocess.DEVNULL)
+            rp, col, val = graphs.read_csr_bin(o)
+        (rp2, col2, val2), _ = run_port(off, nbrs, prm)
+        assert np.array_equal(rp, rp2) and np.array_equal(col, col2)
+        assert np.array_equal(val.view(np.uint32), val2.view(np.uint32))
+
+    compared = []
+    check()
+    assert len(compared) >= 45, compared

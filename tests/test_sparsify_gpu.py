@@ -129,6 +129,27 @@ def test_device_matches_oracle_midsize_variants(ctx):
         assert_csr_equal(got, ref)
 
 
+def test_device_matches_oracle_random_small_cases(ctx):
+    """Seeded random small graphs and parameters (-sample 0): the device CSR
+    (sliced aggregation by default) is the port's, bit for bit."""
+    rng = np.random.default_rng(2026)
+    for case in range(12):
+        n = int(rng.integers(10, 400))
+        m = min(n * int(rng.integers(1, 5)), n * (n - 1) // 4)
+        off, nbrs = graphs.chung_lu(n, m, float(rng.choice([2.1, 2.5, 3.0])), seed=int(rng.integers(0, 10 ** 6)))
+        if off[-1] == 0:
+            continue
+        walk_len = int(rng.integers(1, 13))
+        prm = dict(seed=int(rng.integers(0, 2 ** 63 - 1)), walk_len=walk_len, tablesz=40 * walk_len * n,
+                   negative=int(rng.integers(1, 6)), sample=0, sample_ratio=float(np.float32(rng.uniform(0.2, 3.0))),
+                   mem_ratio=1.0, upper=int(rng.integers(0, 2)))
+        got, st = device_sparsify(ctx, off, nbrs, prm)
+        ref, _ = port.sparsify(off, nbrs, prm["seed"], walk_len=walk_len, tablesz=prm["tablesz"],
+                               negative=prm["negative"], sample_ratio=prm["sample_ratio"], upper=prm["upper"])
+        assert st["sliced"] == 1, case
+        assert_csr_equal(got, ref)
+
+
 def test_device_is_deterministic(ctx):
     off, nbrs = graphs.chung_lu(3000, 30000, 2.1, seed=4)
     prm = dict(seed=5, walk_len=10, tablesz=2_000_000, negative=1, sample=0, sample_ratio=1.0, mem_ratio=1.0,
