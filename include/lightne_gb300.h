@@ -76,6 +76,12 @@ int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes);
  * and falls back to the pair table in HBM when a slice overflows.
  * slots = 0 always uses the pair table.  The output is the same either way. */
 int lne_ctx_set_sparsify_slices(lne_ctx* ctx, int32_t slots, int32_t slice_bits);
+/* Samples per batch of lne_sparsify's sample buffer (no reference
+ * counterpart: the reference inserts every sample into par_table as it is
+ * drawn).  Default 2^30 (8 GiB of keys; 0 restores it), at least 1024.
+ * Batches are sampled one edge range at a time and added to the pair table
+ * in turn; only a run that fits one batch takes the sliced aggregation. */
+int lne_ctx_set_sparsify_batch(lne_ctx* ctx, int64_t keys);
 /* Wait for all work queued on the context's stream. */
 int lne_ctx_synchronize(lne_ctx* ctx);
 

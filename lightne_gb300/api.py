@@ -48,6 +48,10 @@ class Context:
         (0: always the pair table in HBM) and its slice bits (-1: automatic)."""
         check(_lib.load().lne_ctx_set_sparsify_slices(self.handle, slots, slice_bits))
 
+    def set_sparsify_batch(self, keys: int = 0) -> None:
+        """Samples per batch of the sparsifier (0: the default 2^30)."""
+        check(_lib.load().lne_ctx_set_sparsify_batch(self.handle, keys))
+
     def close(self) -> None:
         if self.handle:
             _lib.load().lne_ctx_destroy(self.handle)

@@ -265,6 +265,14 @@ int lne_ctx_set_sparsify_slices(lne_ctx* ctx, int32_t slots, int32_t slice_bits)
   return LNE_OK;
 }
 
+int lne_ctx_set_sparsify_batch(lne_ctx* ctx, int64_t keys) {
+  LNE_CHECK_ARG(ctx != nullptr, "lne_ctx_set_sparsify_batch: ctx is NULL");
+  LNE_CHECK_ARG(keys == 0 || (keys >= 1024 && keys <= ((int64_t)1 << 34)),
+                "lne_ctx_set_sparsify_batch: keys must be 0 (default) or in [1024, 2^34]");
+  ctx->sparsify_batch_keys = keys == 0 ? ((int64_t)1 << 30) : keys;
+  return LNE_OK;
+}
+
 int lne_ctx_synchronize(lne_ctx* ctx) {
   LNE_CHECK_ARG(ctx != nullptr, "lne_ctx_synchronize: ctx is NULL");
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

@@ -67,6 +67,8 @@ struct lne_ctx {
   // and the number of slice bits (-1: chosen from the sample count).
   int sparsify_slice_slots = 8192;
   int sparsify_slice_bits = -1;
+  // samples per batch of the sparsifier's sample buffer (8 B each)
+  int64_t sparsify_batch_keys = (int64_t)1 << 30;
 };
 
 struct lne_graph {

@@ -916,7 +916,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   // range is processed in batches that fit the buffer.
   const uint64_t per_edge = (uint64_t)exp_rv + 1;
   const uint64_t want_keys = per_edge * (uint64_t)m_dir;
-  const uint64_t max_keys = (uint64_t)1 << 30;  // 8 GiB of keys per batch
+  const uint64_t max_keys = (uint64_t)ctx->sparsify_batch_keys;  // default 2^30: 8 GiB of keys per batch
   const uint64_t buf_keys = want_keys < max_keys ? want_keys : max_keys;
   const int64_t edges_per_batch = (int64_t)std::max<uint64_t>(1, buf_keys / per_edge);
   unsigned long long* keys = nullptr;

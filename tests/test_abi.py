@@ -40,6 +40,7 @@ def test_version_and_error_without_device(lib):
     # NULL out pointer is rejected before any device work
     assert lib.lne_ctx_create(None, 0, None) != 0
     assert lib.lne_ctx_set_sparsify_slices(None, 8192, -1) != 0
+    assert lib.lne_ctx_set_sparsify_batch(None, 0) != 0
 
 
 def test_chebyshev_coefficients_match_scipy(lib):

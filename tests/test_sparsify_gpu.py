@@ -150,6 +150,23 @@ def test_device_matches_oracle_random_small_cases(ctx):
         assert_csr_equal(got, ref)
 
 
+def test_batched_samples_match_reference_golden(ctx):
+    """Sample buffers of a few thousand keys: the edge range is walked in
+    batches, each added to the pair table in turn (the path of runs above
+    2^30 samples); the CSR is still the reference's."""
+    ctx.set_sparsify_batch(4096)
+    try:
+        for path in CASES:
+            z = np.load(path)
+            prm = json.loads(str(z["params"]))
+            got, st = device_sparsify(ctx, z["offsets"], z["nbrs"], prm)
+            assert_csr_equal(got, (z["row_ptr"], z["col"], z["val"]), exact=prm["sample"] == 0)
+            if st["samples_emitted"] > 4096:
+                assert st["sliced"] == 0
+    finally:
+        ctx.set_sparsify_batch(0)
+
+
 def test_device_is_deterministic(ctx):
     off, nbrs = graphs.chung_lu(3000, 30000, 2.1, seed=4)
     prm = dict(seed=5, walk_len=10, tablesz=2_000_000, negative=1, sample=0, sample_ratio=1.0, mem_ratio=1.0,
