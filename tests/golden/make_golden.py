@@ -61,6 +61,15 @@ CASES = {
     "chunglu300_sample1": (lambda: graphs.chung_lu(300, 2000, 2.1, seed=11),
                            dict(seed=3, walk_len=10, tablesz=200000, negative=1, sample=1,
                                 sample_ratio=1.0, mem_ratio=1.0, upper=0)),
+    "single_edge": (lambda: graphs.csr_from_edges(2, np.array([0]), np.array([1])),
+                    dict(seed=21, walk_len=10, tablesz=0, negative=1, sample=0, sample_ratio=8.0,
+                         mem_ratio=1.0, upper=0)),
+    "chunglu500_T20_neg2": (lambda: graphs.chung_lu(500, 3000, 2.1, seed=13),
+                            dict(seed=2 ** 62 + 17, walk_len=20, tablesz=500000, negative=2, sample=0,
+                                 sample_ratio=0.9, mem_ratio=1.0, upper=0)),
+    "hubs2000": (lambda: graphs.chung_lu(2000, 8000, 2.02, seed=14),
+                 dict(seed=31337, walk_len=8, tablesz=0, negative=1, sample=0, sample_ratio=1.2,
+                      mem_ratio=1.0, upper=0)),
 }
 
 RNG_CASES = [(0, 0, 12), (1, 0, 8), (12345, (17 << 32) | 4, 16), (2 ** 63 + 5, 2 ** 40 + 3, 8),
@@ -84,14 +93,19 @@ def run_ref_sparsify(ref_dir: str, off, nbrs, prm: dict):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", nargs="*", help="regenerate only these sparsifier cases (and nothing else)")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + args.ref], check=True)
     for name, (mk, prm) in CASES.items():
+        if args.only and name not in args.only:
+            continue
         off, nbrs = mk()
         rp, col, val = run_ref_sparsify(args.ref, off, nbrs, prm)
         np.savez_compressed(os.path.join(HERE, "sparsify_%s.npz" % name), offsets=off, nbrs=nbrs,
                             row_ptr=rp, col=col, val=val, params=json.dumps(prm))
         print("%-24s n=%d m_dir=%d nnz=%d" % (name, off.size - 1, nbrs.size, rp[-1]))
+    if args.only:
+        return
     streams = []
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_rng")
     for seed, idx, cnt in RNG_CASES:
