@@ -1,12 +1,20 @@
 """ORACLE — test infrastructure, not product code.
 
-The reference's dense stages restated op-for-op in FP32 over torch CPU, for
-the timed CPU baseline of the benchmark (the reference's own MKL build is not
-available: MKL is absent from the reference tree and from the benchmark host).
-Sparse products are CSR x dense (`torch.sparse.mm`), QR is
-`torch.linalg.qr` (Householder, as geqrf + orgqr), small SVDs are
-`torch.linalg.svd`; every thread the host offers is used.
+The reference's whole pipeline on the host cores, for the timed CPU baseline
+of the benchmark: the C port of the sparsifier (oracle/sparsify_port.c), then
+the dense stages in FP32 as the reference runs them through MKL — CSR x dense
+products on every core (oracle/spmm_port.c, in place of mkl_sparse_s_mm),
+Householder QR (`torch.linalg.qr`, as geqrf + orgqr), GEMMs and small SVDs
+(`torch.linalg`, every thread).  The reference's own MKL build is not
+available (MKL is absent from the reference tree and from the benchmark
+host), so this is a port, not the reference binary.
 
+The pipeline is an ordered list of work units; running every unit once, in
+order, is one whole embedding of the workload.  The benchmark's CPU arm times
+its steps as consecutive groups of units, so that its steps together run the
+pipeline exactly once, with nothing scaled or extrapolated.
+
+  sparsifier    LightNE/PathEmbed.h:81-369 (port: oracle/sparsify_port.c)
   randsvd       LightNE/mklredsvd/mklredsvd.cc:93-403 + PathEmbed.h:371-408
   propagate     LightNE/SpectralPropagation.h:45-221
   dense_embed   LightNE/SpectralPropagation.h:16-43
@@ -19,6 +27,8 @@ import time
 import numpy as np
 import torch
 
+from oracle import port
+
 
 def set_threads(n: int | None = None) -> int:
     n = n or os.cpu_count() or 1
@@ -26,22 +36,17 @@ def set_threads(n: int | None = None) -> int:
     return n
 
 
-def csr_tensor(row_ptr, col, val, n):
-    return torch.sparse_csr_tensor(torch.from_numpy(np.ascontiguousarray(row_ptr, dtype=np.int64)),
-                                   torch.from_numpy(np.ascontiguousarray(col, dtype=np.int64)),
-                                   torch.from_numpy(np.ascontiguousarray(val, dtype=np.float32)), size=(n, n))
-
-
 def operator_csr(offsets, nbrs, mu=0.2):
-    """The CSR of M the reference builds (self loop first, SpectralPropagation.h:51-75)."""
+    """The CSR of M the reference builds (self loop first, values computed in
+    double and narrowed to float, SpectralPropagation.h:51-75)."""
     n = offsets.size - 1
     deg = np.diff(offsets)
-    dt = (deg + 1).astype(np.float32).astype(np.float64)
+    dt = (deg + 1).astype(np.float64)
     mu_f = float(np.float32(mu))
     diag = (1.0 - mu_f - 1.0 / dt).astype(np.float32)
     offv = (-1.0 / dt).astype(np.float32)
     rp = offsets + np.arange(n + 1)
-    col = np.empty(rp[-1], dtype=np.int64)
+    col = np.empty(rp[-1], dtype=np.int32)
     val = np.empty(rp[-1], dtype=np.float32)
     col[rp[:-1]] = np.arange(n)
     val[rp[:-1]] = diag
@@ -49,91 +54,174 @@ def operator_csr(offsets, nbrs, mu=0.2):
     mask[rp[:-1]] = False
     col[mask] = nbrs
     val[mask] = np.repeat(offv, deg)
-    return csr_tensor(rp, col, val, n)
+    return rp.astype(np.int64), col, val
 
 
-def randsvd(A, rank, dim, seed=777):
-    g = torch.Generator().manual_seed(seed)
-    n = A.shape[0]
-    O = torch.randn(n, rank, generator=g)
-    Y = torch.sparse.mm(A, O)
-    Q, _ = torch.linalg.qr(Y)
-    B = torch.sparse.mm(A, Q)
-    P = torch.randn(rank, rank, generator=g)
-    Z, _ = torch.linalg.qr(B @ P)
-    C = Z.T @ B
-    U, S, _ = torch.linalg.svd(C)
-    return (Z @ U[:, :dim]) * torch.sqrt(S[:dim]), S
-
-
-def propagate(M, Adj_plus_I, a, order=10, s=0.5):
+def bessel_weights(order, s):
     import scipy.special as ss
     sf = float(np.float32(s))
-    Lx0 = a.clone()
-    tmp = torch.sparse.mm(M, a)
-    Lx1 = 0.5 * torch.sparse.mm(M, tmp) - a
-    conv = float(np.float32(ss.iv(0, sf))) * Lx0 + float(np.float32(-2 * ss.iv(1, sf))) * Lx1
-    for k in range(2, order):
-        tmp = torch.sparse.mm(M, Lx1)
-        Lx2 = torch.sparse.mm(M, tmp) - Lx0 - 2 * Lx1
-        conv += float(np.float32((-2 if k & 1 else 2) * ss.iv(k, sf))) * Lx2
-        Lx0, Lx1 = Lx1, Lx2
-    a = a - conv
-    return torch.sparse.mm(Adj_plus_I, a)
+    c = [float(np.float32(ss.iv(0, sf))), float(np.float32(-2 * ss.iv(1, sf)))]
+    c += [float(np.float32((-2 if k & 1 else 2) * ss.iv(k, sf))) for k in range(2, order)]
+    return c
 
 
-def dense_embed(x):
-    U, S, _ = torch.linalg.svd(x, full_matrices=False)
-    e = U * torch.sqrt(S)
-    nrm = e.norm(dim=1, keepdim=True)
-    return torch.where(nrm > 1e-5, e / nrm, e)
+def _blocks(total, parts):
+    """parts + 1 boundaries splitting [0, total) into near-equal ranges."""
+    return [total * i // parts for i in range(parts + 1)]
 
 
-def timed(fn, *a, **k):
-    t0 = time.perf_counter()
-    out = fn(*a, **k)
-    return out, time.perf_counter() - t0
+class Pipeline:
+    """One whole embedding of a workload on the host cores, as work units.
+
+    w: dict with walk_len, tablesz, sample_ratio (float), rank, dim, order.
+    Units, in order: the sampler over `sample_units` vertex ranges of equal
+    directed-edge counts; the trunc-log + CSR build; the sketch; A Omega in
+    `row_units` row blocks; QR; A Q in row blocks; B P, QR, C = Z^T B, core
+    SVD and U sqrt(S); the operator build; one unit per Chebyshev order; the
+    (A + I) product; the dense SVD embedding."""
+
+    def __init__(self, off, nbrs, w, seed, nthreads=0, sample_units=32, row_units=16, mu=0.2, s=0.5,
+                 svd_seed=777):
+        self.off = np.ascontiguousarray(off, dtype=np.int64)
+        self.nbrs = np.ascontiguousarray(nbrs, dtype=np.int32)
+        self.n = self.off.size - 1
+        self.w = w
+        self.seed = seed
+        self.cores = set_threads(nthreads or None)
+        self.mu, self.s, self.svd_seed = mu, s, svd_seed
+        self.stage_s: dict[str, float] = {}
+        self.units = []
+        # sampler ranges cut on directed-edge counts
+        m_dir = int(self.off[-1])
+        cuts = np.searchsorted(self.off, np.array(_blocks(m_dir, sample_units)), side="left")
+        cuts[0], cuts[-1] = 0, self.n
+        cuts = np.maximum.accumulate(cuts)
+        self.units.append(("sparsify", self._u_session))
+        for i in range(sample_units):
+            self.units.append(("sparsify", lambda a=int(cuts[i]), b=int(cuts[i + 1]): self._u_sample(a, b)))
+        self.units.append(("sparsify", self._u_finish))
+        rb = _blocks(self.n, row_units)
+        self.units.append(("randsvd", self._u_sketch))
+        for i in range(row_units):
+            self.units.append(("randsvd", lambda a=rb[i], b=rb[i + 1]: self._u_spmm("O", "Y", a, b)))
+        self.units.append(("randsvd", self._u_qr1))
+        for i in range(row_units):
+            self.units.append(("randsvd", lambda a=rb[i], b=rb[i + 1]: self._u_spmm("Q", "B", a, b)))
+        self.units.append(("randsvd", self._u_core))
+        self.units.append(("propagate", self._u_operator))
+        for k in range(1, max(w["order"], 2)):
+            self.units.append(("propagate", lambda k=k: self._u_order(k)))
+        self.units.append(("propagate", self._u_aplusi))
+        self.units.append(("dense_embed", self._u_dense))
+
+    # -- sparsifier -------------------------------------------------------
+    def _u_session(self):
+        w = self.w
+        self.sess = port.Session(self.off, self.nbrs, self.seed, walk_len=w["walk_len"], tablesz=w["tablesz"],
+                                 sample_ratio=float(np.float32(w["sample_ratio"])), nthreads=self.cores)
+
+    def _u_sample(self, a, b):
+        self.sess.sample(a, b)
+
+    def _u_finish(self):
+        self.csr, self.sp_stats = self.sess.finish()
+        self.sess = None
+
+    # -- randomized SVD (mklredsvd.cc:93-403) ------------------------------
+    def _u_sketch(self):
+        r = self.w["rank"]
+        self.gen = torch.Generator().manual_seed(self.svd_seed)
+        self.O = torch.randn(self.n, r, generator=self.gen).numpy()
+        self.Y = np.empty((self.n, r), np.float32)
+
+    def _u_spmm(self, src, dst, a, b):
+        rp, col, val = self.csr
+        port.spmm(rp, col, val, getattr(self, src), rows=(a, b), out=getattr(self, dst), nthreads=self.cores)
+
+    def _u_qr1(self):
+        self.Q = torch.linalg.qr(torch.from_numpy(self.Y)).Q.contiguous().numpy()
+        self.B = np.empty_like(self.Q)
+        self.O = self.Y = None
+
+    def _u_core(self):
+        r, d = self.w["rank"], self.w["dim"]
+        B = torch.from_numpy(self.B)
+        P = torch.randn(r, r, generator=self.gen)
+        Z = torch.linalg.qr(B @ P).Q
+        C = Z.T @ B
+        U, S, _ = torch.linalg.svd(C)
+        self.emb = ((Z @ U[:, :d]) * torch.sqrt(S[:d])).contiguous().numpy()
+        self.S = S.numpy()
+        self.Q = self.B = None
+
+    # -- spectral propagation (SpectralPropagation.h:45-221) ---------------
+    def _u_operator(self):
+        self.M = operator_csr(self.off, self.nbrs, self.mu)
+        self.c = bessel_weights(max(self.w["order"], 2), self.s)
+
+    def _mm(self, x):
+        rp, col, val = self.M
+        return port.spmm(rp, col, val, x, nthreads=self.cores)
+
+    def _u_order(self, k):
+        if k == 1:
+            a = self.emb
+            self.L0 = a
+            tmp = self._mm(a)
+            self.L1 = 0.5 * self._mm(tmp) - a
+            self.conv = self.c[0] * self.L0 + self.c[1] * self.L1
+            return
+        tmp = self._mm(self.L1)
+        L2 = self._mm(tmp) - self.L0 - 2 * self.L1
+        self.conv += self.c[k] * L2
+        self.L0, self.L1 = self.L1, L2
+
+    def _u_aplusi(self):
+        a = (self.emb - self.conv).astype(np.float32)
+        ones = np.ones(self.nbrs.size, np.float32)
+        self.y = a + port.spmm(self.off, self.nbrs, ones, a, nthreads=self.cores)
+        self.L0 = self.L1 = self.conv = None
+
+    def _u_dense(self):
+        U, S, _ = torch.linalg.svd(torch.from_numpy(self.y), full_matrices=False)
+        e = U * torch.sqrt(S)
+        nrm = e.norm(dim=1, keepdim=True)
+        self.out = torch.where(nrm > 1e-5, e / nrm, e).numpy()
+
+    # -- driving ------------------------------------------------------------
+    def run(self, lo=0, hi=None):
+        """Runs units [lo, hi) in order; returns their wall seconds."""
+        hi = len(self.units) if hi is None else hi
+        total = 0.0
+        for name, fn in self.units[lo:hi]:
+            t0 = time.perf_counter()
+            fn()
+            dt = time.perf_counter() - t0
+            self.stage_s[name] = self.stage_s.get(name, 0.0) + dt
+            total += dt
+        return total
+
+    @property
+    def samples(self) -> int:
+        return int(self.sp_stats["samples"])
 
 
-def dense_stage_seconds(row_ptr, col, val, offsets, nbrs, rank=138, dim=128, order=10, row_frac=0.05,
-                        seed=0):
-    """Seconds of the reference's dense stages on this host, measured on a
-    bounded sample and scaled by operation count:
-      - one A x Omega product over a random `row_frac` of A's rows, scaled
-        by nnz to the two products of the randomized SVD;
-      - Householder QR, the B P and Z U GEMMs and the core SVD on the full
-        n x rank panels (QR and GEMMs once each, scaled to their counts);
-      - two operator products of the propagation, scaled to its 19;
-      - the n x dim dense SVD.
-    Returns a dict of per-stage seconds."""
-    n = offsets.size - 1
-    rng = np.random.default_rng(seed)
-    rows = np.sort(rng.choice(n, max(1, int(n * row_frac)), replace=False))
-    lens = row_ptr[rows + 1] - row_ptr[rows]
-    sub_rp = np.zeros(rows.size + 1, np.int64)
-    np.cumsum(lens, out=sub_rp[1:])
-    idx = np.concatenate([np.arange(row_ptr[r], row_ptr[r + 1]) for r in rows]) if lens.sum() else np.zeros(0, int)
-    Asub = torch.sparse_csr_tensor(torch.from_numpy(sub_rp), torch.from_numpy(col[idx].astype(np.int64)),
-                                   torch.from_numpy(val[idx]), size=(rows.size, n))
-    O = torch.randn(n, rank)
-    _, t_sub = timed(torch.sparse.mm, Asub, O)
-    frac_nnz = max(lens.sum(), 1) / max(row_ptr[-1], 1)
-    t_spmm = t_sub / frac_nnz
-    Y = torch.randn(n, rank)
-    _, t_qr = timed(torch.linalg.qr, Y)
-    P = torch.randn(rank, rank)
-    _, t_gemm = timed(torch.matmul, Y, P)
-    C = torch.randn(rank, rank)
-    _, t_svd = timed(torch.linalg.svd, C)
-    M = operator_csr(offsets, nbrs)
-    a = torch.randn(n, dim)
-    _, t_op = timed(torch.sparse.mm, M, a)
-    _, t_op2 = timed(torch.sparse.mm, M, a)
-    x = torch.randn(n, dim)
-    _, t_dense = timed(dense_embed, x)
-    return {
-        "randsvd": 2 * t_spmm + 2 * t_qr + 3 * t_gemm + t_svd,
-        "propagate": 19 * 0.5 * (t_op + t_op2),
-        "dense_embed": t_dense,
-        "spmm_sample_rows": int(rows.size),
-    }
+def step_groups(units: int, steps: int):
+    """Boundaries cutting `units` consecutive units into `steps` groups (as
+    equal in count as possible; every group non-empty while steps <= units)."""
+    steps = max(1, min(steps, units))
+    return _blocks(units, steps)
+
+
+def warmup(off, nbrs, w, seed, nthreads, units):
+    """Warm-up for the timed CPU steps: the sampler over the first `units`
+    of 64 edge ranges in a throwaway table, and one small host product."""
+    sess = port.Session(off, nbrs, seed, walk_len=w["walk_len"], tablesz=w["tablesz"],
+                        sample_ratio=float(np.float32(w["sample_ratio"])), nthreads=nthreads)
+    n = off.size - 1
+    cuts = np.searchsorted(off, np.array(_blocks(int(off[-1]), 64)), side="left")
+    for i in range(min(units, 64)):
+        sess.sample(int(cuts[i]), int(min(cuts[i + 1], n)))
+    sess.free()
+    x = np.ones((n, 8), np.float32)
+    port.spmm(off, nbrs, np.ones(nbrs.size, np.float32), x, nthreads=nthreads)

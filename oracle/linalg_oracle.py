@@ -33,16 +33,14 @@ import scipy.special as ss
 
 
 def spmm64(A: sp.csr_matrix, X: np.ndarray) -> np.ndarray:
-    """A @ X in FP64.  Uses torch's multi-threaded CPU CSR product when torch
-    is importable (same FP64 arithmetic, faster on large matrices)."""
-    try:
-        import torch
-    except ImportError:
+    """A @ X in FP64 on every host core (the row-parallel C product of
+    oracle/spmm_port.c; FP64 values, operand and sums)."""
+    from oracle import port
+    A = A.tocsr()
+    if A.shape[0] >= 2 ** 31 or A.shape[1] >= 2 ** 31:
         return A @ X
-    At = torch.sparse_csr_tensor(torch.from_numpy(A.indptr.astype(np.int64)),
-                                 torch.from_numpy(A.indices.astype(np.int64)),
-                                 torch.from_numpy(A.data.astype(np.float64)), size=A.shape)
-    return torch.sparse.mm(At, torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64))).numpy()
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    return port.spmm(A.indptr, A.indices, A.data.astype(np.float64), X)
 
 
 def qr_pos(Y: np.ndarray) -> np.ndarray:

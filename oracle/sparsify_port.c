@@ -42,6 +42,11 @@
 
 #define LNE_EMPTY_KEY UINT64_MAX
 
+/* Status codes shared with the product's C ABI. */
+#define PORT_OK 0
+#define PORT_ERR_ALLOC 2
+#define PORT_ERR_TABLE_FULL 3
+
 static inline uint64_t h64(uint64_t x) {
   x = (x ^ (x >> 30)) * UINT64_C(0xbf58476d1ce4e5b9);
   x = (x ^ (x >> 27)) * UINT64_C(0x94d049bb133111eb);
@@ -173,13 +178,75 @@ static int cmp_u64(const void* a, const void* b) {
   return x < y ? -1 : (x > y ? 1 : 0);
 }
 
-/* Status codes shared with the product's C ABI. */
-#define PORT_OK 0
-#define PORT_ERR_ALLOC 2
-#define PORT_ERR_TABLE_FULL 3
+/*
+ * A sparsifier run in steps: lne_port_session_create sizes and clears the
+ * table, lne_port_session_sample runs the per-edge sampler over the out-edges
+ * of the vertices [u_begin, u_end) (any number of calls, in any order: the
+ * table's final contents do not depend on it), lne_port_session_finish runs
+ * M_exact, the trunc-log map and the CSR build and releases the table.
+ */
+typedef struct {
+  int64_t n;
+  const int64_t* off;
+  const int32_t* nbr;
+  uint64_t seed;
+  int64_t walk_len, negative;
+  int sample, upper;
+  double prm[7];
+  table_t t;
+  uint64_t emitted;
+  double sec_sample;
+} port_session_t;
+
+void* lne_port_session_create(int64_t n, const int64_t* off, const int32_t* nbr, uint64_t seed, int64_t walk_len,
+                              int64_t tablesz, int64_t negative, int sample, float sample_ratio, float mem_ratio,
+                              int upper, int nthreads) {
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  port_session_t* ps = (port_session_t*)calloc(1, sizeof(port_session_t));
+  if (!ps) return NULL;
+  ps->n = n; ps->off = off; ps->nbr = nbr; ps->seed = seed; ps->walk_len = walk_len;
+  ps->negative = negative; ps->sample = sample; ps->upper = upper;
+  lne_port_params(n, off[n], walk_len, tablesz, sample_ratio, mem_ratio, ps->prm);
+  uint64_t cap = (uint64_t)ps->prm[6];
+  ps->t.slots = (slot_t*)malloc(cap * sizeof(slot_t));
+  if (!ps->t.slots) { free(ps); return NULL; }
+  ps->t.mask = cap - 1;
+  ps->t.full = 0;
+  slot_t* sl = ps->t.slots;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)cap; ++i) { sl[i].key = LNE_EMPTY_KEY; sl[i].val = 0.0; }
+  return ps;
+}
+
+int64_t lne_port_session_sample(void* h, int64_t u_begin, int64_t u_end) {
+  port_session_t* ps = (port_session_t*)h;
+  const int64_t* off = ps->off;
+  const int32_t* nbr = ps->nbr;
+  double logn = ps->prm[0], frac = ps->prm[4];
+  uint64_t exp_rv_rounded = (uint64_t)ps->prm[3];
+  double t0 = now_s();
+  uint64_t emitted = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : emitted)
+  for (int64_t u = u_begin; u < u_end; ++u) {
+    for (int64_t e = off[u]; e < off[u + 1]; ++e) {
+      emitted += sample_edge(off, nbr, ps->seed, (uint32_t)u, (uint32_t)nbr[e], (uint64_t)ps->walk_len,
+                             ps->sample, exp_rv_rounded, frac, logn, &ps->t);
+    }
+  }
+  ps->sec_sample += now_s() - t0;
+  ps->emitted += emitted;
+  return ps->t.full ? -PORT_ERR_TABLE_FULL : (int64_t)emitted;
+}
+
+void lne_port_session_free(void* h) {
+  port_session_t* ps = (port_session_t*)h;
+  if (!ps) return;
+  free(ps->t.slots);
+  free(ps);
+}
 
 /*
- * Full sparsifier.  stats (double[16]):
+ * Trunc-log and CSR of a session; frees the session.  stats (double[16]):
  *  0 logn, 1 M, 2 1/lambda, 3 exp_rv_rounded, 4 frac, 5 table_size, 6 capacity,
  *  7 samples emitted, 8 M_exact, 9 factor, 10 nnz_upper (kept slots),
  *  11 nnz, 12 seconds (sampling+insert), 13 seconds (trunc-log + CSR),
@@ -187,39 +254,19 @@ static int cmp_u64(const void* a, const void* b) {
  * On success *out_col / *out_val are malloc'd (free with lne_port_free);
  * row_ptr is caller-allocated int64[n+1].
  */
-int lne_port_sparsify(int64_t n, const int64_t* off, const int32_t* nbr, uint64_t seed,
-                      int64_t walk_len, int64_t tablesz, int64_t negative, int sample,
-                      float sample_ratio, float mem_ratio, int upper, int nthreads,
-                      int64_t* row_ptr, int32_t** out_col, float** out_val, double* stats) {
-  if (nthreads > 0) omp_set_num_threads(nthreads);
-  int64_t m_dir = off[n];
-  double prm[7];
-  lne_port_params(n, m_dir, walk_len, tablesz, sample_ratio, mem_ratio, prm);
-  for (int i = 0; i < 7; ++i) stats[i] = prm[i];
-  double logn = prm[0], frac = prm[4];
-  uint64_t exp_rv_rounded = (uint64_t)prm[3];
-  uint64_t cap = (uint64_t)prm[6];
-  table_t t;
-  t.slots = (slot_t*)malloc(cap * sizeof(slot_t));
-  if (!t.slots) return PORT_ERR_ALLOC;
-  t.mask = cap - 1;
-  t.full = 0;
-#pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < (int64_t)cap; ++i) { t.slots[i].key = LNE_EMPTY_KEY; t.slots[i].val = 0.0; }
-
-  double t0 = now_s();
-  uint64_t emitted = 0;
-#pragma omp parallel for schedule(dynamic, 64) reduction(+ : emitted)
-  for (int64_t u = 0; u < n; ++u) {
-    for (int64_t e = off[u]; e < off[u + 1]; ++e) {
-      emitted += sample_edge(off, nbr, seed, (uint32_t)u, (uint32_t)nbr[e], (uint64_t)walk_len,
-                             sample, exp_rv_rounded, frac, logn, &t);
-    }
-  }
+int lne_port_session_finish(void* h, int64_t* row_ptr, int32_t** out_col, float** out_val, double* stats) {
+  port_session_t* ps = (port_session_t*)h;
+  const int64_t n = ps->n;
+  const int64_t* off = ps->off;
+  const int64_t m_dir = off[n];
+  const int upper = ps->upper;
+  table_t t = ps->t;
+  uint64_t cap = (uint64_t)ps->prm[6];
+  for (int i = 0; i < 7; ++i) stats[i] = ps->prm[i];
+  stats[7] = (double)ps->emitted;
+  stats[12] = ps->sec_sample;
+  if (t.full) { lne_port_session_free(ps); return PORT_ERR_TABLE_FULL; }
   double t1 = now_s();
-  stats[7] = (double)emitted;
-  stats[12] = t1 - t0;
-  if (t.full) { free(t.slots); return PORT_ERR_TABLE_FULL; }
 
   /* M_exact: sum of weights in slot order. */
   double M_exact = 0.0;
@@ -229,12 +276,12 @@ int lne_port_sparsify(int64_t n, const int64_t* off, const int32_t* nbr, uint64_
   stats[8] = M_exact;
   stats[15] = (double)distinct;
   double vol = (double)(size_t)m_dir;
-  double factor = vol * (double)(size_t)m_dir / M_exact / 2 / (double)(size_t)negative;
+  double factor = vol * (double)(size_t)m_dir / M_exact / 2 / (double)(size_t)ps->negative;
   stats[9] = factor;
 
   /* Trunc-log map (PathEmbed.h:203-218), then row counts. */
   int64_t* cnt = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
-  if (!cnt) { free(t.slots); return PORT_ERR_ALLOC; }
+  if (!cnt) { lne_port_session_free(ps); return PORT_ERR_ALLOC; }
   uint64_t kept = 0;
 #pragma omp parallel for schedule(static) reduction(+ : kept)
   for (int64_t i = 0; i < (int64_t)cap; ++i) {
@@ -260,7 +307,7 @@ int lne_port_sparsify(int64_t n, const int64_t* off, const int32_t* nbr, uint64_
   int64_t nnz = row_ptr[n];
   stats[11] = (double)nnz;
   uint64_t* packed = (uint64_t*)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(uint64_t));
-  if (!packed) { free(cnt); free(t.slots); return PORT_ERR_ALLOC; }
+  if (!packed) { free(cnt); lne_port_session_free(ps); return PORT_ERR_ALLOC; }
   memset(cnt, 0, (size_t)(n + 1) * sizeof(int64_t));
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < (int64_t)cap; ++i) {
@@ -281,7 +328,10 @@ int lne_port_sparsify(int64_t n, const int64_t* off, const int32_t* nbr, uint64_
     qsort(packed + row_ptr[i], (size_t)(row_ptr[i + 1] - row_ptr[i]), sizeof(uint64_t), cmp_u64);
   int32_t* col = (int32_t*)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int32_t));
   float* val = (float*)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(float));
-  if (!col || !val) { free(col); free(val); free(packed); free(cnt); free(t.slots); return PORT_ERR_ALLOC; }
+  if (!col || !val) {
+    free(col); free(val); free(packed); free(cnt); lne_port_session_free(ps);
+    return PORT_ERR_ALLOC;
+  }
 #pragma omp parallel for schedule(static)
   for (int64_t j = 0; j < nnz; ++j) {
     col[j] = (int32_t)(packed[j] >> 32);
@@ -293,10 +343,23 @@ int lne_port_sparsify(int64_t n, const int64_t* off, const int32_t* nbr, uint64_
   stats[14] = (double)omp_get_max_threads();
   free(packed);
   free(cnt);
-  free(t.slots);
+  lne_port_session_free(ps);
   *out_col = col;
   *out_val = val;
   return PORT_OK;
+}
+
+/* Full sparsifier in one call: a session over all vertices (stats and
+ * outputs as lne_port_session_finish). */
+int lne_port_sparsify(int64_t n, const int64_t* off, const int32_t* nbr, uint64_t seed,
+                      int64_t walk_len, int64_t tablesz, int64_t negative, int sample,
+                      float sample_ratio, float mem_ratio, int upper, int nthreads,
+                      int64_t* row_ptr, int32_t** out_col, float** out_val, double* stats) {
+  void* ps = lne_port_session_create(n, off, nbr, seed, walk_len, tablesz, negative, sample, sample_ratio,
+                                     mem_ratio, upper, nthreads);
+  if (!ps) return PORT_ERR_ALLOC;
+  lne_port_session_sample(ps, 0, n);
+  return lne_port_session_finish(ps, row_ptr, out_col, out_val, stats);
 }
 
 /*

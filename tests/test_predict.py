@@ -1,8 +1,9 @@
 """Node-classification evaluation (lightne_gb300.predict, the role of
 LightNE/predict.py): the ShuffleSplit indices, the one-vs-rest L2 logistic
 regression optimum, top-k prediction and micro/macro F1 against
-scikit-learn's liblinear run of the reference's predict_cv (on the host
-where scikit-learn is installed)."""
+scikit-learn's liblinear run of the reference's predict_cv: live where
+scikit-learn is installed, and through committed scores
+(tests/golden/predict_sklearn.json) on the device."""
 import numpy as np
 import pytest
 import torch
@@ -66,8 +67,27 @@ def test_f1_definitions():
 
 
 @pytest.mark.gpu
-def test_predict_cv_on_device_matches_host():
-    X, Y = _data(seed=3)
-    a = predict.predict_cv(X, Y, train_ratio=0.5, n_splits=2, random_state=4, device="cuda")
-    b = predict.predict_cv(X, Y, train_ratio=0.5, n_splits=2, random_state=4, device="cpu")
-    assert abs(a[0] - b[0]) < 0.2 and abs(a[1] - b[1]) < 0.2
+@pytest.mark.parametrize("case", range(2))
+def test_predict_cv_on_device_matches_sklearn_liblinear(case):
+    """The device run against scikit-learn's liblinear F1 scores on the same
+    data and splits (tests/golden/predict_sklearn.json, made by
+    tests/golden/make_predict_golden.py), within 0.5 F1 points as on the host."""
+    import json
+    import os
+    ref = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "predict_sklearn.json")))[case]
+    X, Y = _data(seed=ref["data_seed"])
+    mi, ma = predict.predict_cv(X, Y, train_ratio=ref["train_ratio"], n_splits=ref["n_splits"],
+                                random_state=ref["split_seed"], C=ref["C"], device="cuda")[:2]
+    assert abs(mi - ref["micro_f1"]) < 0.5, (mi, ref["micro_f1"])
+    assert abs(ma - ref["macro_f1"]) < 0.5, (ma, ref["macro_f1"])
+
+
+def test_predict_cv_host_matches_sklearn_fixture():
+    """The same comparison on the host (no GPU), against the committed scores."""
+    import json
+    import os
+    for ref in json.load(open(os.path.join(os.path.dirname(__file__), "golden", "predict_sklearn.json"))):
+        X, Y = _data(seed=ref["data_seed"])
+        mi, ma = predict.predict_cv(X, Y, train_ratio=ref["train_ratio"], n_splits=ref["n_splits"],
+                                    random_state=ref["split_seed"], C=ref["C"], device="cpu")[:2]
+        assert abs(mi - ref["micro_f1"]) < 0.5 and abs(ma - ref["macro_f1"]) < 0.5, (mi, ma, ref)
