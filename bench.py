@@ -1,7 +1,8 @@
 """Benchmark of the LightNE embedding pipeline on one GB300 (driver contract).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c2|c1] [--accuracy]
+                    [--workload c2|c1|c3|c5] [--no-accuracy] [--no-cpu-baseline]
+                    [--micro gram|gemm|spmm|spmm16|spmm8|prop] [--quick]
 
 Workload (default c2): seeded Chung-Lu power-law graph (exponent 2.1) with
 n = 1,138,499 vertices and m = 2,990,443 undirected edges, T = 10, b = 1,
@@ -11,11 +12,14 @@ A step is one full embedding: NetSMF sparsifier (path sampling, pair
 aggregation, trunc-log, canonical CSR), randomized SVD and U sqrt(S), spectral
 propagation, dense SVD embedding.  `value` is samples per second of the
 whole pipeline (samples / step time) with the graph resident in HBM, for
-the BF16 form (BF16 SpMM operands, FP32 accumulation); the FP32 form is
-timed in the same run and reported beside it.  `e2e` is the same metric
-through the C ABI with host buffers: graph upload, pipeline, embedding
-download every step.  --accuracy additionally measures both forms against
-the FP64 oracle (minutes of host time).
+the FP16 form (FP16 SpMM operands, FP32 accumulation); the BF16 and FP32
+forms are timed in the same run and reported beside it.  `e2e` is the same
+metric through the C ABI with host buffers: graph upload, pipeline,
+embedding download every step.  After the timed region, every form is
+measured against the FP64 oracle (stage errors and the final embedding's,
+with the 1e-3 gate), and the CPU port of the reference runs one whole
+embedding on the host cores (`cpu_baseline`), whose sparse matrix is
+compared bit for bit with the device's (`parity`).
 
 Under torchrun (N > 1) every rank runs an independent replica of the
 workload: the pipeline has no data-path exchange on one graph; `value` is
@@ -161,76 +165,55 @@ def replica_value(units_per_rank, ws, max_ms):
 # ---------------------------------------------------------------------------
 # CPU side (the oracle port of the reference, timed on the host cores)
 # ---------------------------------------------------------------------------
-def cpu_sparsify(off, nbrs, w):
-    """The C port of the sparsifier on the full workload, all host threads:
-    returns the CSR and its stats (sampling and CSR seconds)."""
-    from oracle import cpu_pipeline, port
-    cores = cpu_pipeline.set_threads()
-    ratio = float(np.float32(w["sample_ratio"]))
-    return port.sparsify(off, nbrs, w["seed"], walk_len=w["walk_len"], tablesz=w["tablesz"], sample_ratio=ratio,
-                         nthreads=cores)
+def cpu_pipeline_run(off, nbrs, w, seed):
+    """One whole embedding of the workload by the CPU port of the reference
+    pipeline (oracle/cpu_pipeline.py), every host thread, nothing scaled.
+    Returns (pipeline, seconds)."""
+    from oracle import cpu_pipeline
+    pipe = cpu_pipeline.Pipeline(off, nbrs, w, seed)
+    cpu_pipeline.warmup(off, nbrs, w, seed, pipe.cores, 2)
+    secs = pipe.run()
+    return pipe, secs
 
 
-def cpu_pipeline_seconds(off, nbrs, w, sp=None, edge_frac=None):
-    """Seconds of the reference pipeline on this host's cores: the C port of
-    the sparsifier (the full run in `sp`, or, with edge_frac, the sampler
-    over that fraction of the edges scaled to all samples plus the full
-    run's CSR time), and the dense stages on a bounded sample scaled by
-    operation count (oracle/cpu_pipeline.py)."""
-    from oracle import cpu_pipeline, port
-    cores = cpu_pipeline.set_threads()
-    if sp is None:
-        sp = cpu_sparsify(off, nbrs, w)
-    (rp, col, val), st = sp
-    t_sample, t_csr = st["sec_sample"], st["sec_csr"]
-    if edge_frac is not None:
-        ratio = float(np.float32(w["sample_ratio"]))
-        got, sec = port.sample_range(off, nbrs, w["seed"], 0, int(nbrs.size * edge_frac), walk_len=w["walk_len"],
-                                     tablesz=w["tablesz"], sample_ratio=ratio, nthreads=cores)
-        t_sample = sec * st["samples"] / max(got, 1)
-    dense = cpu_pipeline.dense_stage_seconds(rp, col, val, off, nbrs, rank=w["rank"], dim=w["dim"],
-                                             order=w["order"])
-    total = t_sample + t_csr + dense["randsvd"] + dense["propagate"] + dense["dense_embed"]
-    return {"total": total, "sampler": t_sample, "csr": t_csr, "randsvd": dense["randsvd"],
-            "propagate": dense["propagate"], "dense_embed": dense["dense_embed"], "samples": st["samples"],
-            "cores": cores, "spmm_sample_rows": dense["spmm_sample_rows"], "edge_frac": edge_frac}
-
-
-def cpu_sample_text(c):
-    samp = ("sampler over the first %.0f%% of directed edges scaled to all samples" % (100 * c["edge_frac"])
-            if c["edge_frac"] else "full sparsifier run")
-    return ("C port of the sparsifier (%s: %.1f s sampling, %.1f s CSR); randomized SVD, propagation and dense "
-            "SVD in torch FP32 on %d threads, SpMM timed over a 5%% row sample (%d rows) and scaled by nnz, "
-            "QR/GEMM/SVD timed once and scaled by count"
-            % (samp, c["sampler"], c["csr"], c["cores"], c["spmm_sample_rows"]))
+def cpu_sample_text(pipe, secs, steps=None):
+    st = pipe.stage_s
+    head = ("one whole embedding, every unit run once in order" if steps is None else
+            "one whole embedding cut into %d steps of consecutive work units (the steps together run the "
+            "pipeline once, in order)" % steps)
+    return ("%s: C port of the sparsifier (%.1f s: sampler + pair table + trunc-log + CSR), randomized SVD "
+            "(%.1f s), propagation (%.1f s) and dense SVD (%.1f s) in FP32 with row-parallel C CSR products "
+            "and torch-CPU QR/GEMM/SVD on %d threads; %.1f s in total, nothing scaled"
+            % (head, st.get("sparsify", 0.0), st.get("randsvd", 0.0), st.get("propagate", 0.0),
+               st.get("dense_embed", 0.0), pipe.cores, secs))
 
 
 def run_reference(args, ws, rank):
-    """CPU arm: the oracle port of the reference (the reference's own code
-    does not build on the benchmark host), every host thread.  One full
-    sparsifier run sets up the matrix; each step then times a bounded sample
-    (sampler over a quarter of the edges, dense stages on a row sample)."""
+    """CPU arm: the oracle port of the reference pipeline (the reference's own
+    code does not build on the benchmark host: it needs MKL), every host
+    thread.  The K timed steps are K consecutive groups of the pipeline's
+    work units, so together they run one whole embedding exactly once; the
+    warm-up steps run sampler chunks in a throwaway table."""
     if rank != 0:
         return
+    from oracle import cpu_pipeline
     off, nbrs = load_graph(args.workload)
     w = WORKLOADS[args.workload]
-    sp = cpu_sparsify(off, nbrs, w)
-    secs = []
-    c = None
-    for i in range(args.warmup + args.steps):
-        c = cpu_pipeline_seconds(off, nbrs, w, sp=sp, edge_frac=0.25)
-        if i >= args.warmup:
-            secs.append(c["total"])
-    per = float(np.mean(secs))
-    val = c["samples"] / per
+    pipe = cpu_pipeline.Pipeline(off, nbrs, w, w["seed"])
+    cpu_pipeline.warmup(off, nbrs, w, w["seed"], pipe.cores, args.warmup)
+    cuts = cpu_pipeline.step_groups(len(pipe.units), args.steps)
+    secs = [pipe.run(cuts[i], cuts[i + 1]) for i in range(len(cuts) - 1)]
+    total = float(np.sum(secs))
+    val = pipe.samples / total
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": val, "unit": "samples/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded Chung-Lu; no dataset)",
-        "config": {"workload": w["label"], "stages_s": {k: c[k] for k in ("sampler", "csr", "randsvd",
-                                                                           "propagate", "dense_embed")}},
-        "cpu_baseline": {"value": val, "unit": "samples/s", "cores": c["cores"], "kind": "port",
-                         "sample": cpu_sample_text(c)},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / len(secs) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded Chung-Lu; no dataset)",
+        "config": {"workload": w["label"], "pipeline_seconds": total, "steps_timed": len(secs),
+                   "units": len(pipe.units), "stages_s": dict(pipe.stage_s), "samples": pipe.samples},
+        "cpu_baseline": {"value": val, "unit": "samples/s", "cores": pipe.cores, "kind": "port",
+                         "sample": cpu_sample_text(pipe, total, len(secs))},
         "e2e": {"value": val, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -251,35 +234,38 @@ def pipeline_step(ctx, g, w, precision, seed):
     return out, emb, {"sparsify": s1, "randsvd": s2, "propagate": s3, "nnz": nnz}
 
 
+def launch_count(ctx):
+    import ctypes
+
+    from lightne_gb300 import _lib
+    v = ctypes.c_int64()
+    _lib.check(_lib.load().lne_ctx_launch_count(ctx.handle, ctypes.byref(v)))
+    return v.value
+
+
 def time_form(ctx, g, w, precision, seed, steps, warmup, stream, flush):
+    """Mean ms per step of one form (CUDA events on the context's stream, L2
+    flushed between steps) and the library's kernel launches in the timed
+    steps."""
     import torch
     for _ in range(warmup):
         pipeline_step(ctx, g, w, precision, seed)
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     stats = []
-    out = None
+    out = emb = None
+    launches = 0
     for i in range(steps):
         flush.zero_()  # L2 flush between timed steps (outside the step events)
+        c0 = launch_count(ctx)
         ev[i][0].record(stream)
         out, emb, st = pipeline_step(ctx, g, w, precision, seed)
         ev[i][1].record(stream)
+        launches += launch_count(ctx) - c0
         stats.append(st)
     torch.cuda.synchronize()
     ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
-    return ms, stats, out, emb
-
-
-# lne_dense_embed: CholeskyQR3 (3 x (Gram + reduction, Cholesky/inverse,
-# update GEMM) + one trace), Gram, Jacobi (FP32 preconditioning, two
-# Newton-Schulz steps of two launches each, FP64 sweeps, finish), column
-# scaling, GEMM, row normalisation
-DENSE_EMBED_LAUNCHES = 3 * 4 + 1 + 2 + 7 + 1 + 1 + 1
-
-
-def launches_of(st):
-    return (st["sparsify"]["kernel_launches"] + st["randsvd"]["kernel_launches"] +
-            st["propagate"]["kernel_launches"] + DENSE_EMBED_LAUNCHES)
+    return ms, stats, out, emb, launches
 
 
 class _DevArray:
@@ -409,6 +395,14 @@ def profiled_traffic(name):
     return None
 
 
+# The forms timed on the GPU: FP16 (the headline: 16-bit SpMM operands that
+# meet the 1e-3 FP64 error gate), BF16 (the form as first specified: 16-bit
+# operands with 8 significant bits), FP32 (the plain form).
+FORMS = ("fp16", "bf16", "fp32")
+HEADLINE = "fp16"
+ERROR_GATE = 1e-3
+
+
 def run_ours(args, ws, rank, local):
     import torch
 
@@ -423,42 +417,48 @@ def run_ours(args, ws, rank, local):
     g = Graph.from_device(ctx, off.size - 1, d_off.data_ptr(), d_nbrs.data_ptr(), int(off[-1]))
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     seed = w["seed"] + rank
+    forms = (args.form or HEADLINE,) if args.quick else FORMS
     barrier(ws)
+    res = {}
     with ClockSampler(local) as clk:
-        ms_bf, st_bf, out_bf, emb_bf = time_form(ctx, g, w, "bf16", seed, args.steps, args.warmup, stream, flush)
-        if args.quick:
-            ms_fp, st_fp = ms_bf, st_bf
-        else:
-            ms_fp, st_fp, out_fp, emb_fp = time_form(ctx, g, w, "fp32", seed, args.steps, args.warmup, stream,
-                                                     flush)
+        for form in forms:
+            res[form] = time_form(ctx, g, w, form, seed, args.steps, args.warmup, stream, flush)
     barrier(ws)
     if args.quick:
         if rank == 0:
-            print(json.dumps({"quick": True, "ms_per_step_bf16": ms_bf, "stages": st_bf[-1]}))
+            f0 = forms[0]
+            print(json.dumps({"quick": True, "form": f0, "ms_per_step": res[f0][0], "stages": res[f0][1][-1],
+                              "gpu_launches_per_step": res[f0][4] / args.steps}))
         ctx.close()
         return
-    ms_bf = allmax(ws, ms_bf)
-    ms_fp = allmax(ws, ms_fp)
-    samples = st_bf[-1]["sparsify"]["samples_emitted"]
-    value = replica_value(samples, ws, ms_bf)
+    ms = {f: allmax(ws, res[f][0]) for f in forms}
+    st_h = res[HEADLINE][1]
+    samples = st_h[-1]["sparsify"]["samples_emitted"]
+    value = replica_value(samples, ws, ms[HEADLINE])
 
     # e2e through the C ABI with host (pinned) buffers: upload, pipeline, download
     off_p = torch.from_numpy(off).pin_memory().numpy()
     nbrs_p = torch.from_numpy(nbrs).pin_memory().numpy()
-    e2e_t = []
+    e2e_t, parts = [], []
     host_out = torch.empty(off.size - 1, w["dim"], dtype=torch.float32).pin_memory()
-    for i in range(3):
+    for i in range(4):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        gg = Graph.from_numpy(ctx, off_p, nbrs_p)
-        out, _, _ = pipeline_step(ctx, gg, w, "bf16", seed)
+        gg = Graph.from_numpy(ctx, off_p, nbrs_p)  # host -> device copies and the graph build (synchronises)
+        ta = time.perf_counter()
+        out, _, _ = pipeline_step(ctx, gg, w, HEADLINE, seed)
+        torch.cuda.synchronize()
+        tb = time.perf_counter()
         host_out.copy_(out)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         gg.free()
         if i > 0:
             e2e_t.append(t1 - t0)
+            parts.append((ta - t0, tb - ta, t1 - tb))
     e2e_s = allmax(ws, float(np.mean(e2e_t)))
+    e2e_parts = {k: float(np.mean([p_[j] for p_ in parts])) for j, k in enumerate(("upload_s", "pipeline_s",
+                                                                                     "download_s"))}
     h2d = off.nbytes + nbrs.nbytes
     d2h = host_out.numel() * 4
     ms_plain = None
@@ -467,75 +467,100 @@ def run_ours(args, ws, rank, local):
 
     if rank == 0:
         hbm, kind = peaks()
-        s_last = st_bf[-1]
         n = off.size - 1
-        nnz = s_last["nnz"]
+        nnz = st_h[-1]["nnz"]
         ld = (w["rank"] + 7) // 8 * 8
+        sx = {"fp32": 4, "bf16": 2, "fp16": 2}
 
-        def spmm_gbs(st, sx):
-            ms = float(np.mean([x["randsvd"]["ms_spmm2"] for x in st]))
-            comp = 8 * (n + 1) + 8 * nnz + n * ld * sx + n * ld * 4
-            gath = 8 * (n + 1) + 8 * nnz + nnz * ld * sx + n * ld * 4
-            return ms, comp / (ms / 1e3) / 1e9, gath / (ms / 1e3) / 1e9
+        def spmm_gbs(form):
+            ms_ = float(np.mean([x["randsvd"]["ms_spmm2"] for x in res[form][1]]))
+            comp = 8 * (n + 1) + 8 * nnz + n * ld * sx[form] + n * ld * 4
+            gath = 8 * (n + 1) + 8 * nnz + nnz * ld * sx[form] + n * ld * 4
+            return {"ms": ms_, "GB/s_compulsory": comp / (ms_ / 1e3) / 1e9, "GB/s_gather": gath / (ms_ / 1e3) / 1e9,
+                    "bytes_compulsory": comp}
 
-        # B = A Q reads the FP32 Q in both forms (s_x = 4)
-        ms_spmm_bf, comp_bf, gath_bf = spmm_gbs(st_bf, 4)
-        ms_spmm_fp, comp_fp, gath_fp = spmm_gbs(st_fp, 4)
-        ms_sample = float(np.mean([x["sparsify"]["ms_sample"] for x in st_bf]))
+        stage = lambda form, a, b: float(np.mean([x[a][b] for x in res[form][1]]))  # noqa: E731
+        ms_sample = stage(HEADLINE, "sparsify", "ms_sample")
         sampler_gbs = samples * 70.0 / (ms_sample / 1e3) / 1e9
-        stage = lambda st, a, b: float(np.mean([x[a][b] for x in st]))  # noqa: E731
-        # The dominant kernel (largest share of the step in the ncu launch
-        # list): the randomized SVD's SpMM B = A Q (k_spmm<float>, one launch
-        # per step), timed by the library's CUDA events on the launching
-        # stream.  Its DRAM traffic per launch comes from the committed ncu
-        # capture of the same kernel at this workload.
-        comp_bytes = 8 * (n + 1) + 8 * nnz + 2 * n * ld * 4
-        traffic = profiled_traffic("spmm_fp32_c2.md") if args.workload == "c2" else None
-        roof = {"kernel": "k_spmm<float> (B = A Q, FP32 Q, n x %d: one lne_spmm call, two column-slab launches "
-                          "+ chunk sums)" % ld, "bound": "hbm", "achieved": comp_bf,
-                "bytes_model": "compulsory 8(n+1) + 8 nnz + n ld 4 (Q) + n ld 4 (B) = %d B per launch" % comp_bytes,
-                "ms_per_launch": ms_spmm_bf, "achieved_gather_model": gath_bf,
-                "peak": hbm, "unit": "GB/s", "frac": comp_bf / hbm, "peak_kind": kind, "traffic": traffic,
-                "traffic_GB/s": None if traffic is None else traffic / (ms_spmm_bf / 1e3) / 1e9}
+        # The roofline kernel: the randomized SVD's SpMM B = A Q (one lne_spmm
+        # call per step: the main column slab, the tail slab from its dense
+        # copy, the long-row chunk sums), timed by the library's CUDA events on
+        # the launching stream.  Its DRAM traffic per call comes from the
+        # committed ncu capture of the same call at this workload.
+        sp_h = spmm_gbs(HEADLINE)
+        traffic = profiled_traffic("spmm_fp16_c2.md") if args.workload == "c2" else None
+        roof = {"kernel": "k_spmm<__half> (B = A Q, FP16 copy of 2^12 Q, n x %d: the main column slab, the "
+                          "tail slab and the long-row chunk sums of one lne_spmm call)" % ld,
+                "bound": "hbm", "achieved": sp_h["GB/s_compulsory"],
+                "bytes_model": "compulsory 8(n+1) + 8 nnz + n ld 2 (Q) + n ld 4 (B) = %d B per call"
+                               % sp_h["bytes_compulsory"],
+                "ms_per_launch": sp_h["ms"], "achieved_gather_model": sp_h["GB/s_gather"],
+                "peak": hbm, "unit": "GB/s", "frac": sp_h["GB/s_compulsory"] / hbm, "peak_kind": kind,
+                "traffic": traffic,
+                "traffic_GB/s": None if traffic is None else traffic / (sp_h["ms"] / 1e3) / 1e9}
+        forms_cfg = {}
+        for form in forms:
+            forms_cfg[form] = {
+                "embed_secs": ms[form] / 1e3, "samples_per_s": replica_value(samples, ws, ms[form]),
+                "stages_ms": {"sample": stage(form, "sparsify", "ms_sample"),
+                              "trunclog": stage(form, "sparsify", "ms_trunclog"),
+                              "csr": stage(form, "sparsify", "ms_csr"),
+                              "randsvd": stage(form, "randsvd", "ms_total"),
+                              "propagate": stage(form, "propagate", "ms_total")},
+                "spmm_B_AQ": spmm_gbs(form),
+            }
         line = {
             "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_bf, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16 SpMM operands, fp32 accumulate (int64 sparsifier)",
+            "warmup": args.warmup, "ms_per_step": ms[HEADLINE], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp16 SpMM operands, fp32 accumulate (int64 sparsifier)",
             "data": "synthetic (seeded Chung-Lu; no dataset)",
             "config": {
-                "workload": w["label"], "samples_per_step": samples, "nnz": nnz,
+                "workload": w["label"], "samples_per_step": samples, "nnz": nnz, "form": HEADLINE,
                 "l2": "512 MiB flush between timed steps",
-                "embed_secs_bf16": ms_bf / 1e3, "embed_secs_fp32": ms_fp / 1e3,
-                "fp32_form_value": replica_value(samples, ws, ms_fp), "bf16_over_fp32_speedup": ms_fp / ms_bf,
-                "stages_ms_bf16": {
-                    "sample": ms_sample, "trunclog": stage(st_bf, "sparsify", "ms_trunclog"),
-                    "csr": stage(st_bf, "sparsify", "ms_csr"), "randsvd": stage(st_bf, "randsvd", "ms_total"),
-                    "propagate": stage(st_bf, "propagate", "ms_total")},
-                "stages_ms_fp32": {
-                    "randsvd": stage(st_fp, "randsvd", "ms_total"), "propagate": stage(st_fp, "propagate",
-                                                                                       "ms_total")},
-                "spmm_svd_bf16": {"ms": ms_spmm_bf, "GB/s_compulsory": comp_bf, "GB/s_gather": gath_bf},
-                "spmm_svd_fp32": {"ms": ms_spmm_fp, "GB/s_compulsory": comp_fp, "GB/s_gather": gath_fp},
+                "forms": forms_cfg,
+                "fp16_over_fp32_speedup": ms["fp32"] / ms["fp16"],
+                "bf16_over_fp32_speedup": ms["fp32"] / ms["bf16"],
                 "sampler_GB/s": sampler_gbs,
                 "plain_fp32_gpu": None if ms_plain is None else {
-                    "embed_secs": ms_plain / 1e3, "bf16_form_speedup": ms_plain / ms_bf,
+                    "embed_secs": ms_plain / 1e3, "fp16_form_speedup": ms_plain / ms[HEADLINE],
                     "form": "same sparsifier; dense stages as unfused cuSPARSE/cuSOLVER/cuBLAS calls via torch, "
                             "FP32"},
             },
             "e2e": {"value": samples * ws / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s},
-            "gpu_launches": int(launches_of(s_last)) * args.steps,
+                    "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s, "breakdown": e2e_parts},
+            "gpu_launches": int(res[HEADLINE][4]),
             "roofline": roof,
             "clocks": clk.summary(),
         }
-        if args.accuracy:
-            line["accuracy"] = accuracy(ctx, g, w, seed, off, nbrs)
+        csr_dev = None
+        if not args.no_accuracy or not args.no_cpu_baseline:
+            csr_dev = device_csr(ctx, g, w, seed)
+        if not args.no_accuracy:
+            line["accuracy"] = accuracy(ctx, g, w, off, nbrs, csr_dev, forms)
         if not args.no_cpu_baseline:
-            c = cpu_pipeline_seconds(off, nbrs, w)
-            line["cpu_baseline"] = {"value": c["samples"] / c["total"], "unit": "samples/s", "cores": c["cores"],
-                                    "kind": "port", "sample": cpu_sample_text(c), "seconds": c["total"]}
+            pipe, secs = cpu_pipeline_run(off, nbrs, w, seed)
+            line["cpu_baseline"] = {"value": pipe.samples / secs, "unit": "samples/s", "cores": pipe.cores,
+                                    "kind": "port", "sample": cpu_sample_text(pipe, secs), "seconds": secs}
+            rp, col, val = csr_dev
+            prp, pcol, pval = pipe.csr
+            line["parity"] = {
+                "csr_bit_exact": bool(np.array_equal(rp, prp) and np.array_equal(col, pcol) and
+                                      np.array_equal(val.view(np.uint32), pval.view(np.uint32))),
+                "nnz": int(rp[-1]), "nnz_port": int(prp[-1]),
+                "against": "the C port of the reference sparsifier (oracle/sparsify_port.c, pinned to the "
+                           "reference's own generate_trunc_log_matrix_v2 by tests/golden), same seed"}
         print(json.dumps(line))
     ctx.close()
+
+
+def device_csr(ctx, g, w, seed):
+    """The device sparsifier's CSR of this workload, downloaded."""
+    from lightne_gb300.api import generate_trunc_log_matrix_v2
+    csr, _ = generate_trunc_log_matrix_v2(ctx, g, seed, walk_len=w["walk_len"], table_size=w["tablesz"],
+                                          sample_ratio=float(np.float32(w["sample_ratio"])))
+    out = csr.download()
+    csr.free()
+    return out
 
 
 def run_micro(args, local):
@@ -604,7 +629,15 @@ def run_micro(args, local):
                                               sample_ratio=float(np.float32(w["sample_ratio"])))
         g.free()
         Y = torch.empty((n, ld), dtype=torch.float32, device="cuda")
-        if args.micro == "spmm8":
+        if args.micro == "spmm16":
+            # B = A Q of the FP16 form: an FP16 copy of 2^12 Q
+            Xh = (X * 4096.0).to(torch.float16)
+            del X
+            call = lambda: lib.lne_spmm(ctx.handle, csr.handle, _lib.LNE_PREC_FP16,  # noqa: E731
+                                        vp(Xh.data_ptr()), ld, ld, 1.0 / 4096.0, 0.0, vp(Y.data_ptr()), ld)
+            model = 8 * (n + 1) + 8 * csr.nnz + n * ld * 2 + n * ld * 4
+            bytes_text = "8(n+1) + 8 nnz + n ld 2 + n ld 4 (CSR, FP16 Q once, B written)"
+        elif args.micro == "spmm8":
             # the sketch product Y = A Omega of the BF16 form: Omega's values
             # are e4m3-representable, so its FP8 copy is exact
             ldq = (r + 15) // 16 * 16
@@ -621,24 +654,26 @@ def run_micro(args, local):
                                         vp(Y.data_ptr()), ld)
             model = 8 * (n + 1) + 8 * csr.nnz + 2 * n * ld * 4
             bytes_text = "8(n+1) + 8 nnz + 2 n ld 4 (CSR, Q once, B written)"
-    for _ in range(args.warmup):
-        _lib.check(call())
-    torch.cuda.synchronize()
-    times = []
-    for _ in range(args.steps):
-        flush.zero_()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        _lib.check(call())
-        b.record(stream)
+    for panel_mb in [float(x) for x in str(args.panel_mb).split(",")]:
+        _lib.check(lib.lne_ctx_set_spmm_panel_bytes(ctx.handle, int(panel_mb * (1 << 20))))
+        for _ in range(args.warmup):
+            _lib.check(call())
         torch.cuda.synchronize()
-        times.append(a.elapsed_time(b))
-    ms = float(np.mean(times))
-    hbm, kind = peaks()
-    print(json.dumps({"micro": args.micro, "workload": w["label"], "n": n, "rank": r, "ld": ld,
-                      "nnz": csr.nnz if csr else None, "ms_per_launch": ms, "bytes_model": bytes_text,
-                      "bytes": model, "GB/s": model / (ms / 1e3) / 1e9, "peak_GB/s": hbm, "peak_kind": kind,
-                      "frac": model / (ms / 1e3) / 1e9 / hbm}))
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            _lib.check(call())
+            b.record(stream)
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+        ms = float(np.mean(times))
+        hbm, kind = peaks()
+        print(json.dumps({"micro": args.micro, "panel_mb": panel_mb, "workload": w["label"], "n": n, "rank": r,
+                          "ld": ld, "nnz": csr.nnz if csr else None, "ms_per_launch": ms, "bytes_model": bytes_text,
+                          "bytes": model, "GB/s": model / (ms / 1e3) / 1e9, "peak_GB/s": hbm, "peak_kind": kind,
+                          "frac": model / (ms / 1e3) / 1e9 / hbm}))
     if csr:
         csr.free()
     if args.micro == "prop":
@@ -724,7 +759,7 @@ def run_scale(args, local):
     out["csr_row_ptr_ok"] = sums[0][1]
     out["deterministic"] = sums[0][0] == sums[1][0]
     embs = {}
-    for prec in ("fp32", "bf16"):
+    for prec in FORMS:
         torch.cuda.synchronize()
         t = time.time()
         emb, S, s2 = randsvd(ctx, csr, w["rank"], w["dim"], precision=prec, seed=SVD_SEED)
@@ -738,12 +773,14 @@ def run_scale(args, local):
         del y
     csr.free()
     e32, p32 = (x.double().cpu().numpy() for x in embs["fp32"])
-    e16, p16 = (x.double().cpu().numpy() for x in embs["bf16"])
-    out["bf16_vs_fp32_svd_procrustes"] = lo.procrustes_rel_error(e16, e32)
-    out["bf16_vs_fp32_final_procrustes"] = lo.procrustes_rel_error(p16, p32)
-    del e32, p32, e16, p16
+    for prec in ("fp16", "bf16"):
+        e16, p16 = (x.double().cpu().numpy() for x in embs[prec])
+        out[prec + "_vs_fp32_svd_procrustes"] = lo.procrustes_rel_error(e16, e32)
+        out[prec + "_vs_fp32_final_procrustes"] = lo.procrustes_rel_error(p16, p32)
+        del e16, p16
+    del e32, p32
     if labels is not None:
-        emb = embs["bf16"][0]
+        emb = embs[HEADLINE][0]
         del embs
         rng = np.random.default_rng(w["seed"])
         perm = rng.permutation(n)
@@ -755,7 +792,7 @@ def run_scale(args, local):
         # adjoint); the 20 Adam steps then move (mu, s) and the classifier
         # together, the filter's gradients coming from the adjoint
         with torch.no_grad():
-            y0 = chebyshev_expansion(ctx, g, emb, w["dim"], order=w["order"], mu=0.2, s=0.5, precision="bf16")[0]
+            y0 = chebyshev_expansion(ctx, g, emb, w["dim"], order=w["order"], mu=0.2, s=0.5, precision=HEADLINE)[0]
             z0 = (y0 / y0.norm(dim=1, keepdim=True).clamp_min(1e-12))[tr]
         del y0
         W = torch.zeros(w["dim"], w["blocks"], device="cuda", requires_grad=True)
@@ -773,7 +810,7 @@ def run_scale(args, local):
         torch.cuda.synchronize()
         t = time.time()
         for step in range(w["adam_steps"] + 1):
-            y = ChebyshevPropagation(emb, mu, sp_, ctx, g, w["order"], "bf16")
+            y = ChebyshevPropagation(emb, mu, sp_, ctx, g, w["order"], HEADLINE)
             z = y / y.norm(dim=1, keepdim=True).clamp_min(1e-12)
             loss = torch.nn.functional.cross_entropy(z[tr] @ W + b, yl[tr])
             if step in (0, w["adam_steps"] // 2, w["adam_steps"]):
@@ -793,42 +830,56 @@ def run_scale(args, local):
     ctx.close()
 
 
-def accuracy(ctx, g, w, seed, off, nbrs):
-    """Both forms against the FP64 oracle on this workload (minutes of host
-    time): randomized SVD singular values, subspace angle and embedding
-    error after Procrustes, propagation output error, final embedding."""
+def accuracy(ctx, g, w, off, nbrs, csr_host, forms):
+    """Every form against the FP64 oracle on this workload (oracle/linalg_oracle.py,
+    same sketches): randomized SVD singular values, subspace angle and
+    embedding error after Procrustes; the propagation stage alone (each form
+    propagates the oracle's embedding); and the final embedding of the whole
+    chain (randomized SVD, propagation, dense SVD: the form's own chain
+    against the FP64 chain), after Procrustes."""
     import scipy.sparse as sp
-    import torch
 
-    from lightne_gb300.api import chebyshev_expansion, gaussian, generate_trunc_log_matrix_v2, randsvd
+    from lightne_gb300.api import CSR, chebyshev_expansion, gaussian, get_embedding_dense, randsvd
     from oracle import linalg_oracle as lo
-    ratio = float(np.float32(w["sample_ratio"]))
-    csr, _ = generate_trunc_log_matrix_v2(ctx, g, seed, walk_len=w["walk_len"], table_size=w["tablesz"],
-                                          sample_ratio=ratio)
-    rp, col, val = csr.download()
+    rp, col, val = csr_host
     n = off.size - 1
     A = sp.csr_matrix((val.astype(np.float64), col, rp), shape=(n, n))
-    res = {}
-    # both forms share one (BF16-representable) sketch, so one FP64 run serves both
+    res = {"gate": ERROR_GATE}
+    # every form shares the sketches, so one FP64 run serves all of them
     P = gaussian(ctx, SVD_SEED, 1, w["rank"], w["rank"]).double().cpu().numpy()
     om = gaussian(ctx, SVD_SEED, 0, n, w["rank"]).double().cpu().numpy()
     t0 = time.perf_counter()
     ref, Sref = lo.randsvd(A, om, P, w["dim"])
-    yref, _ = lo.propagate(off, nbrs, ref.astype(np.float32), order=w["order"])
+    del om
+    ref32 = ref.astype(np.float32)
+    yiso, _ = lo.propagate(off, nbrs, ref32, order=w["order"])
+    ychain, _ = lo.propagate(off, nbrs, ref, order=w["order"])
+    fin_ref, _ = lo.dense_embed(ychain)
+    del ychain
     res["oracle_seconds"] = time.perf_counter() - t0
-    for form in ("fp32", "bf16"):
+    import torch
+    d_rp, d_col, d_val = (torch.from_numpy(a).cuda() for a in (rp, col, val))
+    csr = CSR.wrap_device(ctx, n, int(rp[-1]), d_rp.data_ptr(), d_col.data_ptr(), d_val.data_ptr())
+    for form in forms:
         emb, S, _ = randsvd(ctx, csr, w["rank"], w["dim"], precision=form, seed=SVD_SEED)
         e = emb.double().cpu().numpy()
-        # propagate the oracle's embedding so that the stage error is isolated
-        y, _ = chebyshev_expansion(ctx, g, ref.astype(np.float32), w["dim"], order=w["order"], precision=form)
+        y, _ = chebyshev_expansion(ctx, g, ref32, w["dim"], order=w["order"], precision=form)
         yy = y.double().cpu().numpy()
+        del y
+        yc, _ = chebyshev_expansion(ctx, g, emb, w["dim"], order=w["order"], precision=form)
+        fin, _ = get_embedding_dense(ctx, yc, w["dim"])
+        del yc
+        final = lo.procrustes_rel_error(fin.double().cpu().numpy(), fin_ref)
         res[form] = {
             "svd_singular_values_max_rel": lo.rel_sv_error(S[:w["dim"]], Sref[:w["dim"]]),
             "svd_subspace_max_angle_rad": lo.max_principal_angle(e, ref),
             "svd_embedding_rel_frobenius_procrustes": lo.procrustes_rel_error(e, ref),
-            "propagation_rel_frobenius": float(np.linalg.norm(yy - yref) / np.linalg.norm(yref)),
+            "propagation_rel_frobenius": float(np.linalg.norm(yy - yiso) / np.linalg.norm(yiso)),
+            "final_embedding_rel_frobenius_procrustes": final,
+            "meets_gate": bool(final <= ERROR_GATE),
         }
     csr.free()
+    del d_rp, d_col, d_val
     return res
 
 
@@ -840,11 +891,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + sorted(SCALE_RUNS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--accuracy", action="store_true")
-    ap.add_argument("--quick", action="store_true", help="BF16 form only, no e2e / CPU legs (for profiling)")
-    ap.add_argument("--micro", choices=["gram", "gemm", "spmm", "spmm8", "prop"],
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 oracle errors of every form")
+    ap.add_argument("--quick", action="store_true", help="headline form only, no e2e / CPU legs (for profiling)")
+    ap.add_argument("--form", choices=list(FORMS), help="--quick: the form to time (default: the headline form)")
+    ap.add_argument("--micro", choices=["gram", "gemm", "spmm", "spmm16", "spmm8", "prop"],
                     help="time one C-ABI call alone (for profiling)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 GPU form (library calls) leg")
+    ap.add_argument("--panel-mb", default="0",
+                    help="--micro: comma-separated SpMM column-panel budgets in MiB, each timed in turn (0: no "
+                         "panels; negative: two panels, the lowest ids up to the budget, then the rest)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

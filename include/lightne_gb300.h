@@ -46,10 +46,14 @@ extern "C" {
 #define LNE_ERR_UNSUPPORTED 5  /* size beyond what this build handles */
 #define LNE_ERR_NUMERIC 6      /* factorisation failed (e.g. non-SPD Gram) */
 
-/* Dense operand precision of SpMM / propagation. */
+/* Dense operand precision of SpMM / propagation.  The 16-bit forms store
+ * the dense operand every SpMM gathers in 16 bits and accumulate in FP32;
+ * FP16 keeps 11 significant bits (BF16: 8) in the same bytes, on values
+ * scaled by a power of two into its range. */
 #define LNE_PREC_FP32 0
 #define LNE_PREC_BF16 1
 #define LNE_PREC_FP8 2 /* e4m3; SpMM dense operand only (lne_spmm x_prec) */
+#define LNE_PREC_FP16 3
 
 typedef struct lne_ctx lne_ctx;
 typedef struct lne_graph lne_graph;
@@ -64,8 +68,12 @@ const char* lne_version(void);
  * (NULL: the default stream). */
 int lne_ctx_create(lne_ctx** out, int device, void* stream);
 int lne_ctx_destroy(lne_ctx* ctx);
-/* L2 tuning: the bytes of L2 one column panel of an SpMM
- * dense operand may occupy (default 64 MiB; 0 disables column panels). */
+/* L2 tuning of the SpMM over a CSR (no reference counterpart): the dense
+ * operand's rows are cut into column panels of A whose slice of the
+ * operand fits in L2, one gather pass per panel.  bytes > 0: panels of at
+ * most that many bytes; bytes < 0: two panels, the lowest ids up to |bytes|
+ * then the rest (on graphs whose hubs have the lowest ids, most gathers hit
+ * the first); 0 (the default): no panels. */
 int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes);
 /* Aggregation of the sparsifier's pair samples (no reference counterpart:
  * the reference always inserts into par_table, LightNE/par_table.h:86-109).
@@ -84,6 +92,11 @@ int lne_ctx_set_sparsify_slices(lne_ctx* ctx, int32_t slots, int32_t slice_bits)
 int lne_ctx_set_sparsify_batch(lne_ctx* ctx, int64_t keys);
 /* Wait for all work queued on the context's stream. */
 int lne_ctx_synchronize(lne_ctx* ctx);
+/* Kernels the pipeline entry points (lne_sparsify, lne_randsvd,
+ * lne_propagate, lne_propagate_adjoint, lne_dense_embed, lne_spmm) have
+ * launched on this context so far, a diagnostic with no reference
+ * counterpart. */
+int lne_ctx_launch_count(const lne_ctx* ctx, int64_t* out);
 
 /*
  * Device memory helpers for callers that do not link the CUDA runtime
@@ -151,8 +164,8 @@ int lne_trunc_log_values(lne_ctx* ctx, const double* x, int64_t n, double* out);
 /*
  * SpMM: Y = alpha * A * X + beta * Y (mkl_sparse_s_mm, row-major,
  * non-transposed, as LightNE/mklredsvd/mklredsvd.cc:235-245).  X is n x d
- * with leading dimension ldx (device, FP32, BF16 or FP8 e4m3 per x_prec;
- * rows on 16-byte boundaries: ldx a multiple of 8, of 16 for FP8), Y is
+ * with leading dimension ldx (device, FP32, BF16, FP16 or FP8 e4m3 per
+ * x_prec; rows on 16-byte boundaries: ldx a multiple of 8, of 16 for FP8), Y is
  * n x d FP32 with ldy.
  * beta == 0 does not read Y.  Sums are formed in a fixed order: the result
  * is bitwise reproducible.  The first call on a matrix builds its work list.
@@ -166,9 +179,11 @@ typedef struct lne_randsvd_params {
   int64_t rank;                 /* -rank: sketch width r (oversampled) */
   int64_t dim;                  /* -dim: embedding dimension d <= r */
   int32_t normalize;            /* -normalize: L2-normalise embedding rows */
-  int32_t precision;            /* LNE_PREC_BF16: the sketch product A * Omega reads a BF16
-                                   Omega (exact: the sketch is BF16-representable); the product
-                                   A * Q reads FP32 Q in both forms */
+  int32_t precision;            /* LNE_PREC_FP32: every operand FP32.  LNE_PREC_BF16 and
+                                   LNE_PREC_FP16: the sketch product A * Omega reads an FP8
+                                   (e4m3) copy of Omega (exact: the sketch's values are
+                                   e4m3-representable), and A * Q reads a BF16 copy of Q, or an
+                                   FP16 copy of 2^12 * Q (|Q| <= 1); FP32 accumulation */
   uint64_t seed;                /* Gaussian sketch seed (the reference's VSL seed is 777) */
   int32_t random_project_only;  /* -random_project_only: return (A * Omega)[:, :dim] */
   int32_t sparse_project;       /* -sparse_project: Omega is the very sparse random projection
@@ -235,7 +250,11 @@ int lne_sparse_projection(lne_ctx* ctx, uint64_t seed, int64_t n, int64_t rank, 
 typedef struct lne_propagate_params {
   int64_t dim;        /* columns of the embedding (rank == dim in LightNE.cc:114) */
   int32_t order;      /* -order: number of Chebyshev terms K */
-  int32_t precision;  /* LNE_PREC_FP32 or LNE_PREC_BF16 (SpMM dense operand) */
+  int32_t precision;  /* LNE_PREC_FP32, LNE_PREC_BF16 or LNE_PREC_FP16: the type of the
+                         vectors the SpMMs gather (FP32 accumulation and FP32 state in
+                         every form; the FP16 form scales its input by a power of two so
+                         that its largest |value| lies in [64, 128), and unscales the
+                         outputs: an exact scaling) */
   double mu;          /* 0.2 in LightNE.cc:114 (narrowed to float, as the reference) */
   double s;           /* 0.5 in LightNE.cc:114 (Bessel argument, narrowed to float) */
 } lne_propagate_params;
@@ -317,11 +336,15 @@ int lne_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int64_t k, const f
  * process whose device memory belongs to another allocator or fixed arena,
  * or one under a hard memory cap).  The same product as lne_gram to FP32
  * accuracy (the row blocks may differ); its scratch is a 16 MiB file-scope
- * device array that every GPU loading the library holds
- * until exit, so ceil(n / 2048) * c1 * c2 must be at most 4,194,304 and
- * c2 at most 256 (else LNE_ERR_UNSUPPORTED).  The first call on a device
- * looks up the array's device address (make it before any stream capture).
- * Calls share the array: calls that overlap on the GPU race.
+ * device array that every GPU loading the library holds until exit, so
+ * ceil(max(n, 1) / 2048) * c1 * c2 must be at most 4,194,304 (else
+ * LNE_ERR_UNSUPPORTED).  Up to 256 columns it runs on the tensor cores,
+ * wider operands on the CUDA cores.  n = 0 writes zeros to G.  The first
+ * call on a device looks up the array's device address, which (with CUDA's
+ * lazy module loading) loads the array and commits its 16 MiB: make that
+ * call, for example with n = 0, before a memory cap applies and before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU
+ * race.  The caller's current device is restored on return.
  */
 int lne_gram_noalloc(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, const float* B, int64_t ldb, int64_t c2,
                      int64_t n, double* G);

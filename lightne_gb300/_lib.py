@@ -22,6 +22,7 @@ LNE_ERR_NUMERIC = 6
 LNE_PREC_FP32 = 0
 LNE_PREC_BF16 = 1
 LNE_PREC_FP8 = 2
+LNE_PREC_FP16 = 3
 
 _STATUS_NAMES = {
     LNE_ERR_INVALID: "LNE_ERR_INVALID",
@@ -142,6 +143,7 @@ SIGNATURES = {
     "lne_ctx_create": (ctypes.c_int, [PVP, ctypes.c_int, VP]),
     "lne_ctx_destroy": (ctypes.c_int, [VP]),
     "lne_ctx_synchronize": (ctypes.c_int, [VP]),
+    "lne_ctx_launch_count": (ctypes.c_int, [VP, ctypes.POINTER(I64)]),
     "lne_ctx_set_spmm_panel_bytes": (ctypes.c_int, [VP, I64]),
     "lne_ctx_set_sparsify_slices": (ctypes.c_int, [VP, I32, I32]),
     "lne_ctx_set_sparsify_batch": (ctypes.c_int, [VP, I64]),

@@ -12,13 +12,13 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import (LNE_PREC_BF16, LNE_PREC_FP32, LneError, PropagateParams, PropagateStats, RandsvdParams,
+from ._lib import (LNE_PREC_BF16, LNE_PREC_FP16, LNE_PREC_FP32, LneError, PropagateParams, PropagateStats, RandsvdParams,
                    RandsvdStats, SparsifyParams, SparsifyStats, check)
 
 __all__ = ["Context", "Graph", "CSR", "generate_trunc_log_matrix_v2", "randsvd",
            "chebyshev_expansion", "get_embedding_dense", "gaussian", "chebyshev_coefficients", "propagate_adjoint", "ChebyshevPropagation", "LneError"]
 
-PRECISIONS = {"fp32": LNE_PREC_FP32, "bf16": LNE_PREC_BF16}
+PRECISIONS = {"fp32": LNE_PREC_FP32, "bf16": LNE_PREC_BF16, "fp16": LNE_PREC_FP16}
 
 
 def _ptr(a: np.ndarray) -> ctypes.c_void_p:

@@ -13,8 +13,8 @@
 //
 // Added flags (defaults keep the reference behaviour): -seed <u64> (the
 // reference seeds the sampler with time(0), PathEmbed.h:499), -mu and
-// -theta (hard-coded 0.2 and 0.5 at LightNE.cc:114), -precision fp32|bf16
-// (SpMM dense operand; default fp32), -device <int>.
+// -theta (hard-coded 0.2 and 0.5 at LightNE.cc:114), -precision
+// fp32|bf16|fp16 (SpMM dense operand; default fp32), -device <int>.
 //
 // Exit status: 0 on success; the library's status code (with its message on
 // stderr) on failure.  Where the reference prints "looping forever" and
@@ -223,7 +223,11 @@ int main(int argc, char** argv) {
     fprintf(stderr, "LightNE: -step_coeff must have -walklen entries\n");
     return LNE_ERR_INVALID;
   }
-  const int prec = precision == "bf16" ? LNE_PREC_BF16 : LNE_PREC_FP32;
+  if (precision != "fp32" && precision != "bf16" && precision != "fp16") {
+    fprintf(stderr, "LightNE: -precision must be fp32, bf16 or fp16\n");
+    return LNE_ERR_INVALID;
+  }
+  const int prec = precision == "bf16" ? LNE_PREC_BF16 : (precision == "fp16" ? LNE_PREC_FP16 : LNE_PREC_FP32);
 
   std::vector<int64_t> off;
   std::vector<int32_t> nbrs;

@@ -250,7 +250,7 @@ int lne_ctx_destroy(lne_ctx* ctx) {
 }
 
 int lne_ctx_set_spmm_panel_bytes(lne_ctx* ctx, int64_t bytes) {
-  LNE_CHECK_ARG(ctx != nullptr && bytes >= 0, "lne_ctx_set_spmm_panel_bytes: bad argument");
+  LNE_CHECK_ARG(ctx != nullptr, "lne_ctx_set_spmm_panel_bytes: bad argument");
   ctx->spmm_panel_bytes = bytes;
   return LNE_OK;
 }
@@ -276,6 +276,12 @@ int lne_ctx_set_sparsify_batch(lne_ctx* ctx, int64_t keys) {
 int lne_ctx_synchronize(lne_ctx* ctx) {
   LNE_CHECK_ARG(ctx != nullptr, "lne_ctx_synchronize: ctx is NULL");
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return LNE_OK;
+}
+
+int lne_ctx_launch_count(const lne_ctx* ctx, int64_t* out) {
+  LNE_CHECK_ARG(ctx != nullptr && out != nullptr, "lne_ctx_launch_count: NULL argument");
+  *out = ctx->launch_count;
   return LNE_OK;
 }
 

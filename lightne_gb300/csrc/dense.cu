@@ -167,8 +167,7 @@ int gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int6
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_gemm_tall(const float* __restrict__ In, int64_t ldi, int k,
                                                    const float* __restrict__ W, int c2, int64_t n,
-                                                   float* __restrict__ Out, int64_t ldo,
-                                                   __nv_bfloat16* __restrict__ OutB) {
+                                                   float* __restrict__ Out, int64_t ldo, Copy16 OutB) {
   __shared__ __align__(16) float As[16][128 + 4];
   __shared__ __align__(16) float Ws[16][64];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -210,14 +209,14 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const float* __restrict__ In,
       if (c < ldo) {
         const float v = c < c2 ? acc[p][q] : 0.f;
         Out[row * ldo + c] = v;
-        if (OutB) OutB[row * ldo + c] = __float2bfloat16_rn(v);
+        copy16_put(OutB, row * ldo + c, v);
       }
     }
   }
 }
 
 int gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
-              int64_t ldo, __nv_bfloat16* OutB) {
+              int64_t ldo, Copy16 OutB) {
   if (n <= 0) return LNE_OK;
   if (tc_supported((int)std::max<int64_t>(c2, ldo))) return tc_gemm_tall(ctx, In, ldi, k, W, c2, n, Out, ldo, OutB);
   dim3 grid((unsigned)((n + 127) / 128), (unsigned)((ldo + 63) / 64));
@@ -1235,7 +1234,7 @@ extern "C" int lne_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int64_t
                 "lne_gemm_tall: bad argument");
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
   LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, ctx->stream));
-  int rc = gemm_tall(ctx, In, ldi, (int)k, W, (int)c2, n, Out, ldo, nullptr);
+  int rc = gemm_tall(ctx, In, ldi, (int)k, W, (int)c2, n, Out, ldo);
   if (rc) return rc;
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   int h = 0;

@@ -8,6 +8,7 @@
 #include <cuda_fp8.h>
 #include <stdint.h>
 
+#include "dense_common.cuh"
 #include "lne_internal.h"
 
 namespace lne {
@@ -30,9 +31,10 @@ int gram(lne_ctx* ctx, const float* A, int64_t lda, int c1, const float* B, int6
          double* G);
 
 // Out (n x c2, ldo) = In (n x k, ldi) * W (k x c2, FP32 row-major, ldw = c2).
-// Optional BF16 copy of Out (ldb = ldo).  Columns c2..ldo-1 of Out are zeroed.
+// Optional 16-bit copy of Out (same ld; BF16, or FP16 of scale * Out).
+// Columns c2..ldo-1 of Out are zeroed.
 int gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
-              int64_t ldo, __nv_bfloat16* OutB);
+              int64_t ldo, Copy16 OutB = Copy16());
 
 // Cholesky G + shift*I = L L^T (FP64, in place on a device r x r buffer) and
 // W = L^-T as FP32 (r x r row-major, upper triangular).  Returns
@@ -54,7 +56,7 @@ int jacobi_svd_launches(lne_ctx* ctx, int r);
 // gemm_tall for up to 256 columns; gram/gemm_tall use them when they apply.
 bool tc_supported(int c2);
 int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
-                 int64_t ldo, __nv_bfloat16* OutB);
+                 int64_t ldo, Copy16 OutB);
 // Streaming tensor-core Gram: applies when both operands are 16-byte aligned
 // with row strides that are multiples of 4 floats and the shape fits.  Uses
 // at most max_blocks CTAs; `partial` (NULL: allocated here) holds

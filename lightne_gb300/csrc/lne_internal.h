@@ -58,9 +58,9 @@ struct lne_ctx {
   int num_sms = 0;
   size_t smem_optin = 0;
   void* log_table = nullptr;    // device lne::LogTable (double-float log(c_j), 1/c_j)
-  // L2 bytes a column panel of the SpMM dense operand may take (0: no
-  // panels, the default: with full-width lane layouts the gathers run as
-  // fast from HBM as from L2-sized panels at 1.1M x 144)
+  // Column panels of the SpMM dense operand: > 0, panels of at most that
+  // many bytes of L2; < 0, two panels, the lowest ids up to |bytes| of L2
+  // first, then the rest; 0 (the default): no panels
   int64_t spmm_panel_bytes = 0;
   // Sliced aggregation of the sparsifier's samples (counts, one batch):
   // shared-memory table size per slice (0: always the pair table in HBM)
@@ -69,6 +69,9 @@ struct lne_ctx {
   int sparsify_slice_bits = -1;
   // samples per batch of the sparsifier's sample buffer (8 B each)
   int64_t sparsify_batch_keys = (int64_t)1 << 30;
+  // kernels launched by the entry points that ran on this context (each
+  // adds its own count when it returns successfully)
+  int64_t launch_count = 0;
 };
 
 struct lne_graph {
@@ -93,11 +96,14 @@ struct lne_csr {
   cudaStream_t stream = nullptr;
   lne::SpmmPlan plan;
   bool plan_ready = false;
-  // column panels for the cache-blocked SpMM (built on first use for a
-  // given panel width): seg[r * (npanels + 1) + p] = first entry of row r
-  // with column >= p * panel_width, relative to row_ptr[r]
-  int64_t panel_width = 0;
+  // column panels for the cache-blocked SpMM (built on first use for given
+  // panel bounds): seg[r * (npanels + 1) + p] = first entry of row r with
+  // column >= panel_bounds[p], relative to row_ptr[r]
+  std::vector<int64_t> panel_bounds;
   int npanels = 0;
+  // share of the entries whose column is below hub_cols (-1: not measured)
+  int64_t hub_cols = 0;
+  double hub_share = -1.0;
   int32_t* seg = nullptr;
   std::vector<lne::SpmmPlan> panel_plans;
 };
@@ -138,8 +144,12 @@ static constexpr int kPlanLaunches = 11;
 int build_plan_csr(lne_ctx* ctx, lne_csr* c);
 int build_plan_graph(lne_ctx* ctx, lne_graph* g);
 void free_plan(SpmmPlan& p);
-// Column panels of width pw for the cache-blocked SpMM (synchronises).
-int build_panels(lne_ctx* ctx, lne_csr* c, int64_t pw);
+// Column panels [bounds[p], bounds[p + 1]) for the cache-blocked SpMM
+// (bounds[0] = 0, bounds.back() = n; synchronises).
+int build_panels(lne_ctx* ctx, lne_csr* c, const std::vector<int64_t>& bounds);
 void free_panels(lne_csr* c);
+// The share of A's entries with a column below pw, cached on the matrix in
+// hub_share (synchronises once per matrix and pw).
+int hub_share(lne_ctx* ctx, lne_csr* c, int64_t pw);
 
 }  // namespace lne

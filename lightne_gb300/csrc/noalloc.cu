@@ -11,17 +11,23 @@
 // calls no cudaMalloc, cudaFree or allocating library routine.
 //
 // The array is a module-scope __device__ variable: every GPU that loads this
-// library holds its 16 MiB until the process exits.  In host code the
-// array's name is a host-side stand-in, not a device address, so its device
-// address is looked up with cudaGetSymbolAddress once per device, with that
-// device current, on the first call for that device (make that first call
-// before any stream capture).  All calls share the one array and it keeps
-// the last call's contents; every partial a call reads it has written first,
-// so nothing needs clearing.  Calls whose work overlaps on the GPU (other
-// streams, other host threads) race on the array and must be serialised by
-// the caller.
+// library holds its 16 MiB until the process exits.  With CUDA's lazy module
+// loading (the default since CUDA 12.2) the module that holds the array is
+// loaded, and its 16 MiB committed, only when the array's address is first
+// looked up: on the first call for a device.  A caller that will run under a
+// memory cap should therefore make one call per device before the cap
+// applies; a call with n = 0 does that set-up and only zeroes G.  In host
+// code the array's name is a host-side stand-in, not a device address, so
+// its device address is looked up with cudaGetSymbolAddress once per device,
+// with that device current, on that first call (make it before any stream
+// capture).  All calls share the one array and it keeps the last call's
+// contents; every partial a call reads it has written first, so nothing
+// needs clearing.  Calls whose work overlaps on the GPU (other streams,
+// other host threads) race on the array and must be serialised by the
+// caller.  The calling thread's current device is restored on return.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -70,24 +76,38 @@ using namespace lne;
 
 extern "C" int lne_gram_noalloc(lne_ctx* ctx, const float* A, int64_t lda, int64_t c1, const float* B, int64_t ldb,
                                 int64_t c2, int64_t n, double* G) {
-  LNE_CHECK_ARG(ctx && A && B && G && n >= 1 && c1 >= 1 && c2 >= 1 && lda >= c1 && ldb >= c2,
+  LNE_CHECK_ARG(ctx && A && B && G && n >= 0 && c1 >= 1 && c2 >= 1 && lda >= c1 && ldb >= c2,
                 "lne_gram_noalloc: bad argument");
-  if (c2 > 256) {
-    set_error("lne_gram_noalloc: at most 256 columns of B");
-    return LNE_ERR_UNSUPPORTED;
-  }
-  const int64_t nb = (n + 2047) / 2048;
-  if (c1 > kNoAllocScratchFloats || nb * c1 * c2 > kNoAllocScratchFloats) {
+  const int64_t nb = std::max<int64_t>(1, (n + 2047) / 2048);
+  if (c1 > kNoAllocScratchFloats || c2 > kNoAllocScratchFloats || nb * c1 * c2 > kNoAllocScratchFloats) {
     set_error("lne_gram_noalloc: ceil(n / 2048) * c1 * c2 exceeds the 4,194,304 partial sums of the "
               "fixed 16 MiB scratch; use lne_gram");
     return LNE_ERR_UNSUPPORTED;
   }
+  // the tensor-core Gram takes up to 256 columns; the CUDA-core Gram any
+  // width, with one grid row per 2048-row block
+  const bool tc = c1 <= 256 && c2 <= 256 && tc_gram_stream_supported(ctx, A, lda, (int)c1, B, ldb, (int)c2);
+  if (!tc && nb > 65535) {
+    set_error("lne_gram_noalloc: more than 65535 row blocks of 2048 on the CUDA-core path; use lne_gram");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) {
+    cudaGetLastError();
+    prev = -1;
+  }
+  struct RestoreDevice {
+    int dev;
+    ~RestoreDevice() {
+      if (dev >= 0) cudaSetDevice(dev);
+    }
+  } restore{prev};
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
   float* scratch = nullptr;
   int rc = noalloc_scratch(ctx->device, &scratch);
   if (rc) return rc;
   LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, ctx->stream));
-  if (tc_gram_stream_supported(ctx, A, lda, (int)c1, B, ldb, (int)c2))
+  if (tc)
     rc = tc_gram_stream(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G, scratch, nb);
   else
     rc = gram_simt_into(ctx, A, lda, (int)c1, B, ldb, (int)c2, n, G, scratch);

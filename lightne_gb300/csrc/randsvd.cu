@@ -8,10 +8,12 @@
 // instead of Householder geqrf+orgqr; R has a positive diagonal, so Q is the
 // unique thin-QR factor with that sign convention.  The core SVD is a
 // one-sided FP64 Jacobi.  The Gaussian sketches come from a counter-based
-// generator (MKL's SFMT19937 stream cannot be reproduced without MKL); its
-// values are BF16-representable, so in the BF16 form the product A * Omega
-// reads a BF16 sketch with no loss.
+// generator (MKL's SFMT19937 stream cannot be reproduced without MKL).  The
+// sketch's values are e4m3-representable, so the 16-bit forms gather it from
+// an exact FP8 copy; their product A * Q gathers a 16-bit copy of Q (BF16,
+// or FP16 of 2^12 Q) that the last CholeskyQR GEMM writes beside the FP32 Q.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -47,19 +49,21 @@ struct Buf {
   }
 };
 
-// Y = A * X with FP32 output, X FP32, BF16 or FP8; `add` accumulates the later
-// column panels of the cache-blocked SpMM.
+// Y = scale * (A * X) with FP32 output, X FP32, BF16, FP16 or FP8 (scale
+// undoes the power-of-two scaling of an FP16 copy; 1 otherwise); `add`
+// accumulates the later column panels of the cache-blocked SpMM.
 struct EpiStore {
   float* __restrict__ Y;
   int64_t ldy;
   int d;
   bool add;
+  float scale = 1.0f;
   template <int N>
   __device__ __forceinline__ void operator()(int64_t r, int e0, const float (&a)[N]) const {
     float* y = Y + r * ldy + e0;
 #pragma unroll
     for (int i = 0; i < N; ++i)
-      if (e0 + i < d) y[i] = add ? y[i] + a[i] : a[i];
+      if (e0 + i < d) y[i] = add ? fmaf(scale, a[i], y[i]) : scale * a[i];
   }
 };
 
@@ -82,9 +86,10 @@ __global__ void k_copy_cols(const float* __restrict__ X, int64_t ldx, int64_t n,
 
 }  // namespace
 
-// In-place CholeskyQR on X (n x ld FP32, r columns) using tmp as the ping-pong
-// partner; the result ends in X.  Xb (optional) receives a BF16 copy.
-static int cholqr3(lne_ctx* ctx, float* X, float* tmp, int64_t n, int64_t ld, int r, __nv_bfloat16* Xb,
+// CholeskyQR on X (n x ld FP32, r columns) with tmp as the ping-pong
+// partner; the two pointers are swapped so that the result ends in X.  Xb
+// (optional) receives a 16-bit copy of the result from the last GEMM.
+static int cholqr3(lne_ctx* ctx, float*& X, float*& tmp, int64_t n, int64_t ld, int r, Copy16 Xb,
                    int* launches) {
   Buf B(ctx);
   double* G = nullptr;
@@ -111,22 +116,34 @@ static int cholqr3(lne_ctx* ctx, float* X, float* tmp, int64_t n, int64_t ld, in
       if (rc != LNE_ERR_NUMERIC || attempt == 5) return rc;
     }
     const bool last = pass == 2;
-    if ((rc = gemm_tall(ctx, src, ld, r, W, r, n, dst, ld, last ? Xb : nullptr))) return rc;
+    if ((rc = gemm_tall(ctx, src, ld, r, W, r, n, dst, ld, last ? Xb : Copy16()))) return rc;
     *launches += 1;
     float* t = src;
     src = dst;
     dst = t;
   }
-  // three passes: the result is in tmp; move it to X
-  LNE_CUDA_TRY(cudaMemcpyAsync(X, src, sizeof(float) * n * ld, cudaMemcpyDeviceToDevice, ctx->stream));
+  // three passes: the result is in the buffer tmp came in
+  X = src;
+  tmp = dst;
   return LNE_OK;
 }
 
 template <typename XT>
-static int spmm_store(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ld, int d, float* Y, int* launches) {
-  EpiStore epi{Y, ld, d, false};
-  return spmm_csr_panels<XT>(ctx, A, X, ld, d, epi, launches);
+static int spmm_store(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ld, int d, float* Y, int* launches,
+                      float scale = 1.0f, int64_t panel_bytes = 0) {
+  EpiStore epi{Y, ld, d, false, scale};
+  return spmm_csr_panels<XT>(ctx, A, X, ld, d, epi, launches, panel_bytes);
 }
+
+// The product A * Q of the 16-bit forms gathers Q in two column panels when
+// Q's lowest-id rows up to this many bytes receive at least half of A's
+// entries (power-law graphs numbered hubs first): their gathers then stay
+// in L2 (1.1M x 144 FP16 at nnz 351M: 14.7 -> 13.3 ms alone).
+static constexpr int64_t kHubPanelBytes = (int64_t)64 << 20;
+
+// Scale of the FP16 copy of Q: |Q| <= 1 (orthonormal columns), so 2^12 Q
+// stays below 4097, and entries down to 2^-26 stay in FP16's normal range.
+static constexpr float kQHalfScale = 4096.0f;
 
 }  // namespace lne
 
@@ -144,7 +161,8 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
   LNE_CHECK_ARG(ctx && Acsr && p && d_emb, "lne_randsvd: NULL argument");
   LNE_CHECK_ARG(p->rank >= 1 && p->dim >= 1 && p->dim <= p->rank, "lne_randsvd: need 1 <= dim <= rank");
   LNE_CHECK_ARG(p->rank <= Acsr->n, "lne_randsvd: rank above n");
-  LNE_CHECK_ARG(p->precision == LNE_PREC_FP32 || p->precision == LNE_PREC_BF16, "lne_randsvd: bad precision");
+  LNE_CHECK_ARG(p->precision == LNE_PREC_FP32 || p->precision == LNE_PREC_BF16 || p->precision == LNE_PREC_FP16,
+                "lne_randsvd: bad precision");
   if (p->rank > 1024) {
     set_error("lne_randsvd: rank above 1024 is not supported by the one-block Jacobi core");
     return LNE_ERR_UNSUPPORTED;
@@ -155,9 +173,11 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
   const int64_t n = A->n;
   const int r = (int)p->rank, dim = (int)p->dim;
   const int64_t ld = pad_ld(r);
-  const bool bf16 = p->precision == LNE_PREC_BF16;
+  const bool f16 = p->precision == LNE_PREC_FP16;
+  const bool low = p->precision != LNE_PREC_FP32;  // a 16-bit form
   cudaStream_t st = ctx->stream;
   int launches = 0;
+  if (!A->plan_ready) launches += kPlanLaunches;
   int rc = build_plan_csr(ctx, A);
   if (rc) return rc;
 
@@ -170,11 +190,12 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
 
   Buf B(ctx);
   float *Y = nullptr, *T = nullptr, *Bm = nullptr, *P = nullptr, *Wf = nullptr;
-  __nv_fp8_e4m3* Xq = nullptr;  // the sketch's FP8 copy (BF16 form)
+  __nv_fp8_e4m3* Xq = nullptr;  // the sketch's FP8 copy (16-bit forms)
+  uint16_t* Q16 = nullptr;       // the 16-bit copy of Q (16-bit forms)
   const int64_t ldq = pad_ld_fp8(r);
   double *C = nullptr, *U = nullptr, *S = nullptr;
   if ((rc = B.get(&Y, (size_t)n * ld, "Y")) || (rc = B.get(&T, (size_t)n * ld, "QR scratch")) ||
-      (bf16 && (rc = B.get(&Xq, (size_t)n * ldq, "FP8 sketch"))))
+      (low && !p->sparse_project && (rc = B.get(&Xq, (size_t)n * ldq, "FP8 sketch"))))
     return rc;
 
   cudaEventRecord(ev[0], st);
@@ -186,7 +207,7 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
     if ((rc = sparse_projection_build(ctx, n, r, p->seed, p->sparse_project_s, &O, &launches))) return rc;
     if ((rc = sparse_projection_product(ctx, A, O, Y, ld, &launches))) return rc;
     launches -= 1;  // the Gaussian draw counted below does not happen
-  } else if (bf16) {
+  } else if (low) {
     // the sketch's values are e4m3-representable: its FP8 copy is exact
     if ((rc = gaussian_fill_fp8(ctx, p->seed, 0, n, r, Xq, ldq))) return rc;
     if ((rc = spmm_store<__nv_fp8_e4m3>(ctx, A, Xq, ldq, (int)ld, Y, &launches))) return rc;
@@ -206,30 +227,44 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
     if (h_S)
       for (int i = 0; i < r; ++i) h_S[i] = 1.0f;
     LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (p->normalize) launches += 1;
     if (stats) {
       memset(stats, 0, sizeof(*stats));
       cudaEventElapsedTime(&stats->ms_sketch, ev[0], ev[1]);
-      stats->kernel_launches = launches + (p->normalize ? 1 : 0);
+      stats->kernel_launches = launches;
     }
+    ctx->launch_count += launches;
     return LNE_OK;
   }
 
-  // Q = qr(Y)
-  if ((rc = cholqr3(ctx, Y, T, n, ld, r, nullptr, &launches))) return rc;
+  // Q = qr(Y), with its 16-bit copy in the 16-bit forms
+  Copy16 q16;
+  if (low) {
+    if ((rc = B.get(&Q16, (size_t)n * ld, "16-bit Q"))) return rc;
+    q16.p = Q16;
+    q16.kind = f16 ? 2 : 1;
+    q16.scale = f16 ? kQHalfScale : 1.0f;
+  }
+  if ((rc = cholqr3(ctx, Y, T, n, ld, r, q16, &launches))) return rc;
   cudaEventRecord(ev[2], st);
-  // B = A * Q.  Q is not BF16-representable (unlike the sketch), and a BF16
-  // copy of it costs about 1e-3 relative embedding error, so this product
-  // reads the FP32 Q in both forms.
+  // B = A * Q
   if ((rc = B.get(&Bm, (size_t)n * ld, "B"))) return rc;
-  rc = spmm_store<float>(ctx, A, Y, ld, (int)ld, Bm, &launches);
+  if (f16)
+    rc = spmm_store<__half>(ctx, A, (const __half*)Q16, ld, (int)ld, Bm, &launches, 1.0f / kQHalfScale,
+                            -kHubPanelBytes);
+  else if (low)
+    rc = spmm_store<__nv_bfloat16>(ctx, A, (const __nv_bfloat16*)Q16, ld, (int)ld, Bm, &launches, 1.0f,
+                                   -kHubPanelBytes);
+  else
+    rc = spmm_store<float>(ctx, A, Y, ld, (int)ld, Bm, &launches);
   if (rc) return rc;
   cudaEventRecord(ev[3], st);
   // Z = qr(B * P); Y holds Z from here on
   if ((rc = B.get(&P, (size_t)r * r, "P"))) return rc;
   if ((rc = gaussian_fill_f32(ctx, p->seed, 1, r, r, P, r))) return rc;
-  if ((rc = gemm_tall(ctx, Bm, ld, r, P, r, n, Y, ld, nullptr))) return rc;
+  if ((rc = gemm_tall(ctx, Bm, ld, r, P, r, n, Y, ld))) return rc;
   launches += 2;
-  if ((rc = cholqr3(ctx, Y, T, n, ld, r, nullptr, &launches))) return rc;
+  if ((rc = cholqr3(ctx, Y, T, n, ld, r, Copy16(), &launches))) return rc;
   cudaEventRecord(ev[4], st);
   // C = Z^T B, C = U_C S V^T
   if ((rc = B.get(&C, (size_t)r * r, "C")) || (rc = B.get(&U, (size_t)r * r, "U_C")) ||
@@ -242,7 +277,7 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
   // emb = Z * (U_C[:, :dim] * diag(sqrt(S[:dim])))
   if ((rc = B.get(&Wf, (size_t)r * dim, "U sqrt(S)"))) return rc;
   k_scale_cols<<<(r * dim + 255) / 256, 256, 0, st>>>(U, S, r, dim, Wf);
-  if ((rc = gemm_tall(ctx, Y, ld, r, Wf, dim, n, d_emb, dim, nullptr))) return rc;
+  if ((rc = gemm_tall(ctx, Y, ld, r, Wf, dim, n, d_emb, dim))) return rc;
   launches += 2;
   if (p->normalize) {
     if ((rc = normalize_rows(ctx, d_emb, n, dim, dim, 1e-5f))) return rc;
@@ -276,6 +311,7 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
     stats->kernel_launches = launches;
     stats->spmm_nnz = (double)A->nnz;
   }
+  ctx->launch_count += launches;
   return LNE_OK;
 }
 
@@ -324,14 +360,16 @@ extern "C" int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_
                                  cudaMemcpyDeviceToDevice, st));
   LNE_CUDA_TRY(cudaMemcpyAsync(Q, X, sizeof(float) * n * ld, cudaMemcpyDeviceToDevice, st));
   // X = Q R with Q from CholeskyQR; R = Q^T X; R = U_R S V^T; U = Q U_R
-  if ((rc = cholqr3(ctx, Q, T, n, ld, d, nullptr, &launches))) return rc;
+  if ((rc = cholqr3(ctx, Q, T, n, ld, d, Copy16(), &launches))) return rc;
   if ((rc = gram(ctx, Q, ld, d, X, ld, d, n, C))) return rc;
   int sweeps = 0;
   if ((rc = jacobi_svd(ctx, C, d, U, S, &sweeps))) return rc;
   k_scale_cols<<<(d * d + 255) / 256, 256, 0, st>>>(U, S, d, d, W);
-  if ((rc = gemm_tall(ctx, Q, ld, d, W, d, n, d_emb, d, nullptr))) return rc;
+  if ((rc = gemm_tall(ctx, Q, ld, d, W, d, n, d_emb, d))) return rc;
   // get_embedding_dense normalises unconditionally (SpectralPropagation.h:40)
   if ((rc = normalize_rows(ctx, d_emb, n, d, d, 1e-5f))) return rc;
+  // Gram + reduction, Jacobi, column scaling, GEMM, row normalisation
+  launches += 2 + jacobi_svd_launches(ctx, d) + 1 + 1 + 1;
   if (h_S) {
     std::vector<double> hs(d);
     LNE_CUDA_TRY(cudaMemcpyAsync(hs.data(), S, sizeof(double) * d, cudaMemcpyDeviceToHost, st));
@@ -346,5 +384,6 @@ extern "C" int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_
     set_error("lne_dense_embed: a tensor-core wait timed out");
     return LNE_ERR_CUDA;
   }
+  ctx->launch_count += launches;
   return LNE_OK;
 }

@@ -1189,6 +1189,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     stats->kernel_launches = launches;
     stats->sliced = sliced ? 1 : 0;
   }
+  ctx->launch_count += launches;
   lne_csr* c = new lne_csr();
   c->n = n;
   c->nnz = nnz;

@@ -1,6 +1,7 @@
 // SpMM front end: work-list planning, configuration dispatch and the
 // public lne_spmm entry point (mkl_sparse_s_mm, row-major, non-transposed).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -106,16 +107,16 @@ void free_plan(SpmmPlan& p) {
   p = SpmmPlan();
 }
 
-// seg[r * np1 + p] = (first entry of row r with column >= p * pw) - row_ptr[r]
+// seg[r * np1 + p] = (first entry of row r with column >= bounds[p]) - row_ptr[r]
 __global__ void k_panel_seg(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, int64_t n,
-                            int64_t pw, int np1, int32_t* __restrict__ seg) {
+                            const int64_t* __restrict__ bounds, int np1, int32_t* __restrict__ seg) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const int64_t a = row_ptr[r], b = row_ptr[r + 1];
   seg[r * np1] = 0;
   int64_t lo = a;
   for (int p = 1; p < np1; ++p) {
-    const int64_t bound = (int64_t)p * pw;
+    const int64_t bound = bounds[p];
     int64_t hi = b;
     while (lo < hi) {  // first index in [lo, b) with col >= bound
       const int64_t mid = (lo + hi) >> 1;
@@ -125,28 +126,73 @@ __global__ void k_panel_seg(const int64_t* __restrict__ row_ptr, const int32_t* 
   }
 }
 
+// Entries of each row with a column below pw (rows sorted by column): one
+// binary search per row, summed per block.
+__global__ void k_hub_count(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, int64_t n,
+                            int64_t pw, unsigned long long* __restrict__ total) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long c = 0;
+  if (r < n) {
+    int64_t lo = row_ptr[r], hi = row_ptr[r + 1];
+    const int64_t a = lo;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)col[mid] < pw) lo = mid + 1; else hi = mid;
+    }
+    c = (unsigned long long)(lo - a);
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(total, c);
+}
+
+int hub_share(lne_ctx* ctx, lne_csr* c, int64_t pw) {
+  if (c->hub_share >= 0.0 && c->hub_cols == pw) return LNE_OK;
+  unsigned long long* d = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, (void**)&d, sizeof(unsigned long long), "hub count"))) return rc;
+  LNE_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
+  k_hub_count<<<(unsigned)((c->n + 255) / 256), 256, 0, ctx->stream>>>(c->row_ptr, c->col, c->n, pw, d);
+  unsigned long long h = 0;
+  LNE_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, d);
+  LNE_CUDA_TRY(cudaGetLastError());
+  c->hub_cols = pw;
+  c->hub_share = c->nnz > 0 ? (double)h / (double)c->nnz : 0.0;
+  return LNE_OK;
+}
+
 void free_panels(lne_csr* c) {
   for (auto& p : c->panel_plans) free_plan(p);
   c->panel_plans.clear();
   if (c->seg) cudaFree(c->seg);
   c->seg = nullptr;
   c->npanels = 0;
-  c->panel_width = 0;
+  c->panel_bounds.clear();
 }
 
-int build_panels(lne_ctx* ctx, lne_csr* c, int64_t pw) {
-  if (c->panel_width == pw && c->seg) return LNE_OK;
+int build_panels(lne_ctx* ctx, lne_csr* c, const std::vector<int64_t>& bounds) {
+  if (c->panel_bounds == bounds && c->seg) return LNE_OK;
   free_panels(c);
   const int64_t n = c->n;
-  const int np = (int)((n + pw - 1) / pw);
+  const int np = (int)bounds.size() - 1;
   int32_t* seg = nullptr;
+  int64_t* d_bounds = nullptr;
   int rc;
   if ((rc = dalloc(ctx, (void**)&seg, sizeof(int32_t) * n * (np + 1), "spmm panel segments"))) return rc;
-  k_panel_seg<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(c->row_ptr, c->col, n, pw, np + 1, seg);
+  if ((rc = dalloc(ctx, (void**)&d_bounds, sizeof(int64_t) * (np + 1), "spmm panel bounds"))) {
+    dfree(ctx, seg);
+    return rc;
+  }
+  LNE_CUDA_TRY(cudaMemcpyAsync(d_bounds, bounds.data(), sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  k_panel_seg<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(c->row_ptr, c->col, n, d_bounds, np + 1, seg);
   LNE_CUDA_TRY(cudaGetLastError());
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, d_bounds);
   c->seg = seg;
   c->npanels = np;
-  c->panel_width = pw;
+  c->panel_bounds = bounds;
   c->panel_plans.resize(np);
   for (int p = 0; p < np; ++p) {
     PanelRows R{c->row_ptr, seg, c->col, c->val, np + 1, p};
@@ -185,14 +231,23 @@ extern "C" int lne_spmm(lne_ctx* ctx, const lne_csr* A, int x_prec, const void* 
                         float alpha, float beta, float* Y, int64_t ldy) {
   LNE_CHECK_ARG(ctx && A && X && Y, "lne_spmm: NULL argument");
   LNE_CHECK_ARG(d >= 1 && ldx >= d && ldy >= d, "lne_spmm: need 1 <= d <= ldx, ldy");
-  LNE_CHECK_ARG(x_prec == LNE_PREC_FP32 || x_prec == LNE_PREC_BF16 || x_prec == LNE_PREC_FP8,
-                "lne_spmm: x_prec must be FP32, BF16 or FP8");
+  LNE_CHECK_ARG(x_prec == LNE_PREC_FP32 || x_prec == LNE_PREC_BF16 || x_prec == LNE_PREC_FP8 ||
+                    x_prec == LNE_PREC_FP16,
+                "lne_spmm: x_prec must be FP32, BF16, FP16 or FP8");
   LNE_CHECK_ARG(ldx % (x_prec == LNE_PREC_FP8 ? 16 : 8) == 0 && ((uintptr_t)X % 16) == 0,
                 "lne_spmm: X rows must start on 16-byte boundaries (ldx a multiple of 8, 16 for FP8)");
   LNE_CUDA_TRY(cudaSetDevice(ctx->device));
   lne_csr* Am = const_cast<lne_csr*>(A);
   EpiAxpby epi{alpha, beta, Y, ldy, (int)d, false};
-  if (x_prec == LNE_PREC_FP32) return spmm_csr_panels<float>(ctx, Am, (const float*)X, ldx, d, epi);
-  if (x_prec == LNE_PREC_FP8) return spmm_csr_panels<__nv_fp8_e4m3>(ctx, Am, (const __nv_fp8_e4m3*)X, ldx, d, epi);
-  return spmm_csr_panels<__nv_bfloat16>(ctx, Am, (const __nv_bfloat16*)X, ldx, d, epi);
+  int launches = 0, rc;
+  if (x_prec == LNE_PREC_FP32)
+    rc = spmm_csr_panels<float>(ctx, Am, (const float*)X, ldx, d, epi, &launches);
+  else if (x_prec == LNE_PREC_FP8)
+    rc = spmm_csr_panels<__nv_fp8_e4m3>(ctx, Am, (const __nv_fp8_e4m3*)X, ldx, d, epi, &launches);
+  else if (x_prec == LNE_PREC_FP16)
+    rc = spmm_csr_panels<__half>(ctx, Am, (const __half*)X, ldx, d, epi, &launches);
+  else
+    rc = spmm_csr_panels<__nv_bfloat16>(ctx, Am, (const __nv_bfloat16*)X, ldx, d, epi, &launches);
+  if (rc == LNE_OK) ctx->launch_count += launches;
+  return rc;
 }

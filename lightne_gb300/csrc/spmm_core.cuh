@@ -90,12 +90,13 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
   constexpr int kUnroll = kStaged < 1 ? 1 : (kStaged > 4 ? 4 : kStaged);
   const int lane = threadIdx.x & 31;
   const int grp = lane / G, gl = lane % G;
-  if constexpr (E == 16) {
-    // 16 elements per vector (FP8): the gathers of 4 / VPL nonzeros are
-    // staged as raw 16-byte words (4 registers each), widened at the FMAs
+  if constexpr (E == 16 || (G & (G - 1)) != 0) {
+    // 16 elements per vector (FP8), or a group of 9 lanes: the gathers of
+    // 4 / VPL nonzeros are staged as raw 16-byte words (4 registers each),
+    // widened at the FMAs
     constexpr int kU = VPL >= 4 ? 1 : 4 / VPL;
-    // G = 9 (a 144-element row: 9 vectors): three groups of 9 lanes, lanes
-    // 27..31 idle
+    // G = 9 (a 144-element row: 9 FP8 vectors, or 18 BF16 / FP16 vectors
+    // at two per lane): three groups of 9 lanes, lanes 27..31 idle
     const bool in_grp = grp < P;
     for (int64_t base = j0; base < j1; base += 32) {
       const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);

@@ -58,9 +58,11 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
   while (c_off < c_total) {
     int64_t rem = c_total - c_off, C2 = 1;
     while (C2 * 2 <= rem && C2 * 2 <= 128) C2 *= 2;
-    // an FP8 row of 144 elements is one 9-vector slab (three groups of 9
-    // lanes): its tail vector shares the gathers of the row
+    // a 144-element row is one slab of three groups of 9 lanes: 9 FP8
+    // vectors (one per lane) or 18 BF16 / FP16 vectors (two per lane), so
+    // its tail shares the gathers of the row instead of a second pass
     if (E == 16 && rem == 9) C2 = 9;
+    if (E == 8 && rem == 18) C2 = 18;
     const int C = (int)C2;
     const int64_t ldp = (int64_t)C * E;
     if (plan.n_chunks > 0 && partial == nullptr) {
@@ -85,7 +87,9 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
       ldxs = (int64_t)C * E;
     }
     const int e_base = (int)(c_off * E);
-    if (E == 16 && (C == 1 || C == 9)) {
+    if (E == 8 && C == 18) {
+      if constexpr (E == 8) spmm_launch<XT, 9, 2>(ctx, R, plan, Xs, ldxs, C, partial, ldp, e_base, epi);
+    } else if (E == 16 && (C == 1 || C == 9)) {
       // FP8: one lane per nonzero for one vector, three 9-lane groups for a
       // 144-element row (instantiated for FP8 only)
       if constexpr (E == 16) {
@@ -130,24 +134,45 @@ static int spmm_run(lne_ctx* ctx, Rows R, const SpmmPlan& plan, const XT* X, int
 
 // Cache-blocked SpMM over a CSR: when the dense operand is larger than the
 // context's panel budget, the columns are cut into panels whose slice of X
-// fits in L2 and one pass per panel gathers only from that slice.  The
-// epilogue is called with add = false on the first panel and add = true on
-// the later ones (fixed panel order: reproducible sums).
+// fits in L2 and one pass per panel gathers only from that slice (panels of
+// at most the budget each, or, with a negative budget, two panels: the
+// lowest ids up to the budget, which on graphs whose hubs have low ids
+// take most of the gathers, then the rest).  The epilogue is called with
+// add = false on the first panel and add = true on the later ones (fixed
+// panel order: reproducible sums).
 template <typename XT, class EpiT>
 static int spmm_csr_panels(lne_ctx* ctx, lne_csr* A, const XT* X, int64_t ldx, int64_t d, EpiT epi,
-                           int* launches = nullptr) {
+                           int* launches = nullptr, int64_t panel_bytes = 0) {
   const int64_t row_bytes = ldx * (int64_t)sizeof(XT);
   const int64_t xbytes = A->n * row_bytes;
+  // the context's setting wins; otherwise the caller's suggestion
+  const int64_t want = ctx->spmm_panel_bytes != 0 ? ctx->spmm_panel_bytes : panel_bytes;
+  int64_t budget = want < 0 ? -want : want;
   int rc;
-  if (ctx->spmm_panel_bytes <= 0 || xbytes <= ctx->spmm_panel_bytes) {
+  if (want < 0 && budget > 0 && xbytes > budget) {
+    // a two-panel split pays only when the first panel takes most entries
+    const int64_t pw = std::max<int64_t>(1, budget / row_bytes);
+    if (launches && !(A->hub_share >= 0.0 && A->hub_cols == pw)) *launches += 1;
+    if ((rc = hub_share(ctx, A, pw))) return rc;
+    if (A->hub_share < 0.5) budget = 0;
+  }
+  if (budget == 0 || xbytes <= budget) {
     if (!A->plan_ready && launches) *launches += kPlanLaunches;
     if ((rc = build_plan_csr(ctx, A))) return rc;
     CsrRows R{A->row_ptr, A->col, A->val};
     epi.add = false;
     return spmm_run<XT>(ctx, R, A->plan, X, ldx, d, epi, launches, A->n);
   }
-  const int64_t pw = std::max<int64_t>(1, ctx->spmm_panel_bytes / row_bytes);
-  if ((rc = build_panels(ctx, A, pw))) return rc;
+  const int64_t pw = std::max<int64_t>(1, budget / row_bytes);
+  std::vector<int64_t> bounds{0};
+  if (want < 0) {
+    bounds.push_back(pw);
+  } else {
+    for (int64_t b = pw; b < A->n; b += pw) bounds.push_back(b);
+  }
+  bounds.push_back(A->n);
+  if (A->panel_bounds != bounds && launches) *launches += 1 + (int)(bounds.size() - 1) * kPlanLaunches;
+  if ((rc = build_panels(ctx, A, bounds))) return rc;
   for (int p = 0; p < A->npanels; ++p) {
     PanelRows R{A->row_ptr, A->seg, A->col, A->val, A->npanels + 1, p};
     epi.add = p > 0;

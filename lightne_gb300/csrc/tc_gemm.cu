@@ -145,7 +145,7 @@ __device__ __forceinline__ void tc_teardown(TcShared* sh, uint32_t tmem) {
 __global__ void __launch_bounds__(kTcThreads) k_tc_gemm_tall(const float* __restrict__ In, int64_t ldi, int K,
                                                              const float* __restrict__ W, int c2, int nmma, int64_t n,
                                                              float* __restrict__ Out, int64_t ldo,
-                                                             __nv_bfloat16* __restrict__ OutB, int* flags) {
+                                                             Copy16 OutB, int* flags) {
   extern __shared__ __align__(128) uint8_t smem[];
   TcShared* sh = reinterpret_cast<TcShared*>(smem + kStages * kStageBytes);
   tc_setup(sh);
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm_tall(const float* __rest
           if (col < ldo) {
             const float x = col < c2 ? v[i] : 0.0f;
             Out[row * ldo + col] = x;
-            if (OutB) OutB[row * ldo + col] = __float2bfloat16_rn(x);
+            copy16_put(OutB, row * ldo + col, x);
           }
         }
       }
@@ -306,7 +306,7 @@ __device__ __forceinline__ void stream_finish(StreamShared* sh, uint32_t tmem, u
 __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __restrict__ In, int64_t ldi, int K,
                                                                  const float* __restrict__ W, int c2, int nmma,
                                                                  int64_t n, float* __restrict__ Out, int64_t ldo,
-                                                                 __nv_bfloat16* __restrict__ OutB, int* flags) {
+                                                                 Copy16 OutB, int* flags) {
   extern __shared__ __align__(1024) uint8_t stream_smem[];
   const int nsl = (K + kSlice - 1) / kSlice;
   const uint32_t wslice = (uint32_t)nmma * kSliceRowBytes;
@@ -424,12 +424,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gemm_stream(const float* __
             for (int i = 0; i < 16; ++i)
               if (cg * 16 + i < ldo) orow[i] = v[i];
           }
-          if (OutB) {
-            __nv_bfloat16* brow = OutB + row * ldo + cg * 16;
-#pragma unroll
-            for (int i = 0; i < 16; ++i)
-              if (cg * 16 + i < ldo) brow[i] = __float2bfloat16_rn(v[i]);
-          }
+          copy16_put_row16(OutB, row, ldo, cg * 16, v, (int)std::min<int64_t>(16, ldo - cg * 16));
         }
       }
       tc::fence_before_sync();  // the next tile's first MMA follows a __syncthreads
@@ -471,7 +466,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const __grid_const
                                                              const float* __restrict__ In, int64_t ldi, int K,
                                                              const float* __restrict__ W, int c2, int nmma, int ring,
                                                              int64_t n, float* __restrict__ Out, int64_t ldo,
-                                                             __nv_bfloat16* __restrict__ OutB, int* flags) {
+                                                             Copy16 OutB, int* flags) {
   extern __shared__ __align__(1024) uint8_t stream_smem[];
   const int nsl = (K + kSlice - 1) / kSlice;
   const uint32_t wslice = (uint32_t)nmma * kSliceRowBytes;
@@ -660,12 +655,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const __grid_const
             for (int i = 0; i < 16; ++i)
               if (cg * 16 + i < ldo) orow[i] = v[i];
           }
-          if (OutB) {
-            __nv_bfloat16* brow = OutB + row * ldo + cg * 16;
-#pragma unroll
-            for (int i = 0; i < 16; ++i)
-              if (cg * 16 + i < ldo) brow[i] = __float2bfloat16_rn(v[i]);
-          }
+          copy16_put_row16(OutB, row, ldo, cg * 16, v, (int)std::min<int64_t>(16, ldo - cg * 16));
         }
       }
       tc::fence_before_sync();
@@ -1218,7 +1208,7 @@ static bool tmap_rows16x128(CUtensorMap* m, const float* base, int64_t rows, int
 }
 
 int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
-                 int64_t ldo, __nv_bfloat16* OutB) {
+                 int64_t ldo, Copy16 OutB) {
   if (n <= 0) return LNE_OK;
   const int nmma = std::max(16, (int)((std::max<int64_t>(c2, ldo) + 15) / 16 * 16));
   if (nmma > 256) {

@@ -56,7 +56,8 @@ def test_status_and_precision_constants_match_header():
     from lightne_gb300 import _lib
     txt = open(os.path.join(ROOT, "include", "lightne_gb300.h")).read()
     defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"^#define (LNE_[A-Z0-9_]+) (\d+)", txt, re.M)}
-    assert {"LNE_OK", "LNE_ERR_TABLE_FULL", "LNE_PREC_FP32", "LNE_PREC_BF16", "LNE_PREC_FP8"} <= set(defs)
+    assert {"LNE_OK", "LNE_ERR_TABLE_FULL", "LNE_PREC_FP32", "LNE_PREC_BF16", "LNE_PREC_FP8",
+            "LNE_PREC_FP16"} <= set(defs)
     for name, value in defs.items():
         if hasattr(_lib, name):
             assert getattr(_lib, name) == value, name

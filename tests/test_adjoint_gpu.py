@@ -1,7 +1,9 @@
 """Adjoint of the spectral propagation (lne_propagate_adjoint and the
 torch.autograd.Function) against an FP64 dense-operator autograd reference
 and FP64 central finite differences (step 1e-6).  Tolerances: dL/da and
-dL/dmu, dL/ds within 1e-4 relative (FP32 form)."""
+dL/dmu, dL/ds within 1e-4 relative (FP32 form).  The 16-bit forms gather
+16-bit vectors for dL/da (within 1e-3 for FP16, 3e-3 for BF16) and compute
+the parameter gradients in FP32 (within 1e-4)."""
 import math
 
 import numpy as np
@@ -67,6 +69,37 @@ def test_adjoint_matches_dense_autograd(ctx, order):
     assert rel < 1e-4, rel
     assert abs(dmu - mut.grad.item()) <= 1e-4 * abs(mut.grad.item()) + 1e-6, (dmu, mut.grad.item())
     assert abs(ds - st.grad.item()) <= 1e-4 * abs(st.grad.item()) + 1e-6, (ds, st.grad.item())
+    g.free()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp16", 1e-3), ("bf16", 3e-3)])
+@pytest.mark.parametrize("a_scale,g_scale", [(1.0, 1.0), (1e-5, 4e3)])
+def test_adjoint_16bit_forms(ctx, precision, tol, a_scale, g_scale):
+    """The 16-bit forms against the FP64 dense autograd; the second case puts
+    the input and the output gradient far outside FP16's normal range (the
+    FP16 form scales the output gradient by a power of two and unscales the
+    results).  dL/dmu and dL/ds come from the FP32 tangent pass."""
+    off, nbrs = graphs.chung_lu(400, 2500, 2.1, seed=43)
+    g = Graph.from_numpy(ctx, off, nbrs)
+    dim, order = 16, 10
+    rng = np.random.default_rng(7)
+    a = a_scale * rng.standard_normal((400, dim))
+    W = rng.standard_normal((dim, 4))
+    at = torch.tensor(a, requires_grad=True)
+    mut = torch.tensor(0.2, dtype=torch.float64, requires_grad=True)
+    st = torch.tensor(0.5, dtype=torch.float64, requires_grad=True)
+    y = dense_forward(off, nbrs, at, mut, st, order)
+    gy = g_scale * rng.standard_normal(tuple(y.shape))
+    (y * torch.tensor(gy)).sum().backward()
+    ga, dmu, ds = propagate_adjoint(ctx, g, a.astype(np.float32), gy.astype(np.float32), dim, order=order,
+                                    precision=precision)
+    ref = at.grad.numpy()
+    ga = ga.double().cpu().numpy()
+    assert np.isfinite(ga).all()
+    rel = np.linalg.norm(ga - ref) / np.linalg.norm(ref)
+    assert rel < tol, rel
+    assert abs(dmu - mut.grad.item()) <= 1e-4 * abs(mut.grad.item()), (dmu, mut.grad.item())
+    assert abs(ds - st.grad.item()) <= 1e-4 * abs(st.grad.item()), (ds, st.grad.item())
     g.free()
 
 

@@ -1,7 +1,10 @@
 """Randomized SVD, spectral propagation and dense embedding on the device
 against the FP64 oracle (oracle/linalg_oracle.py) with the same Gaussian
-sketches.  Tolerances: FP32 form <= 1e-4 relative embedding error after
-Procrustes; BF16 form <= 2e-2 (BF16 operands carry 2^-9 relative rounding)."""
+sketches.  Tolerances (relative embedding error after Procrustes, relative
+Frobenius error of the propagation): the FP32 form <= 1e-4 / 1e-5; the FP16
+form <= 1e-3, the gate the 16-bit forms are held to; the BF16 form, whose
+operands carry 2^-9 relative rounding, <= 3e-3 (it does not meet the gate on
+every input: its measured errors are recorded beside the benchmark)."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -26,15 +29,15 @@ def netsmf_matrix(ctx):
     g.free()
 
 
-@pytest.mark.parametrize("precision,tol", [("fp32", 1e-4), ("bf16", 2e-2)])
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-4), ("fp16", 1e-3), ("bf16", 3e-3)])
 @pytest.mark.parametrize("normalize", [False, True])
 def test_randsvd_matches_fp64(ctx, netsmf_matrix, precision, tol, normalize):
     csr, A, _ = netsmf_matrix
     rank, dim, seed = 48, 32, 777
     emb, S, st = randsvd(ctx, csr, rank, dim, normalize=normalize, precision=precision, seed=seed)
     om = gaussian(ctx, seed, 0, A.shape[0], rank)
-    if precision == "bf16":
-        om = om.to(torch.bfloat16).float()
+    # the 16-bit forms gather the sketch from an FP8 copy: exact
+    assert torch.equal(om.to(torch.float8_e4m3fn).float(), om)
     P = gaussian(ctx, seed, 1, rank, rank)
     ref, Sref = lo.randsvd(A, om.double().cpu().numpy(), P.double().cpu().numpy(), dim, normalize=normalize)
     e = emb.double().cpu().numpy()
@@ -53,7 +56,7 @@ def test_random_project_only(ctx, netsmf_matrix):
     np.testing.assert_allclose(emb.double().cpu().numpy(), ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
 
 
-@pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("bf16", 1.5e-2)])
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("fp16", 1e-3), ("bf16", 3e-3)])
 @pytest.mark.parametrize("order,dim", [(10, 128), (10, 20), (2, 16), (3, 16)])
 def test_propagate_matches_fp64(ctx, netsmf_matrix, precision, tol, order, dim):
     _, _, (off, nbrs) = netsmf_matrix
@@ -66,6 +69,22 @@ def test_propagate_matches_fp64(ctx, netsmf_matrix, precision, tol, order, dim):
     assert rel < tol, rel
     rel2 = np.linalg.norm(a2.double().cpu().numpy() - a2ref) / np.linalg.norm(a2ref)
     assert rel2 < tol, rel2
+    g.free()
+
+
+@pytest.mark.parametrize("scale", [1e-6, 1.0, 3e3])
+def test_propagate_fp16_input_scaling(ctx, netsmf_matrix, scale):
+    """The FP16 form scales its input by a power of two into FP16's range:
+    inputs far below or above it give the same relative error."""
+    _, _, (off, nbrs) = netsmf_matrix
+    g = Graph.from_numpy(ctx, off, nbrs)
+    a = (scale * np.random.default_rng(5).standard_normal((off.size - 1, 32))).astype(np.float32)
+    y, a2, _ = chebyshev_expansion(ctx, g, a, 32, order=10, precision="fp16", return_a=True)
+    yref, a2ref = lo.propagate(off, nbrs, a, order=10)
+    y = y.double().cpu().numpy()
+    assert np.isfinite(y).all()
+    rel = np.linalg.norm(y - yref) / np.linalg.norm(yref)
+    assert rel < 1e-3, rel
     g.free()
 
 

@@ -1,4 +1,4 @@
-"""lne_spmm (explicit CSR x dense, FP32, BF16 or FP8 dense operand) against an
+"""lne_spmm (explicit CSR x dense, FP32, BF16, FP16 or FP8 dense operand) against an
 FP64 numpy product of the same operands.  Tolerance: FP32 accumulation,
 |err| <= 1e-5 * (|A| |X|) elementwise."""
 import ctypes
@@ -8,7 +8,7 @@ import pytest
 import torch
 
 from lightne_gb300 import _lib
-from lightne_gb300._lib import LNE_PREC_BF16, LNE_PREC_FP8, LNE_PREC_FP32
+from lightne_gb300._lib import LNE_PREC_BF16, LNE_PREC_FP8, LNE_PREC_FP16, LNE_PREC_FP32
 from lightne_gb300.api import CSR
 
 pytestmark = pytest.mark.gpu
@@ -27,14 +27,16 @@ def random_csr(n, avg, long_rows=(), seed=0):
     return rp, col, val
 
 
-DTYPES = {LNE_PREC_FP32: torch.float32, LNE_PREC_BF16: torch.bfloat16, LNE_PREC_FP8: torch.float8_e4m3fn}
+DTYPES = {LNE_PREC_FP32: torch.float32, LNE_PREC_BF16: torch.bfloat16, LNE_PREC_FP8: torch.float8_e4m3fn,
+          LNE_PREC_FP16: torch.float16}
 
 
 @pytest.mark.parametrize("d,prec", [(128, LNE_PREC_FP32), (138, LNE_PREC_FP32), (20, LNE_PREC_FP32),
                                     (600, LNE_PREC_FP32), (128, LNE_PREC_BF16), (138, LNE_PREC_BF16),
                                     (60, LNE_PREC_BF16), (1100, LNE_PREC_BF16), (144, LNE_PREC_FP8),
                                     (138, LNE_PREC_FP8), (16, LNE_PREC_FP8), (700, LNE_PREC_FP8),
-                                    (2100, LNE_PREC_FP8)])
+                                    (2100, LNE_PREC_FP8), (144, LNE_PREC_FP16), (138, LNE_PREC_FP16),
+                                    (40, LNE_PREC_FP16)])
 def test_spmm_matches_fp64(ctx, lib, d, prec):
     n = 3000
     rp, col, val = random_csr(n, 12, long_rows=[(5, 2500), (77, 2049), (2999, 2048)], seed=d)
