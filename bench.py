@@ -28,6 +28,7 @@ the total over ranks divided by the max time over ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -346,6 +347,11 @@ def _lib_check(rc):
     _lib.check(rc)
 
 
+def _lib_load():
+    from lightne_gb300 import _lib
+    return _lib.load()
+
+
 def plain_struct(off, nbrs):
     """CSR structure of A + I with the self loop first in every row (the
     operator's layout, SpectralPropagation.h:51-75) and d~ = degree + 1."""
@@ -449,8 +455,9 @@ def run_ours(args, ws, rank, local):
         out, _, _ = pipeline_step(ctx, gg, w, HEADLINE, seed)
         torch.cuda.synchronize()
         tb = time.perf_counter()
-        host_out.copy_(out)
-        torch.cuda.synchronize()
+        # the embedding to the host through the C ABI (lne_copy_to_host)
+        _lib_check(_lib_load().lne_copy_to_host(ctx.handle, ctypes.c_void_p(host_out.data_ptr()),
+                                                ctypes.c_void_p(out.data_ptr()), out.numel() * 4))
         t1 = time.perf_counter()
         gg.free()
         if i > 0:
@@ -686,10 +693,11 @@ SCALE_RUNS = {
                rank=138, dim=128, order=10,
                label="R-MAT (0.57, 0.19, 0.19, 0.05) scale 22 edge factor 16 symmetrised dedup, T=10, "
                      "samples=10*T*m, rank 138, dim 128, K=10"),
-    "c5": dict(kind="sbm", n=1 << 23, blocks=50, degree=24.0, ratio=20.0, seed=6, walk_len=10, per_edge=40,
-               tablesz=4_250_000_000, rank=138, dim=128, order=10, adam_steps=20,
-               label="SBM n=2^23, 50 equal blocks, mean degree 24, p_in/p_out=20, T=10, samples=4*T*m (the pair "
-                     "table of 10*T*m would need 2^34 slots = 275 GB), rank 138, dim 128, K=10, 20 Adam steps"),
+    "c5": dict(kind="sbm", n=1 << 23, blocks=50, degree=24.0, ratio=20.0, seed=6, walk_len=10, per_edge=100,
+               tablesz=8_500_000_000, rank=138, dim=128, order=10, adam_steps=20,
+               label="SBM n=2^23, 50 equal blocks, mean degree 24, p_in/p_out=20, T=10, samples=10*T*m (a pair "
+                     "table of 2^34 slots, 275 GB, does not fit: hash-range rounds), rank 138, dim 128, K=10, "
+                     "20 Adam steps"),
 }
 
 
@@ -755,7 +763,7 @@ def run_scale(args, local):
         out["sparsify_s"] = time.time() - t
         sums.append(csr_checksum(csr))
     out["sparsify"] = {k: st[k] for k in ("samples_emitted", "distinct", "nnz_upper", "nnz", "capacity",
-                                          "ms_sample", "ms_trunclog", "ms_csr")}
+                                          "ms_sample", "ms_trunclog", "ms_csr", "sliced")}
     out["csr_row_ptr_ok"] = sums[0][1]
     out["deterministic"] = sums[0][0] == sums[1][0]
     embs = {}
@@ -778,7 +786,32 @@ def run_scale(args, local):
         out[prec + "_vs_fp32_svd_procrustes"] = lo.procrustes_rel_error(e16, e32)
         out[prec + "_vs_fp32_final_procrustes"] = lo.procrustes_rel_error(p16, p32)
         del e16, p16
-    del e32, p32
+    del p32
+    if w["kind"] == "rmat":
+        # The propagation and dense-SVD stages against the FP64 host oracle,
+        # on one common input (the FP32 form's SVD embedding): the FP64
+        # randomized SVD of this matrix (7.4e9 entries) is out of reach on
+        # the host, the propagation (133M graph entries) is not.
+        t = time.time()
+        a32 = e32.astype(np.float32)
+        del e32
+        yref, _ = lo.propagate(off, nbrs, a32, order=w["order"])
+        fin_ref, _ = lo.dense_embed(yref)
+        fp64 = {"oracle_seconds": None, "input": "the FP32 form's SVD embedding"}
+        for prec in FORMS:
+            y, _ = chebyshev_expansion(ctx, g, a32, w["dim"], order=w["order"], precision=prec)
+            yy = y.double().cpu().numpy()
+            fin, _ = get_embedding_dense(ctx, y, w["dim"])
+            del y
+            fp64[prec] = {"propagation_rel_frobenius": float(np.linalg.norm(yy - yref) / np.linalg.norm(yref)),
+                          "propagation_then_dense_svd_procrustes":
+                              lo.procrustes_rel_error(fin.double().cpu().numpy(), fin_ref)}
+            del yy, fin
+        dense, _ = get_embedding_dense(ctx, yref.astype(np.float32), w["dim"])
+        fp64["dense_svd_alone_procrustes"] = lo.procrustes_rel_error(dense.double().cpu().numpy(), fin_ref)
+        fp64["oracle_seconds"] = time.time() - t
+        out["fp64_stages"] = fp64
+        del yref, fin_ref, dense
     if labels is not None:
         emb = embs[HEADLINE][0]
         del embs

@@ -90,6 +90,18 @@ int lne_ctx_set_sparsify_slices(lne_ctx* ctx, int32_t slots, int32_t slice_bits)
  * Batches are sampled one edge range at a time and added to the pair table
  * in turn; only a run that fits one batch takes the sliced aggregation. */
 int lne_ctx_set_sparsify_batch(lne_ctx* ctx, int64_t keys);
+/* Hash-range rounds of lne_sparsify (no reference counterpart): with counts
+ * (-sample 0) and more samples than one batch, the sampler is replayed in
+ * rounds that each keep the samples of one range of pair hashes (a batch's
+ * worth), counted by the sliced aggregation; a first sweep counts each
+ * row's kept entries, a second writes them into their rows, and the rows
+ * are then sorted by column.  It needs the CSR plus one batch's buffers,
+ * where the pair table path needs the table and twice the CSR's entries.
+ * mode 0 (the default): rounds when the pair table and a batch do not fit
+ * in free device memory; 1: always; -1: never.  row_sort_max (a power of
+ * two up to 8192; 0: 8192): rows with more entries are sorted by the radix
+ * sort instead of in shared memory.  The output is the same either way. */
+int lne_ctx_set_sparsify_rounds(lne_ctx* ctx, int32_t mode, int32_t row_sort_max);
 /* Wait for all work queued on the context's stream. */
 int lne_ctx_synchronize(lne_ctx* ctx);
 /* Kernels the pipeline entry points (lne_sparsify, lne_randsvd,
@@ -100,7 +112,11 @@ int lne_ctx_launch_count(const lne_ctx* ctx, int64_t* out);
 
 /*
  * Device memory helpers for callers that do not link the CUDA runtime
- * (stream-ordered on the context's stream; copies synchronise).
+ * (stream-ordered on the context's stream; copies synchronise).  A host
+ * buffer that is page-locked and mapped (cudaHostAlloc or cudaHostRegister
+ * memory) is copied by a kernel over the CPU-GPU link, faster than a copy
+ * engine; pageable memory goes through cudaMemcpyAsync.  lne_graph_upload
+ * and lne_csr_download copy the same way.
  */
 int lne_device_alloc(lne_ctx* ctx, int64_t bytes, void** out);
 int lne_device_free(lne_ctx* ctx, void* p);
@@ -141,7 +157,8 @@ typedef struct lne_sparsify_stats {
   int64_t exp_rv_rounded, table_size, capacity, samples_emitted, distinct, nnz_upper, nnz;
   float ms_sample, ms_trunclog, ms_csr; /* device time per stage (CUDA events) */
   int32_t kernel_launches;              /* kernels this call launched */
-  int32_t sliced;                       /* 1: pairs counted by the sliced aggregation, 0: pair table */
+  int32_t sliced;                       /* 1: pairs counted by the sliced aggregation, 0: pair table,
+                                           2: hash-range rounds */
 } lne_sparsify_stats;
 
 /*

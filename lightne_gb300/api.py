@@ -52,6 +52,12 @@ class Context:
         """Samples per batch of the sparsifier (0: the default 2^30)."""
         check(_lib.load().lne_ctx_set_sparsify_batch(self.handle, keys))
 
+    def set_sparsify_rounds(self, mode: int = 0, row_sort_max: int = 0) -> None:
+        """Hash-range rounds above one batch of samples (counts): 0 when the
+        pair table does not fit, 1 always, -1 never; rows longer than
+        row_sort_max (0: 8192) are sorted by the radix sort."""
+        check(_lib.load().lne_ctx_set_sparsify_rounds(self.handle, mode, row_sort_max))
+
     def close(self) -> None:
         if self.handle:
             _lib.load().lne_ctx_destroy(self.handle)

@@ -279,11 +279,69 @@ int lne_ctx_synchronize(lne_ctx* ctx) {
   return LNE_OK;
 }
 
+int lne_ctx_set_sparsify_rounds(lne_ctx* ctx, int32_t mode, int32_t row_sort_max) {
+  LNE_CHECK_ARG(ctx != nullptr && mode >= -1 && mode <= 1, "lne_ctx_set_sparsify_rounds: bad argument");
+  LNE_CHECK_ARG(row_sort_max == 0 || (row_sort_max >= 2 && row_sort_max <= 8192 &&
+                                      (row_sort_max & (row_sort_max - 1)) == 0),
+                "lne_ctx_set_sparsify_rounds: row_sort_max must be 0 or a power of two in [2, 8192]");
+  ctx->sparsify_rounds = mode;
+  ctx->sparsify_row_sort_max = row_sort_max ? row_sort_max : 8192;
+  return LNE_OK;
+}
+
 int lne_ctx_launch_count(const lne_ctx* ctx, int64_t* out) {
   LNE_CHECK_ARG(ctx != nullptr && out != nullptr, "lne_ctx_launch_count: NULL argument");
   *out = ctx->launch_count;
   return LNE_OK;
 }
+
+}  // extern "C"
+
+namespace lne {
+
+// Byte copy through the SMs: 16-byte vectors where both ends allow, bytes
+// at the edges.
+__global__ void k_copy_sm(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, int64_t bytes) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  const int64_t head = (int64_t)((16 - ((uintptr_t)src & 15)) & 15);
+  const bool vec = (((uintptr_t)src ^ (uintptr_t)dst) & 15) == 0 && bytes > head;
+  if (!vec) {
+    for (int64_t i = tid; i < bytes; i += nth) dst[i] = src[i];
+    return;
+  }
+  const int64_t n16 = (bytes - head) / 16;
+  const uint4* s16 = reinterpret_cast<const uint4*>(src + head);
+  uint4* d16 = reinterpret_cast<uint4*>(dst + head);
+  for (int64_t i = tid; i < n16; i += nth) d16[i] = s16[i];
+  if (tid < head) dst[tid] = src[tid];
+  const int64_t tail0 = head + 16 * n16;
+  if (tid < bytes - tail0) dst[tail0 + tid] = src[tail0 + tid];
+}
+
+int copy_async(lne_ctx* ctx, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+  if (bytes == 0) return LNE_OK;
+  const void* host = kind == cudaMemcpyDeviceToHost ? dst : src;
+  cudaPointerAttributes a;
+  if ((kind == cudaMemcpyDeviceToHost || kind == cudaMemcpyHostToDevice) &&
+      cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+      a.devicePointer != nullptr && bytes >= ((size_t)1 << 20)) {
+    const int64_t off = (const char*)host - (const char*)a.hostPointer;
+    char* hd = (char*)a.devicePointer + (a.hostPointer ? off : 0);
+    const uint8_t* s = kind == cudaMemcpyDeviceToHost ? (const uint8_t*)src : (const uint8_t*)hd;
+    uint8_t* d = kind == cudaMemcpyDeviceToHost ? (uint8_t*)hd : (uint8_t*)dst;
+    k_copy_sm<<<(unsigned)(ctx->num_sms * 4), 512, 0, ctx->stream>>>(s, d, (int64_t)bytes);
+    LNE_CUDA_TRY(cudaGetLastError());
+    return LNE_OK;
+  }
+  cudaGetLastError();  // a failed attribute query leaves an error behind
+  LNE_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream));
+  return LNE_OK;
+}
+
+}  // namespace lne
+
+extern "C" {
 
 static int graph_build_common(lne_ctx* ctx, lne_graph* g, const int32_t* d_nbrs_in) {
   const int64_t n = g->n;
@@ -368,22 +426,21 @@ static int graph_upload_impl(lne_ctx* ctx, int64_t n, const int64_t* offsets, co
   const int32_t* d_nbrs_in = nullptr;
   int32_t* staged = nullptr;
   cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  cudaError_t e = cudaMemcpyAsync(g->off64, offsets, sizeof(int64_t) * (n + 1), kind, ctx->stream);
-  if (e == cudaSuccess && m_dir > 0) {
+  rc = copy_async(ctx, g->off64, offsets, sizeof(int64_t) * (n + 1), kind);
+  if (rc == LNE_OK && m_dir > 0) {
     if (on_device) {
       d_nbrs_in = nbrs;
     } else {
       // Stage the host neighbours in the `src` buffer's twin: copy into nbrs
       // directly and let the build kernel rewrite in place.
       staged = (int32_t*)g->nbrs;
-      e = cudaMemcpyAsync(staged, nbrs, sizeof(int32_t) * m_dir, cudaMemcpyHostToDevice, ctx->stream);
+      rc = copy_async(ctx, staged, nbrs, sizeof(int32_t) * m_dir, cudaMemcpyHostToDevice);
       d_nbrs_in = staged;
     }
   }
-  if (e != cudaSuccess) {
-    set_error(std::string("lne_graph_upload: copy failed: ") + cudaGetErrorString(e));
+  if (rc) {
     lne_graph_free(g);
-    return LNE_ERR_CUDA;
+    return rc;
   }
   rc = graph_build_common(ctx, g, d_nbrs_in);
   if (rc) { lne_graph_free(g); return rc; }
@@ -415,14 +472,18 @@ int lne_device_free(lne_ctx* ctx, void* p) {
 
 int lne_copy_to_host(lne_ctx* ctx, void* host_dst, const void* dev_src, int64_t bytes) {
   LNE_CHECK_ARG(ctx && host_dst && dev_src && bytes >= 0, "lne_copy_to_host: bad argument");
-  LNE_CUDA_TRY(cudaMemcpyAsync(host_dst, dev_src, (size_t)bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  int rc = copy_async(ctx, host_dst, dev_src, (size_t)bytes, cudaMemcpyDeviceToHost);
+  if (rc) return rc;
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return LNE_OK;
 }
 
 int lne_copy_to_device(lne_ctx* ctx, void* dev_dst, const void* host_src, int64_t bytes) {
   LNE_CHECK_ARG(ctx && dev_dst && host_src && bytes >= 0, "lne_copy_to_device: bad argument");
-  LNE_CUDA_TRY(cudaMemcpyAsync(dev_dst, host_src, (size_t)bytes, cudaMemcpyHostToDevice, ctx->stream));
+  LNE_CUDA_TRY(cudaSetDevice(ctx->device));
+  int rc = copy_async(ctx, dev_dst, host_src, (size_t)bytes, cudaMemcpyHostToDevice);
+  if (rc) return rc;
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return LNE_OK;
 }
@@ -436,13 +497,13 @@ int lne_csr_info(const lne_csr* c, int64_t* n, int64_t* nnz) {
 
 int lne_csr_download(lne_ctx* ctx, const lne_csr* c, int64_t* row_ptr, int32_t* col, float* val) {
   LNE_CHECK_ARG(ctx && c, "lne_csr_download: NULL argument");
-  if (row_ptr)
-    LNE_CUDA_TRY(cudaMemcpyAsync(row_ptr, c->row_ptr, sizeof(int64_t) * (c->n + 1), cudaMemcpyDeviceToHost,
-                                 ctx->stream));
-  if (col && c->nnz)
-    LNE_CUDA_TRY(cudaMemcpyAsync(col, c->col, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost, ctx->stream));
-  if (val && c->nnz)
-    LNE_CUDA_TRY(cudaMemcpyAsync(val, c->val, sizeof(float) * c->nnz, cudaMemcpyDeviceToHost, ctx->stream));
+  int rc;
+  if (row_ptr && (rc = copy_async(ctx, row_ptr, c->row_ptr, sizeof(int64_t) * (c->n + 1), cudaMemcpyDeviceToHost)))
+    return rc;
+  if (col && c->nnz && (rc = copy_async(ctx, col, c->col, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost)))
+    return rc;
+  if (val && c->nnz && (rc = copy_async(ctx, val, c->val, sizeof(float) * c->nnz, cudaMemcpyDeviceToHost)))
+    return rc;
   LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return LNE_OK;
 }

@@ -69,6 +69,11 @@ struct lne_ctx {
   int sparsify_slice_bits = -1;
   // samples per batch of the sparsifier's sample buffer (8 B each)
   int64_t sparsify_batch_keys = (int64_t)1 << 30;
+  // hash-range rounds above one batch (counts): 0 when the pair table does
+  // not fit, 1 always, -1 never; rows longer than row_sort_max (a power of
+  // two) are sorted by the radix sort instead of in shared memory
+  int sparsify_rounds = 0;
+  int sparsify_row_sort_max = 8192;
   // kernels launched by the entry points that ran on this context (each
   // adds its own count when it returns successfully)
   int64_t launch_count = 0;
@@ -126,6 +131,13 @@ struct lne_csr {
   } while (0)
 
 namespace lne {
+
+// Stream-ordered copy between host and device memory on ctx->stream.  A
+// page-locked host buffer mapped into the device's address space (1 MiB or
+// more) is copied by a kernel: the SMs' loads and stores over the CPU-GPU
+// link reach more bandwidth than one copy engine.  Anything else goes
+// through cudaMemcpyAsync.
+int copy_async(lne_ctx* ctx, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind);
 
 // Stream-ordered allocation on the context's stream; returns LNE_OK or
 // LNE_ERR_ALLOC with the message set.

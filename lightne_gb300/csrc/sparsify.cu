@@ -50,6 +50,11 @@ struct SampleArgs {
   double logn;
   uint64_t mask;
   int use_frac;
+  // hash-range rounds (the counts path above one batch): keep only the
+  // samples whose hashed key has these top qbits (0: keep every sample),
+  // and store the key rotated left by qbits
+  int qbits;
+  uint32_t qsel;
 };
 
 __device__ __forceinline__ bool table_full(const int* flags) {
@@ -280,39 +285,62 @@ __global__ void __launch_bounds__(kWalkThreads, 6) k_walk(const Vertex* __restri
 // about half the lanes.  Here every lane runs the same instructions; only
 // the neighbour load (walk phases) and the vertex-record load (a walk that
 // goes on) are predicated.  HASHED writes hash64_2(key) instead of the key.
+// The grid is persistent: a lane whose edge has drawn all its samples takes
+// the next unstarted edge of [e0, e1) from edge_ctr (one atomic per warp
+// and refill), so the lanes of a warp stay busy until the range runs out
+// instead of waiting for the warp's longest edge.  Which lane samples which
+// edge does not change any sample: every edge's draws come from its own
+// generator, fork((u << 32) | v).
 template <bool HASHED>
 __global__ void __launch_bounds__(kWalkThreads, 6) k_walk_counts(
     const Vertex* __restrict__ vd, const uint32_t* __restrict__ nbrs, const uint32_t* __restrict__ src, int64_t e0,
     int64_t e1, SampleArgs a, unsigned long long* __restrict__ out_keys, unsigned long long* __restrict__ out_count,
-    uint64_t out_cap, int* flags) {
+    uint64_t out_cap, int* flags, unsigned long long* __restrict__ edge_ctr) {
   __shared__ unsigned long long qk[kWalkThreads / 32][kQueue];
   __shared__ unsigned long long rmag[kMaxRMagic + 1];
   for (int i = threadIdx.x; i <= kMaxRMagic; i += blockDim.x) rmag[i] = gm_magic(i > 0 ? (uint32_t)i : 1u);
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t e = e0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  bool active = e < e1;
+  bool active = false, exhausted = false;
   uint32_t u = 0, v = 0, x = 0, left1 = 0, left2 = 0, r = 1;
   uint32_t cur_off = 0, div = 1;
   uint64_t mag = 1;
   uint4 vu = make_uint4(0, 1, 1, 0), vv = make_uint4(0, 1, 1, 0);
   uint64_t s = 0, todo = 0;
   int phase = kPhR;
-  if (active) {
-    u = __ldg(src + e);
-    v = __ldg(nbrs + e);
-    vu = __ldg(reinterpret_cast<const uint4*>(vd + u));
-    vv = __ldg(reinterpret_cast<const uint4*>(vd + v));
-    s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
-    todo = a.exp_rv;
-    if (a.use_frac) todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
-    active = todo > 0;
-    div = (uint32_t)a.walk_len;
-    mag = a.walk_magic;
-  }
   const uint32_t T = (uint32_t)a.walk_len;
   int qlen = 0;  // warp-uniform
-  while (__any_sync(kFullMask, active)) {
+  for (;;) {
+    // refill: the lanes without an edge take the next ones
+    const unsigned need = __ballot_sync(kFullMask, !active && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(edge_ctr, (unsigned long long)__popc(need));
+      base = __shfl_sync(kFullMask, base, leader);
+      if (!active && !exhausted) {
+        const int64_t e = e0 + (int64_t)base + __popc(need & ((1u << lane) - 1));
+        if (e >= e1) {
+          exhausted = true;
+        } else {
+          u = __ldg(src + e);
+          v = __ldg(nbrs + e);
+          vu = __ldg(reinterpret_cast<const uint4*>(vd + u));
+          vv = __ldg(reinterpret_cast<const uint4*>(vd + v));
+          s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
+          todo = a.exp_rv;
+          if (a.use_frac) todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
+          active = todo > 0;
+          phase = kPhR;
+          div = T;
+          mag = a.walk_magic;
+        }
+      }
+    }
+    if (!__any_sync(kFullMask, active)) {
+      if (__all_sync(kFullMask, exhausted)) break;
+      continue;  // lanes whose new edge has no samples take another
+    }
     const uint64_t rnd = rng_draw(s);
     const uint32_t m = gm_mod(rnd, div, mag);
     const bool isR = phase == kPhR, isK = phase == kPhK, isW1 = phase == kPhW1;
@@ -334,12 +362,19 @@ __global__ void __launch_bounds__(kWalkThreads, 6) k_walk_counts(
     uint4 rec = to_v ? vv : vu;
     if (active && isW && (go_u || go_v)) rec = __ldg(reinterpret_cast<const uint4*>(vd + pos));
     const uint32_t rn = m + 1u;  // r from the first draw of a sample
-    const bool emit = active && end;
+    const bool fin = active && end;  // a sample completes
+    bool emit = fin;
     unsigned long long key = 0;
-    if (emit) {
+    if (fin) {
       const uint32_t lo = xn < eb ? xn : eb, hi = xn < eb ? eb : xn;
       key = ((uint64_t)lo << 32) + (uint64_t)hi;
-      if (HASHED) key = hash64_2(key);
+      if (HASHED) {
+        key = hash64_2(key);
+        if (a.qbits) {
+          emit = (uint32_t)(key >> (64 - a.qbits)) == a.qsel;
+          key = (key << a.qbits) | (key >> (64 - a.qbits));
+        }
+      }
     }
     // next state
     const uint64_t rmg = rmag[rn <= (uint32_t)kMaxRMagic ? rn : 0u];
@@ -362,7 +397,7 @@ __global__ void __launch_bounds__(kWalkThreads, 6) k_walk_counts(
       mag = ((uint64_t)rec.w << 32) | rec.z;
       if (div == 0) active = false;  // unreachable for a validated (symmetric) graph
     }
-    if (emit && --todo == 0) active = false;
+    if (fin && --todo == 0) active = false;
     // stage this iteration's keys in the warp queue
     const unsigned em = __ballot_sync(kFullMask, emit);
     if (emit) qk[wid][qlen + __popc(em & ((1u << lane) - 1))] = key;
@@ -471,7 +506,7 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_slice_count(const unsigned
                                                                   int slots_max, Slot* __restrict__ uniq,
                                                                   unsigned long long* __restrict__ n_distinct,
                                                                   unsigned long long* __restrict__ n_samples,
-                                                                  int* __restrict__ flags) {
+                                                                  int* __restrict__ flags, int qbits) {
   extern __shared__ __align__(16) unsigned char slice_smem[];
   unsigned long long* sk = reinterpret_cast<unsigned long long*>(slice_smem);
   unsigned* sc = reinterpret_cast<unsigned*>(slice_smem + sizeof(unsigned long long) * slots_max);
@@ -571,8 +606,10 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_slice_count(const unsigned
 #pragma unroll
       for (int q = 0; q < kSliceMaskRegs; ++q) {
         const int j = (wid + q * nwarps) * 32 + lane;
-        if ((mask[q] >> lane) & 1u)
-          uniq[pos + __popc(mask[q] & lt)] = Slot{hash64_2_inv(sk[j]), (unsigned long long)sc[j]};
+        if ((mask[q] >> lane) & 1u) {
+          const unsigned long long h = qbits ? (sk[j] >> qbits) | (sk[j] << (64 - qbits)) : sk[j];
+          uniq[pos + __popc(mask[q] & lt)] = Slot{hash64_2_inv(h), (unsigned long long)sc[j]};
+        }
         pos += __popc(mask[q]);
       }
       __syncthreads();  // the table is cleared for the next slice
@@ -780,12 +817,56 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
 
   // warp-uniform loop: the lanes of a warp read 32 consecutive slots
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  if (DENSE) {  // every slot occupied (the distinct pairs of the sliced aggregation)
-    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < cap; b += stride) {
-      const uint64_t i = b + lane;
+  if (DENSE) {
+    // every slot occupied (the distinct pairs of the sliced aggregation):
+    // block-uniform rounds of 256 consecutive pairs, whose items are placed
+    // with one atomic on the item count per round (per warp, the atomics on
+    // that one counter serialise in L2)
+    __shared__ unsigned wsum[8];
+    __shared__ unsigned long long bbase;
+    for (uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x; b0 < cap; b0 += stride) {
+      const uint64_t i = b0 + threadIdx.x;
       const bool have = i < cap;
       const Slot sl = have ? T[i] : Slot{kEmptyKey, 0ULL};
-      emit(have, sl.key, sl.val);
+      TruncLogOut<WEIGHTED> o;
+      o.nitem = 0;
+      if (have) o = trunclog_entry<WEIGHTED>(sl.key, sl.val, vd, factor, xf, upper, tab);
+      if (o.nitem) {
+        atomicAdd(&rowcnt[o.u], 1ULL);
+        if (o.nitem == 2) atomicAdd(&rowcnt[o.v], 1ULL);
+        ++kept;
+      }
+      unsigned incl = o.nitem;
+#pragma unroll
+      for (int sh = 1; sh < 32; sh <<= 1) {
+        const unsigned t = __shfl_up_sync(kFullMask, incl, sh);
+        if (lane >= sh) incl += t;
+      }
+      if (lane == 31) wsum[wid] = incl;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += wsum[w];
+        bbase = tot ? atomicAdd(n_items, (unsigned long long)tot) : 0ULL;
+      }
+      __syncthreads();
+      unsigned before = 0;
+      for (int w = 0; w < wid; ++w) before += wsum[w];
+      if (o.nitem) {
+        const uint64_t pos = bbase + before + incl - o.nitem;
+        if (pos + o.nitem <= max_items) {
+          const uint32_t fb = __float_as_uint(o.f);
+          okeys[pos] = ((unsigned long long)o.u << cbits) | o.v;
+          ovals[pos] = fb;
+          if (o.nitem == 2) {
+            okeys[pos + 1] = ((unsigned long long)o.v << cbits) | o.u;
+            ovals[pos + 1] = fb;
+          }
+        } else {
+          atomicOr(&flags[kFlagSortOverflow], 1);
+        }
+      }
+      __syncthreads();  // wsum and bbase are rewritten in the next round
     }
   }
   for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); !DENSE && b < cap; b += stride) {
@@ -863,6 +944,403 @@ struct Events {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Hash-range rounds: the counts path (-sample 0) above one batch of samples
+// when the reference's pair table does not fit in device memory (or when
+// lne_ctx_set_sparsify_rounds forces it).  The sampler is a function of
+// the seed and the edge alone, so it can be replayed: round q replays all
+// edges and keeps the samples whose hash64_2(key) has top bits q, which
+// then fit one batch of the sliced aggregation; the rounds' distinct pairs
+// are disjoint (a pair's samples all fall in one round), so every pair is
+// counted whole in one round.  A first sweep over the rounds applies the
+// trunc-log and counts each row's kept entries (row_ptr); a second sweep
+// replays the rounds and writes each kept entry into its row at an atomic
+// cursor; a last pass sorts every row by column.  Peak memory is the CSR
+// plus one round's buffers, where the pair table path needs the table and
+// twice the CSR's items.
+// ---------------------------------------------------------------------------
+// Total samples (M_exact for counts): per directed entry exp_rv, plus one
+// when the entry's first draw falls below frac (as the sampler starts).
+__global__ void k_count_samples(const uint32_t* __restrict__ nbrs, const uint32_t* __restrict__ src, int64_t m_dir,
+                                SampleArgs a, unsigned long long* __restrict__ total) {
+  unsigned long long c = 0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m_dir; e += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t u = __ldg(src + e), v = __ldg(nbrs + e);
+    uint64_t s = rng_fork(a.seed, ((uint64_t)u << 32) | (uint64_t)v);
+    uint64_t todo = a.exp_rv;
+    if (a.use_frac) todo += (map_uint64(rng_draw(s)) < a.frac) ? 1u : 0u;
+    c += todo;
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(kFullMask, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(total, c);
+}
+
+// Trunc-log of a round's distinct pairs: SCATTER = false counts the kept
+// entries per row (rowcnt) and the kept pairs; SCATTER = true writes each
+// kept entry at row_ptr[row] + an atomic cursor (rowcnt, zeroed first).
+template <bool SCATTER>
+__global__ void __launch_bounds__(256) k_trunclog_rows(const Slot* __restrict__ T, uint64_t count,
+                                                       const Vertex* __restrict__ vd, double factor, int upper,
+                                                       const LogTable* __restrict__ ltab,
+                                                       unsigned long long* __restrict__ rowcnt,
+                                                       unsigned long long* __restrict__ kept_total,
+                                                       const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col,
+                                                       float* __restrict__ val, int* __restrict__ flags) {
+  __shared__ LogTable tab;
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+    tab.log_hi[i] = ltab->log_hi[i];
+    tab.log_lo[i] = ltab->log_lo[i];
+    tab.inv_hi[i] = ltab->inv_hi[i];
+    tab.inv_lo[i] = ltab->inv_lo[i];
+  }
+  __syncthreads();
+  const XDouble xf = xd_from_double(factor);
+  unsigned long long kept = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const Slot sl = T[i];
+    const TruncLogOut<false> o = trunclog_entry<false>(sl.key, sl.val, vd, factor, xf, upper, tab);
+    if (!o.nitem) continue;
+    ++kept;
+    if (!SCATTER) {
+      atomicAdd(&rowcnt[o.u], 1ULL);
+      if (o.nitem == 2) atomicAdd(&rowcnt[o.v], 1ULL);
+    } else {
+      // the first sweep counted exactly these entries; a cursor past its
+      // row is reported instead of written
+      const int64_t cu = (int64_t)atomicAdd(&rowcnt[o.u], 1ULL);
+      if (cu < row_ptr[o.u + 1] - row_ptr[o.u]) {
+        col[row_ptr[o.u] + cu] = (int32_t)o.v;
+        val[row_ptr[o.u] + cu] = o.f;
+      } else {
+        atomicOr(&flags[kFlagSortOverflow], 1);
+      }
+      if (o.nitem == 2) {
+        const int64_t cv = (int64_t)atomicAdd(&rowcnt[o.v], 1ULL);
+        if (cv < row_ptr[o.v + 1] - row_ptr[o.v]) {
+          col[row_ptr[o.v] + cv] = (int32_t)o.u;
+          val[row_ptr[o.v] + cv] = o.f;
+        } else {
+          atomicOr(&flags[kFlagSortOverflow], 1);
+        }
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) kept += __shfl_down_sync(kFullMask, kept, o);
+  if ((threadIdx.x & 31) == 0 && kept) atomicAdd(kept_total, kept);
+}
+
+// Sorts every row of at most maxlen entries (a power of two) by column in
+// shared memory (bitonic, on (col << 32 | value bits): columns are distinct
+// within a row); longer rows are listed in big (count in *nbig).
+__global__ void __launch_bounds__(256) k_row_sort(const int64_t* __restrict__ row_ptr, int64_t n,
+                                                  int32_t* __restrict__ col, float* __restrict__ val, int maxlen,
+                                                  uint32_t* __restrict__ big, unsigned long long* __restrict__ nbig) {
+  extern __shared__ unsigned long long rs_key[];
+  for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
+    const int64_t a = row_ptr[r];
+    const int64_t len = row_ptr[r + 1] - a;
+    if (len <= 1) continue;  // the whole block
+    if (len > maxlen) {
+      if (threadIdx.x == 0) big[atomicAdd(nbig, 1ULL)] = (uint32_t)r;
+      continue;
+    }
+    int P = 2;
+    while (P < len) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+      rs_key[i] = i < len ? (((unsigned long long)(uint32_t)col[a + i] << 32) | __float_as_uint(val[a + i]))
+                          : ~0ULL;
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+          const int ixj = i ^ j;
+          if (ixj > i) {
+            const unsigned long long x = rs_key[i], y = rs_key[ixj];
+            const bool up = (i & k) == 0;
+            if ((x > y) == up) {
+              rs_key[i] = y;
+              rs_key[ixj] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+      const unsigned long long x = rs_key[i];
+      col[a + i] = (int32_t)(x >> 32);
+      val[a + i] = __uint_as_float((uint32_t)x);
+    }
+    __syncthreads();
+  }
+}
+
+// The rows longer than the shared-memory sort: their entries as
+// ((big index) << 32 | col, value bits), in big-row order (GATHER), or the
+// sorted columns and values written back into their rows.
+template <bool GATHER>
+__global__ void k_big_rows(const uint32_t* __restrict__ big, const int64_t* __restrict__ bpref, int64_t nbig,
+                           const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col, float* __restrict__ val,
+                           unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
+                           const int32_t* __restrict__ scol, const float* __restrict__ sval) {
+  for (int64_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+    const int64_t a = row_ptr[big[b]];
+    const int64_t o = bpref[b], len = bpref[b + 1] - bpref[b];
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+      if (GATHER) {
+        keys[o + i] = ((unsigned long long)b << 32) | (uint32_t)col[a + i];
+        vals[o + i] = __float_as_uint(val[a + i]);
+      } else {
+        col[a + i] = scol[o + i];
+        val[a + i] = sval[o + i];
+      }
+    }
+  }
+}
+
+// The rounds path (see above).  Fills *out and stats like lne_sparsify.
+static int sparsify_rounds(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_params* p, SampleArgs a,
+                           uint64_t cap, uint64_t buf_keys, double logn, double M, double inv_lambda, double frac,
+                           size_t exp_rv, size_t table_size, lne_csr** out, lne_sparsify_stats* stats) {
+  cudaStream_t st = ctx->stream;
+  const int64_t n = g->n, m_dir = g->m_dir;
+  const int slots_max = std::min(ctx->sparsify_slice_slots, kSliceSlotsMax);
+  const size_t slice_smem = (size_t)slots_max * (sizeof(unsigned long long) + sizeof(unsigned));
+  Scratch S(ctx);
+  Events ev;
+  int rc, launches = 0;
+  unsigned long long* cnt = nullptr;  // [0] samples [1] round emitted [2] round distinct [3] round counted
+                                      // [4] kept pairs [5] big rows [6] next edge of the sampler
+  if ((rc = S.get((void**)&cnt, 64, "round counters"))) return rc;
+  LNE_CUDA_TRY(cudaMemsetAsync(cnt, 0, 64, st));
+  LNE_CUDA_TRY(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * kFlagWords, st));
+  cudaEventRecord(ev.e[0], st);
+  k_count_samples<<<grid_for(m_dir, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(g->nbrs, g->src, m_dir, a, cnt);
+  ++launches;
+  unsigned long long total = 0;
+  LNE_CUDA_TRY(cudaMemcpyAsync(&total, cnt, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaStreamSynchronize(st));
+  const double M_exact = (double)total;
+  const double factor = (double)(size_t)m_dir * (double)(size_t)m_dir / M_exact / 2 / (double)(size_t)p->negative;
+  // rounds of at most ~60% of a batch each, in expectation
+  int qbits = 0;
+  while (qbits < 16 && (total >> qbits) > buf_keys * 6 / 10) ++qbits;
+  const uint32_t Q = 1u << qbits;
+  unsigned long long *keys = nullptr, *keys2 = nullptr, *rowcnt = nullptr;
+  Slot* uniq = nullptr;
+  int64_t* starts = nullptr;
+  void* scan_tmp = nullptr;
+  if ((rc = S.get((void**)&keys, sizeof(unsigned long long) * buf_keys, "sample buffer")) ||
+      (rc = S.get((void**)&keys2, sizeof(unsigned long long) * buf_keys, "partitioned samples")) ||
+      (rc = S.get((void**)&uniq, sizeof(Slot) * buf_keys, "distinct pairs")) ||
+      (rc = S.get((void**)&starts, sizeof(int64_t) * (((int64_t)1 << kSliceBitsMax) + 1), "slice starts")) ||
+      (rc = S.get((void**)&rowcnt, sizeof(unsigned long long) * n, "row counts")) ||
+      (rc = S.get(&scan_tmp, scan_tmp_bytes(n), "scan scratch")))
+    return rc;
+  LNE_CUDA_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(unsigned long long) * n, st));
+  LNE_CUDA_TRY(cudaFuncSetAttribute(k_slice_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)slice_smem));
+  const unsigned wblocks = (unsigned)std::min<int64_t>((m_dir + kWalkThreads - 1) / kWalkThreads,
+                                                       (int64_t)ctx->num_sms * 6);
+  const unsigned tgrid_cap = (unsigned)ctx->num_sms * 16;
+  int64_t* row_ptr = nullptr;
+  int32_t* col = nullptr;
+  float* val = nullptr;
+  auto fail = [&](int code) {
+    dfree(ctx, row_ptr);
+    dfree(ctx, col);
+    dfree(ctx, val);
+    return code;
+  };
+  unsigned long long distinct = 0, counted = 0;
+  int64_t nnz = 0;
+  for (int sweep = 0; sweep < 2; ++sweep) {
+    if (sweep == 1) {
+      if (distinct >= cap) {
+        char buf[256];
+        snprintf(buf, sizeof(buf),
+                 "lne_sparsify: %llu distinct pairs do not fit the pair table's %llu slots; raise -tablesz (the "
+                 "reference prints \"looping forever\" and exits)",
+                 distinct, (unsigned long long)cap);
+        set_error(buf);
+        return LNE_ERR_TABLE_FULL;
+      }
+      if (counted != total) {
+        set_error("lne_sparsify: the rounds counted a different number of samples (internal error)");
+        return LNE_ERR_UNSUPPORTED;
+      }
+      if ((rc = dalloc(ctx, (void**)&row_ptr, sizeof(int64_t) * (n + 1), "row_ptr"))) return rc;
+      scan_exclusive_i64((const int64_t*)rowcnt, row_ptr, n, scan_tmp, st);
+      launches += 3;
+      LNE_CUDA_TRY(cudaMemcpyAsync(&nnz, row_ptr + n, 8, cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaStreamSynchronize(st));
+      if ((rc = dalloc(ctx, (void**)&col, sizeof(int32_t) * (nnz > 0 ? nnz : 1), "csr col")) ||
+          (rc = dalloc(ctx, (void**)&val, sizeof(float) * (nnz > 0 ? nnz : 1), "csr val")))
+        return fail(rc);
+      LNE_CUDA_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(unsigned long long) * n, st));
+      cudaEventRecord(ev.e[1], st);
+    }
+    for (uint32_t q = 0; q < Q; ++q) {
+      a.qbits = qbits;
+      a.qsel = q;
+      LNE_CUDA_TRY(cudaMemsetAsync(cnt + 1, 0, 24, st));
+      LNE_CUDA_TRY(cudaMemsetAsync(cnt + 6, 0, 8, st));
+      k_walk_counts<true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, 0, m_dir, a, keys, cnt + 1,
+                                                            buf_keys, ctx->d_flags, cnt + 6);
+      ++launches;
+      unsigned long long got = 0;
+      int fl[kFlagWords];
+      LNE_CUDA_TRY(cudaMemcpyAsync(&got, cnt + 1, 8, cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaStreamSynchronize(st));
+      if (got > buf_keys || fl[kFlagSortOverflow]) {
+        set_error("lne_sparsify: a hash-range round exceeded the sample buffer; raise the batch "
+                  "(lne_ctx_set_sparsify_batch)");
+        return fail(LNE_ERR_UNSUPPORTED);
+      }
+      if (got == 0) continue;
+      int sbits = 0;
+      while (sbits < kSliceBitsMax && (got >> sbits) > (uint64_t)slots_max / 4) ++sbits;
+      if ((got >> sbits) > (uint64_t)slots_max * 5 / 8) {
+        set_error("lne_sparsify: a hash-range round has more samples than its slices hold; lower the batch");
+        return fail(LNE_ERR_UNSUPPORTED);
+      }
+      unsigned long long* hk = keys;
+      if ((rc = partition_by_top_bits(ctx, keys, keys2, (int64_t)got, sbits, &hk, &launches))) return fail(rc);
+      const int64_t nslices = (int64_t)1 << sbits;
+      k_slice_bounds<<<grid_for((int64_t)got + 1, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(hk, (int64_t)got,
+                                                                                                  sbits, nslices,
+                                                                                                  starts);
+      const unsigned sgrid = (unsigned)std::min<int64_t>(nslices, 2 * (int64_t)ctx->num_sms);
+      k_slice_count<<<sgrid, kSliceThreads, slice_smem, st>>>(hk, starts, nslices, slots_max, uniq, cnt + 2, cnt + 3,
+                                                              ctx->d_flags, qbits);
+      launches += 2;
+      unsigned long long sc[2] = {0, 0};  // distinct, counted
+      LNE_CUDA_TRY(cudaMemcpyAsync(sc, cnt + 2, sizeof(sc), cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
+      LNE_CUDA_TRY(cudaStreamSynchronize(st));
+      if (fl[kFlagSliceOverflow]) {
+        set_error("lne_sparsify: a slice of a hash-range round overflowed its shared table; lower the batch");
+        return fail(LNE_ERR_UNSUPPORTED);
+      }
+      if (sweep == 0) {
+        distinct += sc[0];
+        counted += sc[1];
+      }
+      const unsigned tg = (unsigned)std::min<int64_t>(((int64_t)sc[0] + 255) / 256, (int64_t)tgrid_cap);
+      if (sc[0] > 0) {
+        if (sweep == 0)
+          k_trunclog_rows<false><<<tg, 256, 0, st>>>(uniq, sc[0], g->vdata, factor, p->upper,
+                                                     (const LogTable*)ctx->log_table, rowcnt, cnt + 4, nullptr,
+                                                     nullptr, nullptr, ctx->d_flags);
+        else
+          k_trunclog_rows<true><<<tg, 256, 0, st>>>(uniq, sc[0], g->vdata, factor, p->upper,
+                                                    (const LogTable*)ctx->log_table, rowcnt, cnt + 5, row_ptr, col,
+                                                    val, ctx->d_flags);
+        ++launches;
+      }
+    }
+  }
+  cudaEventRecord(ev.e[2], st);
+  unsigned long long kept = 0;
+  LNE_CUDA_TRY(cudaMemcpyAsync(&kept, cnt + 4, 8, cudaMemcpyDeviceToHost, st));
+  {
+    int fl[kFlagWords];
+    LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (fl[kFlagSortOverflow]) {
+      set_error("lne_sparsify: the rounds' second sweep kept other entries than the first (internal error)");
+      return fail(LNE_ERR_UNSUPPORTED);
+    }
+  }
+  // sort every row by column; rows longer than the shared-memory sort go
+  // through the radix sort
+  uint32_t* big = nullptr;
+  if ((rc = S.get((void**)&big, sizeof(uint32_t) * (n > 0 ? n : 1), "big rows"))) return fail(rc);
+  LNE_CUDA_TRY(cudaMemsetAsync(cnt + 5, 0, 8, st));
+  const int maxlen = ctx->sparsify_row_sort_max;
+  LNE_CUDA_TRY(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(unsigned long long) * maxlen)));
+  k_row_sort<<<(unsigned)std::min<int64_t>(n, (int64_t)ctx->num_sms * 8), 256, sizeof(unsigned long long) * maxlen,
+               st>>>(row_ptr, n, col, val, maxlen, big, cnt + 5);
+  ++launches;
+  unsigned long long nbig = 0;
+  LNE_CUDA_TRY(cudaMemcpyAsync(&nbig, cnt + 5, 8, cudaMemcpyDeviceToHost, st));
+  LNE_CUDA_TRY(cudaStreamSynchronize(st));
+  LNE_CUDA_TRY(cudaGetLastError());
+  if (nbig > 0) {
+    std::vector<uint32_t> hb(nbig);
+    std::vector<int64_t> hp(n + 1);
+    LNE_CUDA_TRY(cudaMemcpyAsync(hb.data(), big, sizeof(uint32_t) * nbig, cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaMemcpyAsync(hp.data(), row_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    std::sort(hb.begin(), hb.end());
+    std::vector<int64_t> bpref(nbig + 1, 0);
+    for (uint64_t b = 0; b < nbig; ++b) bpref[b + 1] = bpref[b] + (hp[hb[b] + 1] - hp[hb[b]]);
+    const int64_t nb_items = bpref[nbig];
+    int64_t* d_bpref = nullptr;
+    unsigned long long *bk = nullptr, *bk2 = nullptr;
+    uint32_t *bv = nullptr, *bv2 = nullptr;
+    int32_t* scol = nullptr;
+    float* sval = nullptr;
+    if ((rc = S.get((void**)&d_bpref, sizeof(int64_t) * (nbig + 1), "big row offsets")) ||
+        (rc = S.get((void**)&bk, sizeof(unsigned long long) * nb_items, "big row keys")) ||
+        (rc = S.get((void**)&bk2, sizeof(unsigned long long) * nb_items, "big row keys (sort)")) ||
+        (rc = S.get((void**)&bv, sizeof(uint32_t) * nb_items, "big row values")) ||
+        (rc = S.get((void**)&bv2, sizeof(uint32_t) * nb_items, "big row values (sort)")) ||
+        (rc = S.get((void**)&scol, sizeof(int32_t) * nb_items, "big row columns (sorted)")) ||
+        (rc = S.get((void**)&sval, sizeof(float) * nb_items, "big row values (sorted)")))
+      return fail(rc);
+    LNE_CUDA_TRY(cudaMemcpyAsync(big, hb.data(), sizeof(uint32_t) * nbig, cudaMemcpyHostToDevice, st));
+    LNE_CUDA_TRY(cudaMemcpyAsync(d_bpref, bpref.data(), sizeof(int64_t) * (nbig + 1), cudaMemcpyHostToDevice, st));
+    const unsigned bg = (unsigned)std::min<uint64_t>(nbig, (uint64_t)ctx->num_sms * 8);
+    k_big_rows<true><<<bg, 256, 0, st>>>(big, d_bpref, (int64_t)nbig, row_ptr, col, val, bk, bv, nullptr, nullptr);
+    int kbits = 32;
+    while (kbits < 64 && ((uint64_t)1 << (kbits - 32)) < nbig) ++kbits;
+    if ((rc = radix_sort_pairs_to_csr(ctx, bk, bv, bk2, bv2, nb_items, kbits, 0xffffffffULL, scol, sval, &launches)))
+      return fail(rc);
+    k_big_rows<false><<<bg, 256, 0, st>>>(big, d_bpref, (int64_t)nbig, row_ptr, col, val, nullptr, nullptr, scol,
+                                          sval);
+    launches += 2;
+  }
+  cudaEventRecord(ev.e[3], st);
+  LNE_CUDA_TRY(cudaEventSynchronize(ev.e[3]));
+  cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) {
+    set_error(std::string("lne_sparsify: kernel launch failed: ") + cudaGetErrorString(le));
+    return fail(LNE_ERR_CUDA);
+  }
+  if (stats) {
+    stats->logn = logn;
+    stats->total_samples = M;
+    stats->inv_lambda = inv_lambda;
+    stats->frac = frac;
+    stats->factor = factor;
+    stats->m_exact = M_exact;
+    stats->exp_rv_rounded = (int64_t)exp_rv;
+    stats->table_size = (int64_t)table_size;
+    stats->capacity = (int64_t)cap;
+    stats->samples_emitted = (int64_t)total;
+    stats->distinct = (int64_t)distinct;
+    stats->nnz_upper = (int64_t)kept;
+    stats->nnz = nnz;
+    cudaEventElapsedTime(&stats->ms_sample, ev.e[0], ev.e[1]);
+    cudaEventElapsedTime(&stats->ms_trunclog, ev.e[1], ev.e[2]);
+    cudaEventElapsedTime(&stats->ms_csr, ev.e[2], ev.e[3]);
+    stats->kernel_launches = launches;
+    stats->sliced = 2;
+  }
+  ctx->launch_count += launches;
+  lne_csr* c = new lne_csr();
+  c->n = n;
+  c->nnz = nnz;
+  c->row_ptr = row_ptr;
+  c->col = col;
+  c->val = val;
+  c->stream = st;
+  *out = c;
+  return LNE_OK;
+}
+
 extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_params* p, lne_csr** out,
                             lne_sparsify_stats* stats) {
   LNE_CHECK_ARG(ctx && g && p && out, "lne_sparsify: NULL argument");
@@ -893,6 +1371,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   Slot* table = nullptr;  // the pair table in HBM (allocated and cleared on first use)
   Slot* uniq = nullptr;   // sliced aggregation: the distinct pairs with their counts
   unsigned long long* counters = nullptr;  // [0] emitted [1] count sum [2] distinct [3] kept [4] items
+                                           // [6] next edge of the sampler's persistent grid
   double* wsum = nullptr;
   int rc;
   const int sum_blocks = 1024;
@@ -910,6 +1389,8 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   a.logn = logn;
   a.mask = cap - 1;
   a.use_frac = frac > 0.0000000001 ? 1 : 0;
+  a.qbits = 0;
+  a.qsel = 0;
 
   cudaEventRecord(ev.e[0], st);
   // Sample buffer: at most exp_rv + 1 samples per directed entry; the edge
@@ -919,6 +1400,21 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   const uint64_t max_keys = (uint64_t)ctx->sparsify_batch_keys;  // default 2^30: 8 GiB of keys per batch
   const uint64_t buf_keys = want_keys < max_keys ? want_keys : max_keys;
   const int64_t edges_per_batch = (int64_t)std::max<uint64_t>(1, buf_keys / per_edge);
+  // Above one batch, counts take the hash-range rounds when the pair table
+  // and a batch's buffers do not fit in free device memory (or when forced).
+  if (!p->sample && want_keys > max_keys && ctx->sparsify_rounds >= 0 && ctx->sparsify_slice_slots > 0) {
+    bool rounds = ctx->sparsify_rounds == 1;
+    if (!rounds) {
+      size_t fr = 0, tot = 0;
+      LNE_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+      rounds = (double)cap * sizeof(Slot) + 2.0 * sizeof(unsigned long long) * (double)buf_keys > (double)fr;
+    }
+    if (rounds) {
+      S.release(counters);
+      return sparsify_rounds(ctx, g, p, a, cap, buf_keys, logn, M, inv_lambda, frac, exp_rv, table_size, out,
+                             stats);
+    }
+  }
   unsigned long long* keys = nullptr;
   unsigned long long* keys2 = nullptr;  // counts: the batch reordered by slice
   double* wts = nullptr;
@@ -957,9 +1453,11 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   bool sliced = false;
   unsigned long long emitted_total = 0;
   if (sliced_try) {
-    const unsigned wblocks = (unsigned)((m_dir + kWalkThreads - 1) / kWalkThreads);
+    const unsigned wblocks = (unsigned)std::min<int64_t>((m_dir + kWalkThreads - 1) / kWalkThreads,
+                                                         (int64_t)ctx->num_sms * 6);
+    LNE_CUDA_TRY(cudaMemsetAsync(counters + 6, 0, 8, st));
     k_walk_counts<true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, 0, m_dir, a, keys, counters,
-                                                          buf_keys, ctx->d_flags);
+                                                          buf_keys, ctx->d_flags, counters + 6);
     ++launches_sample;
     unsigned long long got = 0;
     LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));
@@ -987,7 +1485,7 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
       LNE_CUDA_TRY(cudaFuncSetAttribute(k_slice_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)slice_smem));
       const unsigned sgrid = (unsigned)std::min<int64_t>(nslices, 2 * (int64_t)ctx->num_sms);
       k_slice_count<<<sgrid, kSliceThreads, slice_smem, st>>>(hk, starts, nslices, slots_max, uniq, counters + 2,
-                                                              counters + 1, ctx->d_flags);
+                                                              counters + 1, ctx->d_flags, 0);
       launches_sample += 2;
       unsigned long long sc[2] = {0, 0};  // samples counted, distinct pairs
       int fl[kFlagWords];
@@ -1020,13 +1518,15 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     for (int64_t eb = 0; eb < m_dir; eb += edges_per_batch) {
       const int64_t ee = std::min<int64_t>(m_dir, eb + edges_per_batch);
       LNE_CUDA_TRY(cudaMemsetAsync(counters, 0, 8, st));
+      LNE_CUDA_TRY(cudaMemsetAsync(counters + 6, 0, 8, st));
       const unsigned wblocks = (unsigned)((ee - eb + kWalkThreads - 1) / kWalkThreads);
       if (p->sample)
         k_walk<true><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, wts,
                                                               counters, buf_keys, ctx->d_flags);
       else
-        k_walk_counts<false><<<wblocks, kWalkThreads, 0, st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, counters,
-                                                               buf_keys, ctx->d_flags);
+        k_walk_counts<false><<<(unsigned)std::min<int64_t>(wblocks, (int64_t)ctx->num_sms * 6), kWalkThreads, 0,
+                               st>>>(g->vdata, g->nbrs, g->src, eb, ee, a, keys, counters, buf_keys, ctx->d_flags,
+                                     counters + 6);
       ++launches_sample;
       unsigned long long got = 0;
       LNE_CUDA_TRY(cudaMemcpyAsync(&got, counters, 8, cudaMemcpyDeviceToHost, st));

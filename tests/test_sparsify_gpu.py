@@ -117,6 +117,25 @@ def test_device_matches_oracle_config1(ctx):
     assert_csr_equal(got2, ref)
 
 
+def test_device_matches_oracle_config2(ctx):
+    """Config 2 at full size: Chung-Lu n=1,138,499, m=2,990,443, T=10,
+    samples = 100 * m (ratio 1.883551 as a float): 299M samples, 351M CSR
+    entries, bit for bit against the port (about half a minute of host
+    time on 16 cores)."""
+    off, nbrs = graphs.chung_lu(1138499, 2990443, 2.1, seed=2)
+    ratio = float(np.float32(1.883551))
+    prm = dict(seed=2, walk_len=10, tablesz=200_000_000, negative=1, sample=0, sample_ratio=ratio, mem_ratio=1.0,
+               upper=0)
+    got, st = device_sparsify(ctx, off, nbrs, prm)
+    assert st["sliced"] == 1
+    assert st["nnz"] == 350_893_437
+    ref, pst = port.sparsify(off, nbrs, 2, walk_len=10, tablesz=200_000_000, sample_ratio=ratio)
+    assert st["samples_emitted"] == pst["samples"] == 299_044_249
+    assert st["distinct"] == pst["distinct"]
+    assert st["m_exact"] == pst["M_exact"] and st["factor"] == pst["factor"]
+    assert_csr_equal(got, ref)
+
+
 def test_device_matches_oracle_midsize_variants(ctx):
     off, nbrs = graphs.chung_lu(5000, 40000, 2.1, seed=9)
     for prm in [dict(seed=77, walk_len=5, tablesz=2_000_000, negative=3, sample=0, sample_ratio=0.8,
@@ -167,6 +186,49 @@ def test_batched_samples_match_reference_golden(ctx):
         ctx.set_sparsify_batch(0)
 
 
+def test_rounds_match_reference_golden(ctx):
+    """The hash-range rounds (the counts path above one batch when the pair
+    table does not fit), forced with 4096-sample batches, so that a case
+    runs up to hundreds of rounds; rows above 64 entries go through the radix
+    sort instead of the shared-memory sort.  The CSR is the reference's."""
+    ctx.set_sparsify_batch(4096)
+    ctx.set_sparsify_rounds(1, 64)
+    try:
+        for path in CASES:
+            z = np.load(path)
+            prm = json.loads(str(z["params"]))
+            if prm["sample"] != 0:
+                continue
+            got, st = device_sparsify(ctx, z["offsets"], z["nbrs"], prm)
+            assert_csr_equal(got, (z["row_ptr"], z["col"], z["val"]))
+            if st["samples_emitted"] > 4096:
+                assert st["sliced"] == 2, path
+    finally:
+        ctx.set_sparsify_rounds()
+        ctx.set_sparsify_batch(0)
+
+
+def test_rounds_match_oracle_config1(ctx):
+    """Config 1 (26.75M entries) through 32 rounds of 2^22-sample batches,
+    against the port."""
+    off, nbrs = graphs.chung_lu(10312, 333983, 2.1, seed=1)
+    ratio = float(np.float32(70.095396))
+    prm = dict(seed=1, walk_len=10, tablesz=13_500_000, negative=1, sample=0, sample_ratio=ratio, mem_ratio=1.0,
+               upper=0)
+    ctx.set_sparsify_batch(1 << 22)
+    ctx.set_sparsify_rounds(1, 0)
+    try:
+        got, st = device_sparsify(ctx, off, nbrs, prm)
+    finally:
+        ctx.set_sparsify_rounds()
+        ctx.set_sparsify_batch(0)
+    assert st["sliced"] == 2
+    ref, pst = port.sparsify(off, nbrs, 1, walk_len=10, tablesz=13_500_000, sample_ratio=ratio)
+    assert st["samples_emitted"] == pst["samples"] and st["distinct"] == pst["distinct"]
+    assert st["m_exact"] == pst["M_exact"] and st["factor"] == pst["factor"]
+    assert_csr_equal(got, ref)
+
+
 def test_device_is_deterministic(ctx):
     off, nbrs = graphs.chung_lu(3000, 30000, 2.1, seed=4)
     prm = dict(seed=5, walk_len=10, tablesz=2_000_000, negative=1, sample=0, sample_ratio=1.0, mem_ratio=1.0,
@@ -187,6 +249,17 @@ def test_table_full_is_a_status_and_context_survives(ctx):
     prm.update(tablesz=2_000_000, mem_ratio=1.0)
     got, _ = device_sparsify(ctx, off, nbrs, prm)
     assert got[0][-1] > 0
+    # the rounds path reports the same status
+    prm.update(tablesz=1000, mem_ratio=0.0)
+    ctx.set_sparsify_batch(4096)
+    ctx.set_sparsify_rounds(1, 0)
+    try:
+        with pytest.raises(LneError) as ei:
+            device_sparsify(ctx, off, nbrs, prm)
+        assert ei.value.status == LNE_ERR_TABLE_FULL
+    finally:
+        ctx.set_sparsify_rounds()
+        ctx.set_sparsify_batch(0)
 
 
 def test_invalid_graph_rejected(ctx):
