@@ -99,9 +99,16 @@ int lne_ctx_set_sparsify_batch(lne_ctx* ctx, int64_t keys);
  * where the pair table path needs the table and twice the CSR's entries.
  * mode 0 (the default): rounds when the pair table and a batch do not fit
  * in free device memory; 1: always; -1: never.  row_sort_max (a power of
- * two up to 8192; 0: 8192): rows with more entries are sorted by the radix
- * sort instead of in shared memory.  The output is the same either way. */
+ * two in [32, 1024]; 0: 1024): the rounds' rows with at most that many
+ * entries are sorted by column by one warp, longer rows by a thread block
+ * through a bitmap of the column range.  The output is the same either
+ * way. */
 int lne_ctx_set_sparsify_rounds(lne_ctx* ctx, int32_t mode, int32_t row_sort_max);
+/* Columns per window of the bitmap row sort of the hash-range rounds (no
+ * reference counterpart): a multiple of 2048, or 0 (the default) for as
+ * many as shared memory holds (1,310,720); a row is swept once per window
+ * of the column range.  The output is the same either way. */
+int lne_ctx_set_row_sort_window(lne_ctx* ctx, int64_t cols);
 /* Wait for all work queued on the context's stream. */
 int lne_ctx_synchronize(lne_ctx* ctx);
 /* Kernels the pipeline entry points (lne_sparsify, lne_randsvd,

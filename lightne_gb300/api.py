@@ -54,9 +54,16 @@ class Context:
 
     def set_sparsify_rounds(self, mode: int = 0, row_sort_max: int = 0) -> None:
         """Hash-range rounds above one batch of samples (counts): 0 when the
-        pair table does not fit, 1 always, -1 never; rows longer than
-        row_sort_max (0: 8192) are sorted by the radix sort."""
+        pair table does not fit, 1 always, -1 never.  The rounds' CSR rows of
+        at most row_sort_max entries (a power of two in [32, 1024]; 0: 1024)
+        are sorted by one warp, longer rows through a bitmap of the column
+        range."""
         check(_lib.load().lne_ctx_set_sparsify_rounds(self.handle, mode, row_sort_max))
+
+    def set_row_sort_window(self, cols: int = 0) -> None:
+        """Columns per window of the rounds' bitmap row sort (a multiple of
+        2048; 0: as many as shared memory holds)."""
+        check(_lib.load().lne_ctx_set_row_sort_window(self.handle, cols))
 
     def close(self) -> None:
         if self.handle:

@@ -281,11 +281,18 @@ int lne_ctx_synchronize(lne_ctx* ctx) {
 
 int lne_ctx_set_sparsify_rounds(lne_ctx* ctx, int32_t mode, int32_t row_sort_max) {
   LNE_CHECK_ARG(ctx != nullptr && mode >= -1 && mode <= 1, "lne_ctx_set_sparsify_rounds: bad argument");
-  LNE_CHECK_ARG(row_sort_max == 0 || (row_sort_max >= 2 && row_sort_max <= 8192 &&
+  LNE_CHECK_ARG(row_sort_max == 0 || (row_sort_max >= 32 && row_sort_max <= 1024 &&
                                       (row_sort_max & (row_sort_max - 1)) == 0),
-                "lne_ctx_set_sparsify_rounds: row_sort_max must be 0 or a power of two in [2, 8192]");
+                "lne_ctx_set_sparsify_rounds: row_sort_max must be 0 or a power of two in [32, 1024]");
   ctx->sparsify_rounds = mode;
-  ctx->sparsify_row_sort_max = row_sort_max ? row_sort_max : 8192;
+  ctx->row_sort_warp_max = row_sort_max ? row_sort_max : 1024;
+  return LNE_OK;
+}
+
+int lne_ctx_set_row_sort_window(lne_ctx* ctx, int64_t cols) {
+  LNE_CHECK_ARG(ctx != nullptr && cols >= 0 && cols % 2048 == 0,
+                "lne_ctx_set_row_sort_window: cols must be 0 or a positive multiple of 2048");
+  ctx->row_sort_window_cols = cols;
   return LNE_OK;
 }
 

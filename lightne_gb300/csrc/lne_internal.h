@@ -70,10 +70,14 @@ struct lne_ctx {
   // samples per batch of the sparsifier's sample buffer (8 B each)
   int64_t sparsify_batch_keys = (int64_t)1 << 30;
   // hash-range rounds above one batch (counts): 0 when the pair table does
-  // not fit, 1 always, -1 never; rows longer than row_sort_max (a power of
-  // two) are sorted by the radix sort instead of in shared memory
+  // not fit, 1 always, -1 never
   int sparsify_rounds = 0;
-  int sparsify_row_sort_max = 8192;
+  // row sort of the rounds' CSR: rows of at most row_sort_warp_max entries
+  // (a power of two in [32, 1024]) are sorted by one warp in registers,
+  // longer rows through a shared-memory bitmap of row_sort_window_cols
+  // columns at a time (0: as many as shared memory holds)
+  int row_sort_warp_max = 1024;
+  int64_t row_sort_window_cols = 0;
   // kernels launched by the entry points that ran on this context (each
   // adds its own count when it returns successfully)
   int64_t launch_count = 0;

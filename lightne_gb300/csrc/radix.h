@@ -1,4 +1,5 @@
-// Device radix sort used by the CSR build of the sparsifier.
+// Device sorts of the sparsifier: the radix sort and partitions of its
+// samples, and the row sort of the hash-range rounds' CSR.
 #pragma once
 #include <stdint.h>
 
@@ -27,5 +28,16 @@ int partition_by_slot(lne_ctx* ctx, const unsigned long long* keys, unsigned lon
 // buffer that holds the sorted words.
 int partition_by_top_bits(lne_ctx* ctx, unsigned long long* keys, unsigned long long* tmp, int64_t count,
                           int top_bits, unsigned long long** result, int* launches);
+
+// Sorts every row of a CSR by column: row r's entries are
+// (scol, sval)[row_ptr[r] .. row_ptr[r + 1]) in any order, with distinct
+// columns in [0, ncols); they are written in column order at the same
+// positions of (dcol, dval).  scol == dcol and sval == dval sort in place.
+// Rows of at most ctx->row_sort_warp_max entries are sorted by one warp in
+// registers, longer ones by a thread block through a shared-memory bitmap of
+// the column range.  A repeated or out-of-range column sets
+// kFlagSortOverflow.  Defined in csr_rows.cu.
+int sort_csr_rows(lne_ctx* ctx, const int64_t* row_ptr, int64_t n, int64_t ncols, const int32_t* scol,
+                  const float* sval, int32_t* dcol, float* dval, int* launches);
 
 }  // namespace lne

@@ -15,7 +15,7 @@
 //   row_ptr i64[n+1]             exclusive scan of rowcnt (the output row_ptr)
 //   items   u64[nnz] + u32[nnz]  (row << cbits | col, float bits) per CSR entry,
 //                                twice (ping-pong buffers of the radix sort)
-//   col/val i32[nnz], f32[nnz]   output CSR
+//   col/val i32[nnz], f32[nnz]   output CSR (every row sorted by column)
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -1030,74 +1030,6 @@ __global__ void __launch_bounds__(256) k_trunclog_rows(const Slot* __restrict__ 
   if ((threadIdx.x & 31) == 0 && kept) atomicAdd(kept_total, kept);
 }
 
-// Sorts every row of at most maxlen entries (a power of two) by column in
-// shared memory (bitonic, on (col << 32 | value bits): columns are distinct
-// within a row); longer rows are listed in big (count in *nbig).
-__global__ void __launch_bounds__(256) k_row_sort(const int64_t* __restrict__ row_ptr, int64_t n,
-                                                  int32_t* __restrict__ col, float* __restrict__ val, int maxlen,
-                                                  uint32_t* __restrict__ big, unsigned long long* __restrict__ nbig) {
-  extern __shared__ unsigned long long rs_key[];
-  for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
-    const int64_t a = row_ptr[r];
-    const int64_t len = row_ptr[r + 1] - a;
-    if (len <= 1) continue;  // the whole block
-    if (len > maxlen) {
-      if (threadIdx.x == 0) big[atomicAdd(nbig, 1ULL)] = (uint32_t)r;
-      continue;
-    }
-    int P = 2;
-    while (P < len) P <<= 1;
-    for (int i = threadIdx.x; i < P; i += blockDim.x)
-      rs_key[i] = i < len ? (((unsigned long long)(uint32_t)col[a + i] << 32) | __float_as_uint(val[a + i]))
-                          : ~0ULL;
-    __syncthreads();
-    for (int k = 2; k <= P; k <<= 1)
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int i = threadIdx.x; i < P; i += blockDim.x) {
-          const int ixj = i ^ j;
-          if (ixj > i) {
-            const unsigned long long x = rs_key[i], y = rs_key[ixj];
-            const bool up = (i & k) == 0;
-            if ((x > y) == up) {
-              rs_key[i] = y;
-              rs_key[ixj] = x;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
-      const unsigned long long x = rs_key[i];
-      col[a + i] = (int32_t)(x >> 32);
-      val[a + i] = __uint_as_float((uint32_t)x);
-    }
-    __syncthreads();
-  }
-}
-
-// The rows longer than the shared-memory sort: their entries as
-// ((big index) << 32 | col, value bits), in big-row order (GATHER), or the
-// sorted columns and values written back into their rows.
-template <bool GATHER>
-__global__ void k_big_rows(const uint32_t* __restrict__ big, const int64_t* __restrict__ bpref, int64_t nbig,
-                           const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col, float* __restrict__ val,
-                           unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
-                           const int32_t* __restrict__ scol, const float* __restrict__ sval) {
-  for (int64_t b = blockIdx.x; b < nbig; b += gridDim.x) {
-    const int64_t a = row_ptr[big[b]];
-    const int64_t o = bpref[b], len = bpref[b + 1] - bpref[b];
-    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
-      if (GATHER) {
-        keys[o + i] = ((unsigned long long)b << 32) | (uint32_t)col[a + i];
-        vals[o + i] = __float_as_uint(val[a + i]);
-      } else {
-        col[a + i] = scol[o + i];
-        val[a + i] = sval[o + i];
-      }
-    }
-  }
-}
-
 // The rounds path (see above).  Fills *out and stats like lne_sparsify.
 static int sparsify_rounds(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_params* p, SampleArgs a,
                            uint64_t cap, uint64_t buf_keys, double logn, double M, double inv_lambda, double frac,
@@ -1252,62 +1184,23 @@ static int sparsify_rounds(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_
       return fail(LNE_ERR_UNSUPPORTED);
     }
   }
-  // sort every row by column; rows longer than the shared-memory sort go
-  // through the radix sort
-  uint32_t* big = nullptr;
-  if ((rc = S.get((void**)&big, sizeof(uint32_t) * (n > 0 ? n : 1), "big rows"))) return fail(rc);
-  LNE_CUDA_TRY(cudaMemsetAsync(cnt + 5, 0, 8, st));
-  const int maxlen = ctx->sparsify_row_sort_max;
-  LNE_CUDA_TRY(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(sizeof(unsigned long long) * maxlen)));
-  k_row_sort<<<(unsigned)std::min<int64_t>(n, (int64_t)ctx->num_sms * 8), 256, sizeof(unsigned long long) * maxlen,
-               st>>>(row_ptr, n, col, val, maxlen, big, cnt + 5);
-  ++launches;
-  unsigned long long nbig = 0;
-  LNE_CUDA_TRY(cudaMemcpyAsync(&nbig, cnt + 5, 8, cudaMemcpyDeviceToHost, st));
-  LNE_CUDA_TRY(cudaStreamSynchronize(st));
-  LNE_CUDA_TRY(cudaGetLastError());
-  if (nbig > 0) {
-    std::vector<uint32_t> hb(nbig);
-    std::vector<int64_t> hp(n + 1);
-    LNE_CUDA_TRY(cudaMemcpyAsync(hb.data(), big, sizeof(uint32_t) * nbig, cudaMemcpyDeviceToHost, st));
-    LNE_CUDA_TRY(cudaMemcpyAsync(hp.data(), row_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st));
-    LNE_CUDA_TRY(cudaStreamSynchronize(st));
-    std::sort(hb.begin(), hb.end());
-    std::vector<int64_t> bpref(nbig + 1, 0);
-    for (uint64_t b = 0; b < nbig; ++b) bpref[b + 1] = bpref[b] + (hp[hb[b] + 1] - hp[hb[b]]);
-    const int64_t nb_items = bpref[nbig];
-    int64_t* d_bpref = nullptr;
-    unsigned long long *bk = nullptr, *bk2 = nullptr;
-    uint32_t *bv = nullptr, *bv2 = nullptr;
-    int32_t* scol = nullptr;
-    float* sval = nullptr;
-    if ((rc = S.get((void**)&d_bpref, sizeof(int64_t) * (nbig + 1), "big row offsets")) ||
-        (rc = S.get((void**)&bk, sizeof(unsigned long long) * nb_items, "big row keys")) ||
-        (rc = S.get((void**)&bk2, sizeof(unsigned long long) * nb_items, "big row keys (sort)")) ||
-        (rc = S.get((void**)&bv, sizeof(uint32_t) * nb_items, "big row values")) ||
-        (rc = S.get((void**)&bv2, sizeof(uint32_t) * nb_items, "big row values (sort)")) ||
-        (rc = S.get((void**)&scol, sizeof(int32_t) * nb_items, "big row columns (sorted)")) ||
-        (rc = S.get((void**)&sval, sizeof(float) * nb_items, "big row values (sorted)")))
-      return fail(rc);
-    LNE_CUDA_TRY(cudaMemcpyAsync(big, hb.data(), sizeof(uint32_t) * nbig, cudaMemcpyHostToDevice, st));
-    LNE_CUDA_TRY(cudaMemcpyAsync(d_bpref, bpref.data(), sizeof(int64_t) * (nbig + 1), cudaMemcpyHostToDevice, st));
-    const unsigned bg = (unsigned)std::min<uint64_t>(nbig, (uint64_t)ctx->num_sms * 8);
-    k_big_rows<true><<<bg, 256, 0, st>>>(big, d_bpref, (int64_t)nbig, row_ptr, col, val, bk, bv, nullptr, nullptr);
-    int kbits = 32;
-    while (kbits < 64 && ((uint64_t)1 << (kbits - 32)) < nbig) ++kbits;
-    if ((rc = radix_sort_pairs_to_csr(ctx, bk, bv, bk2, bv2, nb_items, kbits, 0xffffffffULL, scol, sval, &launches)))
-      return fail(rc);
-    k_big_rows<false><<<bg, 256, 0, st>>>(big, d_bpref, (int64_t)nbig, row_ptr, col, val, nullptr, nullptr, scol,
-                                          sval);
-    launches += 2;
-  }
+  // sort every row by column, in place
+  if ((rc = sort_csr_rows(ctx, row_ptr, n, n, col, val, col, val, &launches))) return fail(rc);
   cudaEventRecord(ev.e[3], st);
   LNE_CUDA_TRY(cudaEventSynchronize(ev.e[3]));
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) {
     set_error(std::string("lne_sparsify: kernel launch failed: ") + cudaGetErrorString(le));
     return fail(LNE_ERR_CUDA);
+  }
+  {
+    int fl[kFlagWords];
+    LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (fl[kFlagSortOverflow]) {
+      set_error("lne_sparsify: CSR entries do not match their rows (internal error)");
+      return fail(LNE_ERR_UNSUPPORTED);
+    }
   }
   if (stats) {
     stats->logn = logn;
@@ -1637,6 +1530,10 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   S.release(scan_tmp);
 
   // Sort the items by (row, col) and write the CSR columns and values.
+  // (Placing the items into their rows at atomic cursors and sorting each
+  // row, as the hash-range rounds do, measured slower here: the cursor
+  // atomics and scattered 4-byte writes ran at ~29G entries/s, and the
+  // per-row sorts cost more than the radix passes they replace.)
   int32_t* col = nullptr;
   float* val = nullptr;
   unsigned long long* tkeys = nullptr;

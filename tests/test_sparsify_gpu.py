@@ -117,6 +117,49 @@ def test_device_matches_oracle_config1(ctx):
     assert_csr_equal(got2, ref)
 
 
+def test_row_sort_tiers_match_reference_golden(ctx):
+    """The hash-range rounds on every golden case with the rows of more than
+    32 entries sorted through the column bitmap, in windows of 2048 columns
+    (several windows where the graph has more vertices)."""
+    ctx.set_sparsify_batch(4096)
+    ctx.set_sparsify_rounds(1, 32)
+    ctx.set_row_sort_window(2048)
+    try:
+        for path in CASES:
+            z = np.load(path)
+            prm = json.loads(str(z["params"]))
+            if prm["sample"] != 0:
+                continue
+            got, _ = device_sparsify(ctx, z["offsets"], z["nbrs"], prm)
+            assert_csr_equal(got, (z["row_ptr"], z["col"], z["val"]))
+    finally:
+        ctx.set_sparsify_rounds()
+        ctx.set_row_sort_window()
+        ctx.set_sparsify_batch(0)
+
+
+def test_row_sort_windows_match_oracle_config1(ctx):
+    """Config 1 through the rounds (n = 10,312: six bitmap windows of 2048
+    columns; rows of more than 32 entries through the bitmap) against the
+    port."""
+    off, nbrs = graphs.chung_lu(10312, 333983, 2.1, seed=1)
+    ratio = float(np.float32(70.095396))
+    prm = dict(seed=1, walk_len=10, tablesz=13_500_000, negative=1, sample=0, sample_ratio=ratio, mem_ratio=1.0,
+               upper=0)
+    ctx.set_sparsify_batch(1 << 22)
+    ctx.set_sparsify_rounds(1, 32)
+    ctx.set_row_sort_window(2048)
+    try:
+        got, st = device_sparsify(ctx, off, nbrs, prm)
+    finally:
+        ctx.set_sparsify_rounds()
+        ctx.set_row_sort_window()
+        ctx.set_sparsify_batch(0)
+    assert st["sliced"] == 2
+    ref, _ = port.sparsify(off, nbrs, 1, walk_len=10, tablesz=13_500_000, sample_ratio=ratio)
+    assert_csr_equal(got, ref)
+
+
 def test_device_matches_oracle_config2(ctx):
     """Config 2 at full size: Chung-Lu n=1,138,499, m=2,990,443, T=10,
     samples = 100 * m (ratio 1.883551 as a float): 299M samples, 351M CSR
@@ -189,8 +232,8 @@ def test_batched_samples_match_reference_golden(ctx):
 def test_rounds_match_reference_golden(ctx):
     """The hash-range rounds (the counts path above one batch when the pair
     table does not fit), forced with 4096-sample batches, so that a case
-    runs up to hundreds of rounds; rows above 64 entries go through the radix
-    sort instead of the shared-memory sort.  The CSR is the reference's."""
+    runs up to hundreds of rounds; rows above 64 entries are sorted through
+    the column bitmap.  The CSR is the reference's."""
     ctx.set_sparsify_batch(4096)
     ctx.set_sparsify_rounds(1, 64)
     try:
