@@ -454,6 +454,7 @@ constexpr int kWsLoadWarp = 8;
 constexpr int kWsMmaWarp = 8 + kWsLoadWarps;
 constexpr int kWsMaxRing = 8;
 constexpr int kWsMaxCols = 256;  // two accumulators of up to 256 TMEM columns
+constexpr int kWsPrefetchTiles = 2;  // tiles of In prefetched into L2 ahead of the TMA ring
 
 struct WsShared {
   unsigned long long raw_full[kWsMaxRing], raw_empty[kWsMaxRing];
@@ -519,10 +520,23 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_tc_gemm_ws(const __grid_const
   int64_t last_commit = -1;  // MMA thread: slice of its last commit
 
   if (TMA && warp == kWsLoadWarp) {
-    // one thread: a 16 x 128 box (8 KB, 64-byte swizzle) per slice
+    // one thread: a 16 x 128 box (8 KB, 64-byte swizzle) per slice; at the
+    // start of each tile the boxes of the tile kWsPrefetchTiles on are
+    // prefetched into L2, so that the ring's loads wait on L2, not DRAM
     if (lane == 0) {
       for (int64_t g = 0; g < total; ++g) {
         const int s = (int)(g % ring);
+        if (g % nsl == 0) {
+          const int64_t pj = g / nsl + kWsPrefetchTiles;
+          if (pj < my_tiles) {
+            const int64_t ptile = blockIdx.x + pj * gridDim.x;
+            for (int q = 0; q < nsl; ++q) tc::tma_prefetch_2d(&tmap, q * kSlice, (int)(ptile * 128));
+          }
+          if (g == 0)  // the first tiles
+            for (int64_t j0 = 1; j0 < kWsPrefetchTiles && j0 < my_tiles; ++j0)
+              for (int q = 0; q < nsl; ++q)
+                tc::tma_prefetch_2d(&tmap, q * kSlice, (int)((blockIdx.x + j0 * gridDim.x) * 128));
+        }
         if (g >= ring &&
             !tc::mbar_wait(tc::smem_addr(&sh->raw_empty[s]), (uint32_t)((g / ring - 1) & 1), kWaitCycles, abortf)) {
           fail();
@@ -897,8 +911,9 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __
 // Warp-specialised form of the symmetric Gram (A = B, c1 = c2 <= 192), with
 // the slices, operand layout, MMAs, TMEM sets and 64-row drains of
 // k_tc_gram_stream<32, R>:
-//   warps 12-13 (load)   cp.async of raw 32-row slices into a ring of
-//                        `ring` slots; raw_full[s] completes when they land
+//   warp 12 lane 0 (load) one TMA box per raw 32-row slice into a ring of
+//                        `ring` slots (raw_full[s] completes when it lands),
+//                        with an L2 prefetch of the slice 8 on (warp 13 idles)
 //   warps 8-11 (split)   raw slot -> TF32 hi/lo operand stage (2 stages),
 //                        releases the raw slot, publishes the stage
 //   warp 14 lane 0 (MMA) D0 (and D1) MMAs of a slice into the TMEM set of
@@ -907,11 +922,14 @@ __global__ void __launch_bounds__(kSThreads, 1) k_tc_gram_stream(const float* __
 //   warps 0-7 (drain)    TMEM set -> FP32 registers (rounded to nearest),
 //                        release the set; the sums go to partial[b] at the end
 // Unlike the block-synchronous form (two block barriers per slice) the
-// stages overlap; both are bound by the MMA sequence itself, about 290 SM
-// cycles per 128 x 144 x 8 TF32 MMA, with the tensor pipe counted busy a
-// quarter of the time.  Every wait is bounded; a timeout
-// sets the context's numeric flag to 2, which ends every other wait within
-// 64 polls.
+// stages overlap.  Timed per slice on one CTA (n = 1.14M, 144 columns): with
+// cp.async loaders (two warps, 1,152 16-byte copies per slice) the loads
+// took about 3,000 of the 3,400 cycles per slice; the split takes ~1,400
+// and the 24 MMAs ~1,500, so the TMA box (one instruction per slice) took
+// the call from 0.51 to 0.35 ms.  The number of MMAs per K step hardly
+// matters (three, one or none: 0.515, 0.509, 0.491 ms before the TMA
+// loads).  Every wait is bounded; a timeout sets the context's numeric flag
+// to 2, which ends every other wait within 64 polls.
 constexpr int kGwsSL = 32;
 constexpr int kGwsGroup = kGroupRows / kGwsSL;  // slices per TMEM set fill
 constexpr int kGwsDrainWarps = 8;
@@ -919,6 +937,7 @@ constexpr int kGwsSplitWarp = 8, kGwsLoadWarp = 12, kGwsMmaWarp = 14;
 constexpr int kGwsThreads = 32 * 15;
 constexpr int kGwsChunks = 6;      // 16-column chunks per drain thread: sets up to 192 columns
 constexpr int kGwsMaxRing = 8;
+constexpr int kGwsPrefetch = 8;    // slices prefetched into L2 ahead of the TMA ring
 
 struct GwsShared {
   unsigned long long raw_full[kGwsMaxRing], raw_empty[kGwsMaxRing];
@@ -926,7 +945,8 @@ struct GwsShared {
   uint32_t tmem_base;
 };
 
-__global__ void __launch_bounds__(kGwsThreads, 1) k_tc_gram_ws(const float* __restrict__ A, int64_t lda, int c1,
+__global__ void __launch_bounds__(kGwsThreads, 1) k_tc_gram_ws(const __grid_constant__ CUtensorMap tmap,
+                                                              const float* __restrict__ A, int64_t lda, int c1,
                                                               int nmma, int ring, int64_t n, int64_t per,
                                                               float* __restrict__ partial, int* flags) {
   extern __shared__ __align__(1024) uint8_t stream_smem[];
@@ -952,7 +972,7 @@ __global__ void __launch_bounds__(kGwsThreads, 1) k_tc_gram_ws(const float* __re
 
   if (t == 0) {
     for (int s = 0; s < ring; ++s) {
-      tc::mbar_init(tc::smem_addr(&sh->raw_full[s]), 64);
+      tc::mbar_init(tc::smem_addr(&sh->raw_full[s]), 1);
       tc::mbar_init(tc::smem_addr(&sh->raw_empty[s]), 4);
     }
     for (int c = 0; c < 2; ++c) {
@@ -972,28 +992,27 @@ __global__ void __launch_bounds__(kGwsThreads, 1) k_tc_gram_ws(const float* __re
   auto fail = [&]() { atomicExch(abortf, 2); };
   bool ok = true;
 
-  if (warp >= kGwsLoadWarp && warp < kGwsMmaWarp) {
-    const int ll = t - 32 * kGwsLoadWarp;  // 0..63
-    const int qa = c1p >> 2;
-    for (int64_t g = 0; g < total; ++g) {
-      const int s = (int)(g % ring);
-      if (g >= ring &&
-          !tc::mbar_wait(tc::smem_addr(&sh->raw_empty[s]), (uint32_t)((g / ring - 1) & 1), kWaitCycles, abortf)) {
-        if (lane == 0) fail();
-        break;
+  if (warp == kGwsLoadWarp) {
+    // one thread: a TMA box of 32 rows x c1p columns per slice (rows past n
+    // and columns past c1 land as zeros), and an L2 prefetch of the slice
+    // kGwsPrefetch slices on, so that the ring's loads wait on L2
+    if (lane == 0) {
+      for (int64_t g = 0; g < total && g < kGwsPrefetch; ++g)
+        tc::tma_prefetch_2d(&tmap, 0, (int)((s0 + g) * kGwsSL));
+      for (int64_t g = 0; g < total; ++g) {
+        const int s = (int)(g % ring);
+        if (g + kGwsPrefetch < total) tc::tma_prefetch_2d(&tmap, 0, (int)((s0 + g + kGwsPrefetch) * kGwsSL));
+        if (g >= ring &&
+            !tc::mbar_wait(tc::smem_addr(&sh->raw_empty[s]), (uint32_t)((g / ring - 1) & 1), kWaitCycles, abortf)) {
+          fail();
+          break;
+        }
+        const uint32_t mb = tc::smem_addr(&sh->raw_full[s]);
+        tc::mbar_arrive_expect_tx(mb, raw_slot);
+        tc::tma_load_2d(tc::smem_addr(raw + (size_t)s * raw_slot), &tmap, 0, (int)((s0 + g) * kGwsSL), mb);
       }
-      const uint32_t dst0 = tc::smem_addr(raw + (size_t)s * raw_slot);
-      for (int idx = ll; idx < kGwsSL * qa; idx += 64) {
-        const int r = idx / qa, q = idx - r * qa;
-        const int64_t row = (s0 + g) * kGwsSL + r;
-        const int cb = c1 - 4 * q;
-        const uint32_t bytes = row < n ? (uint32_t)(cb >= 4 ? 16 : 4 * cb) : 0u;
-        tc::cp_async16(dst0 + (uint32_t)((r * c1p + 4 * q) * 4), bytes ? (const void*)(A + row * lda + 4 * q) : A,
-                       bytes);
-      }
-      tc::cp_async_mbar_arrive(tc::smem_addr(&sh->raw_full[s]));
     }
-    tc::cp_async_wait_all();
+    __syncwarp();
   } else if (warp >= kGwsSplitWarp && warp < kGwsLoadWarp) {
     const int ct = t - 32 * kGwsSplitWarp;  // 0..127
     for (int64_t g = 0; g < total; ++g) {
@@ -1207,6 +1226,22 @@ static bool tmap_rows16x128(CUtensorMap* m, const float* base, int64_t rows, int
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Tensor map of a row-major FP32 matrix (rows x cols, ld elements between
+// rows) read in boxes of box_rows full rows of box_cols columns (cols rounded
+// up to 4), without swizzle; what lies past the matrix reads as zeros.
+static bool tmap_row_slices(CUtensorMap* m, const float* base, int64_t rows, int cols, int64_t ld, int box_cols,
+                            int box_rows) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn || rows < 1 || cols < 1 || rows > 0x7fffffffLL || box_cols > 256 || (box_cols & 3)) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int tc_gemm_tall(lne_ctx* ctx, const float* In, int64_t ldi, int k, const float* W, int c2, int64_t n, float* Out,
                  int64_t ldo, Copy16 OutB) {
   if (n <= 0) return LNE_OK;
@@ -1291,7 +1326,10 @@ int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const floa
     const size_t fixed = gram_ws_smem(c1, 0);
     const int ring = ctx->smem_optin > fixed ? (int)std::min<size_t>(kGwsMaxRing, (ctx->smem_optin - fixed) / slot)
                                              : 0;
-    if (set_cols <= 32 * kGwsChunks && ring >= 2) {
+    CUtensorMap tmap;
+    memset(&tmap, 0, sizeof(tmap));
+    if (set_cols <= 32 * kGwsChunks && ring >= 2 &&
+        tmap_row_slices(&tmap, A, n, c1, lda, (c1 + 3) & ~3, kGwsSL)) {
       const int64_t nslices = (n + kGwsSL - 1) / kGwsSL;
       const int64_t want =
           std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(nslices, ctx->num_sms), max_blocks));
@@ -1306,7 +1344,7 @@ int tc_gram_stream(lne_ctx* ctx, const float* A, int64_t lda, int c1, const floa
       // the CTA allocates all 512 TMEM columns: one CTA per SM
       const size_t lsmem = std::max(gram_ws_smem(c1, ring), ctx->smem_optin / 2 + 1);
       cudaFuncSetAttribute(k_tc_gram_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);
-      k_tc_gram_ws<<<(unsigned)nb, kGwsThreads, lsmem, ctx->stream>>>(A, lda, c1, nmma, ring, n, per, partial,
+      k_tc_gram_ws<<<(unsigned)nb, kGwsThreads, lsmem, ctx->stream>>>(tmap, A, lda, c1, nmma, ring, n, per, partial,
                                                                       ctx->d_flags);
       const int64_t cnt = (int64_t)c1 * c2;
       k_gram_reduce_stream<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(partial, nb, c1, c2, 1, G);
