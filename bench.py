@@ -749,7 +749,8 @@ def run_scale(args, local):
     stream = torch.cuda.current_stream()
     ctx = Context(local, stream=stream.cuda_stream)
     g = Graph.from_numpy(ctx, off, nbrs)
-    out = {"workload": w["label"], "n": n, "m": m, "sample_ratio_float": ratio, "graph_gen_s": gen_s}
+    out = {"workload": w["label"], "n": n, "m": m, "sample_ratio_float": ratio, "graph_gen_s": gen_s,
+           "device_free_gb_before_sparsify": torch.cuda.mem_get_info()[0] / 1e9}
     sums = []
     csr = None
     for rep in range(2):

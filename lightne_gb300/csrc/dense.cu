@@ -1198,6 +1198,36 @@ __global__ void k_trace(const double* G, int r, double* out) {
   }
 }
 
+// ||G - I||_F in FP64 (one block; r x r row-major).
+__global__ void k_identity_distance(const double* __restrict__ G, int r, double* __restrict__ out) {
+  __shared__ double part[32];
+  double s = 0.0;
+  for (int64_t t = threadIdx.x; t < (int64_t)r * r; t += blockDim.x) {
+    const int64_t i = t / r, j = t - i * r;
+    const double e = G[t] - (i == j ? 1.0 : 0.0);
+    s = fma(e, e, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w];
+    *out = sqrt(tot);
+  }
+}
+
+int identity_distance_host(lne_ctx* ctx, const double* G, int r, double* out) {
+  double* d = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, (void**)&d, sizeof(double), "identity distance"))) return rc;
+  k_identity_distance<<<1, 256, 0, ctx->stream>>>(G, r, d);
+  LNE_CUDA_TRY(cudaMemcpyAsync(out, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  LNE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, d);
+  return LNE_OK;
+}
+
 int trace_host(lne_ctx* ctx, const double* G, int r, double* out) {
   double* d = nullptr;
   int rc;

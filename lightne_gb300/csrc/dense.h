@@ -79,5 +79,7 @@ int normalize_rows(lne_ctx* ctx, float* X, int64_t n, int d, int64_t ld, float e
 
 // Trace of a device FP64 r x r matrix, read back to the host (synchronises).
 int trace_host(lne_ctx* ctx, const double* G, int r, double* out);
+// ||G - I||_F of an r x r FP64 matrix, read back to the host (synchronises).
+int identity_distance_host(lne_ctx* ctx, const double* G, int r, double* out);
 
 }  // namespace lne

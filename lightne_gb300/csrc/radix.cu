@@ -337,8 +337,8 @@ int partition_by_top_bits(lne_ctx* ctx, unsigned long long* keys, unsigned long 
                           int top_bits, unsigned long long** result, int* launches) {
   *result = keys;
   if (count <= 0 || top_bits <= 0) return LNE_OK;
-  if (top_bits > 16) {
-    set_error("partition: at most 16 top bits");
+  if (top_bits > 24) {
+    set_error("partition: at most 24 top bits");
     return LNE_ERR_UNSUPPORTED;
   }
   const int passes = (top_bits + 7) / 8;

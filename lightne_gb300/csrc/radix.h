@@ -23,7 +23,7 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
 int partition_by_slot(lne_ctx* ctx, const unsigned long long* keys, unsigned long long* out, int64_t count,
                       int table_bits, int* launches);
 
-// Stable LSD sort of `count` words by their top `top_bits` bits (0..16; 0
+// Stable LSD sort of `count` words by their top `top_bits` bits (0..24; 0
 // is a no-op), ping-ponging between keys and tmp; *result is set to the
 // buffer that holds the sorted words.
 int partition_by_top_bits(lne_ctx* ctx, unsigned long long* keys, unsigned long long* tmp, int64_t count,

@@ -4,8 +4,8 @@
 // and path_embed::compute_u_sigma_root (LightNE/PathEmbed.h:371-408):
 //   Y = A * Omega, Q = qr(Y), B = A * Q, Z = qr(B * P), C = Z^T B,
 //   C = U_C S V^T, matU = Z * U_C, emb[:, j] = sqrt(S_j) * matU[:, j], j < dim.
-// Orthonormalisation is CholeskyQR (a shifted pass, then two plain passes)
-// instead of Householder geqrf+orgqr; R has a positive diagonal, so Q is the
+// Orthonormalisation is CholeskyQR (a shifted pass, then one or two plain
+// passes) instead of Householder geqrf+orgqr; R has a positive diagonal, so Q is the
 // unique thin-QR factor with that sign convention.  The core SVD is a
 // one-sided FP64 Jacobi.  The Gaussian sketches come from a counter-based
 // generator (MKL's SFMT19937 stream cannot be reproduced without MKL).  The
@@ -89,6 +89,15 @@ __global__ void k_copy_cols(const float* __restrict__ X, int64_t ldx, int64_t n,
 // CholeskyQR on X (n x ld FP32, r columns) with tmp as the ping-pong
 // partner; the two pointers are swapped so that the result ends in X.  Xb
 // (optional) receives a 16-bit copy of the result from the last GEMM.
+//
+// The first pass is shifted (Fukaya et al. 2020: G + s I with s = 64 u tr G,
+// the shift growing x10 while a pivot fails), then plain passes follow.
+// After the first pass the Gram of its result G1 = Q1^T Q1 measures how
+// orthogonal Q1 is: with ||G1 - I||_F <= 0.5, kappa(Q1)^2 <= 3 and one more
+// plain pass leaves Q orthogonal to FP32 rounding (CholeskyQR2); otherwise a
+// third pass follows (shifted CholeskyQR3), as for the second QR of the
+// randomized SVD, whose Z = B P has kappa ~ 5e3.
+static constexpr double kCholQR2Tol = 0.5;
 static int cholqr3(lne_ctx* ctx, float*& X, float*& tmp, int64_t n, int64_t ld, int r, Copy16 Xb,
                    int* launches) {
   Buf B(ctx);
@@ -101,9 +110,16 @@ static int cholqr3(lne_ctx* ctx, float*& X, float*& tmp, int64_t n, int64_t ld, 
   const double u32 = 5.9604644775390625e-08;
   for (int pass = 0; pass < 3; ++pass) {
     double shift = 0.0;
+    bool last = pass == 2;
     for (int attempt = 0; attempt < 6; ++attempt) {
       if ((rc = gram(ctx, src, ld, r, src, ld, r, n, G))) return rc;
       *launches += 2;
+      if (pass == 1 && attempt == 0) {
+        double e = 0.0;
+        if ((rc = identity_distance_host(ctx, G, r, &e))) return rc;
+        *launches += 1;
+        last = e <= kCholQR2Tol;
+      }
       if (pass == 0 || attempt > 0) {
         double tr = 0.0;
         if ((rc = trace_host(ctx, G, r, &tr))) return rc;
@@ -115,14 +131,15 @@ static int cholqr3(lne_ctx* ctx, float*& X, float*& tmp, int64_t n, int64_t ld, 
       if (rc == LNE_OK) break;
       if (rc != LNE_ERR_NUMERIC || attempt == 5) return rc;
     }
-    const bool last = pass == 2;
     if ((rc = gemm_tall(ctx, src, ld, r, W, r, n, dst, ld, last ? Xb : Copy16()))) return rc;
     *launches += 1;
     float* t = src;
     src = dst;
     dst = t;
+    if (last) break;
   }
-  // three passes: the result is in the buffer tmp came in
+  // the result is in src: the buffer X came in after two passes, tmp's
+  // after three
   X = src;
   tmp = dst;
   return LNE_OK;

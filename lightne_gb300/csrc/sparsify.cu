@@ -471,7 +471,8 @@ __global__ void k_insert(const unsigned long long* __restrict__ keys, const doub
 // ---------------------------------------------------------------------------
 static constexpr int kSliceThreads = 512;
 static constexpr int kSliceSlotsMax = 8192;  // 96 KB of shared memory: two CTAs per SM
-static constexpr int kSliceBitsMax = 16;
+static constexpr int kSliceBitsMax = 16;        // one batch: two radix passes
+static constexpr int kRoundSliceBitsMax = 24;   // a hash-range round: up to three
 
 __device__ __forceinline__ int64_t slice_of(unsigned long long h, int sbits) {
   return sbits == 0 ? 0 : (int64_t)(h >> (64 - sbits));
@@ -1065,7 +1066,7 @@ static int sparsify_rounds(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_
   if ((rc = S.get((void**)&keys, sizeof(unsigned long long) * buf_keys, "sample buffer")) ||
       (rc = S.get((void**)&keys2, sizeof(unsigned long long) * buf_keys, "partitioned samples")) ||
       (rc = S.get((void**)&uniq, sizeof(Slot) * buf_keys, "distinct pairs")) ||
-      (rc = S.get((void**)&starts, sizeof(int64_t) * (((int64_t)1 << kSliceBitsMax) + 1), "slice starts")) ||
+      (rc = S.get((void**)&starts, sizeof(int64_t) * (((int64_t)1 << kRoundSliceBitsMax) + 1), "slice starts")) ||
       (rc = S.get((void**)&rowcnt, sizeof(unsigned long long) * n, "row counts")) ||
       (rc = S.get(&scan_tmp, scan_tmp_bytes(n), "scan scratch")))
     return rc;
@@ -1131,7 +1132,7 @@ static int sparsify_rounds(lne_ctx* ctx, const lne_graph* g, const lne_sparsify_
       }
       if (got == 0) continue;
       int sbits = 0;
-      while (sbits < kSliceBitsMax && (got >> sbits) > (uint64_t)slots_max / 4) ++sbits;
+      while (sbits < kRoundSliceBitsMax && (got >> sbits) > (uint64_t)slots_max / 4) ++sbits;
       if ((got >> sbits) > (uint64_t)slots_max * 5 / 8) {
         set_error("lne_sparsify: a hash-range round has more samples than its slices hold; lower the batch");
         return fail(LNE_ERR_UNSUPPORTED);
