@@ -97,8 +97,9 @@ int lne_ctx_set_sparsify_batch(lne_ctx* ctx, int64_t keys);
  * row's kept entries, a second writes them into their rows, and the rows
  * are then sorted by column.  It needs the CSR plus one batch's buffers,
  * where the pair table path needs the table and twice the CSR's entries.
- * mode 0 (the default): rounds when the pair table and a batch do not fit
- * in free device memory; 1: always; -1: never.  row_sort_max (a power of
+ * mode 0 (the default): rounds when the pair table path (the table and a
+ * batch while sampling, then the CSR build's two copies of the entries) does
+ * not fit in free device memory; 1: always; -1: never.  row_sort_max (a power of
  * two in [32, 1024]; 0: 1024): the rounds' rows with at most that many
  * entries are sorted by column by one warp, longer rows by a thread block
  * through a bitmap of the column range.  The output is the same either

@@ -1295,13 +1295,19 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   const uint64_t buf_keys = want_keys < max_keys ? want_keys : max_keys;
   const int64_t edges_per_batch = (int64_t)std::max<uint64_t>(1, buf_keys / per_edge);
   // Above one batch, counts take the hash-range rounds when the pair table
-  // and a batch's buffers do not fit in free device memory (or when forced).
+  // path does not fit in free device memory (or when forced): its peak is
+  // the table plus a batch's buffers while sampling, then the CSR build's
+  // items twice (radix ping-pong, 12 bytes each) plus the CSR (8 bytes),
+  // two items per distinct pair, at most min(samples, capacity) pairs.
   if (!p->sample && want_keys > max_keys && ctx->sparsify_rounds >= 0 && ctx->sparsify_slice_slots > 0) {
     bool rounds = ctx->sparsify_rounds == 1;
     if (!rounds) {
       size_t fr = 0, tot = 0;
       LNE_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
-      rounds = (double)cap * sizeof(Slot) + 2.0 * sizeof(unsigned long long) * (double)buf_keys > (double)fr;
+      const double table_peak = (double)cap * sizeof(Slot) + 2.0 * sizeof(unsigned long long) * (double)buf_keys;
+      const double pairs = std::min((double)want_keys, (double)cap);
+      const double csr_peak = 2.0 * pairs * (2.0 * 12.0 + 8.0);
+      rounds = std::max(table_peak, csr_peak) > (double)fr;
     }
     if (rounds) {
       S.release(counters);
@@ -1558,6 +1564,18 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     return rc;
   }
   cudaEventRecord(ev.e[3], st);
+  {
+    int fl[kFlagWords];
+    LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (fl[kFlagRadixTimeout]) {
+      dfree(ctx, row_ptr);
+      dfree(ctx, col);
+      dfree(ctx, val);
+      set_error("lne_sparsify: a radix sort tile waited too long for its predecessor (internal error)");
+      return LNE_ERR_UNSUPPORTED;
+    }
+  }
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) {
     dfree(ctx, row_ptr);
