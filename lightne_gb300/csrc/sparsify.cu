@@ -1564,18 +1564,6 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
     return rc;
   }
   cudaEventRecord(ev.e[3], st);
-  {
-    int fl[kFlagWords];
-    LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
-    LNE_CUDA_TRY(cudaStreamSynchronize(st));
-    if (fl[kFlagRadixTimeout]) {
-      dfree(ctx, row_ptr);
-      dfree(ctx, col);
-      dfree(ctx, val);
-      set_error("lne_sparsify: a radix sort tile waited too long for its predecessor (internal error)");
-      return LNE_ERR_UNSUPPORTED;
-    }
-  }
   cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) {
     dfree(ctx, row_ptr);
