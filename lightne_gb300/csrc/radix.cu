@@ -115,17 +115,28 @@ __device__ __forceinline__ unsigned block_excl_scan_u32(unsigned v, unsigned* wa
   return before + incl - v;
 }
 
-// FINAL: write column = key & col_mask and the value (as float) to the CSR
-// arrays; otherwise write key and value to the next pass's buffers.  The
+// Output of a pass (OUT):
+//   kOutNext   key and value to the next pass's buffers;
+//   kOutCsr    column = key & col_mask and the value (as float) to the CSR
+//              arrays at the sorted position;
+//   kOutUpper  an upper-triangle item (u << cb | v): its CSR entry at
+//              off[u] + position, and its transpose (v << cb | u) to the
+//              next pass's buffers at the sorted position;
+//   kOutLower  a transposed item (v << cb | u): unless u == v, its CSR entry
+//              at off[v] + position.
+// A CSR position outside [0, nnz) (inconsistent counts) sets
+// kFlagSortOverflow instead of being written.  The
 // tile is first copied to shared memory with cp.async (24 KB in flight per
 // CTA, no registers held), ranked from there, reordered into a second
 // shared buffer and written out.
-template <bool FINAL, int MODE, bool VALS>
+enum OutMode : int { kOutNext = 0, kOutCsr = 1, kOutUpper = 2, kOutLower = 3 };
+template <int OUT, int MODE, bool VALS>
 __global__ void __launch_bounds__(kRadixThreads, 4) k_radix_scatter(
     const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t count, int shift, int dbits,
     int64_t ntiles, const int64_t* __restrict__ offs, unsigned long long* __restrict__ okeys,
     uint32_t* __restrict__ ovals, int32_t* __restrict__ ocol, float* __restrict__ oval, unsigned long long col_mask,
-    unsigned long long hmask) {
+    unsigned long long hmask, const int64_t* __restrict__ off = nullptr, int cb = 0, int64_t nnz = 0,
+    int* __restrict__ flags = nullptr) {
   extern __shared__ __align__(16) unsigned char radix_smem[];
   unsigned long long* skey = reinterpret_cast<unsigned long long*>(radix_smem);
   uint32_t* sval = reinterpret_cast<uint32_t*>(radix_smem + sizeof(unsigned long long) * kRadixTile);
@@ -227,9 +238,31 @@ __global__ void __launch_bounds__(kRadixThreads, 4) k_radix_scatter(
     const unsigned long long key = skey[j];
     const int d = (int)digit_of<MODE>(key, shift, mask, hmask);
     const int64_t pos = gstart[d] + (j - (int)tile_start[d]);
-    if (FINAL) {
+    if (OUT == kOutCsr) {
       ocol[pos] = (int32_t)(key & col_mask);
       oval[pos] = __uint_as_float(sval[j]);
+    } else if (OUT == kOutUpper) {
+      const unsigned long long u = key >> cb, v = key & col_mask;
+      const int64_t fp = __ldg(off + u) + pos;
+      if (fp >= 0 && fp < nnz) {
+        ocol[fp] = (int32_t)v;
+        oval[fp] = __uint_as_float(sval[j]);
+      } else {
+        atomicOr(&flags[kFlagSortOverflow], 1);
+      }
+      okeys[pos] = (v << cb) | u;
+      ovals[pos] = sval[j];
+    } else if (OUT == kOutLower) {
+      const unsigned long long v = key >> cb, u = key & col_mask;
+      if (u != v) {
+        const int64_t fp = __ldg(off + v) + pos;
+        if (fp >= 0 && fp < nnz) {
+          ocol[fp] = (int32_t)u;
+          oval[fp] = __uint_as_float(sval[j]);
+        } else {
+          atomicOr(&flags[kFlagSortOverflow], 1);
+        }
+      }
     } else {
       okeys[pos] = key;
       if (VALS) ovals[pos] = sval[j];
@@ -265,9 +298,9 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
   int64_t* hist = (int64_t*)mem;
   int64_t* offs = (int64_t*)(mem + ((hist_bytes + 255) & ~(size_t)255));
   void* scan_tmp = mem + 2 * ((hist_bytes + 255) & ~(size_t)255);
-  cudaFuncSetAttribute(k_radix_scatter<true, kDigitKey, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_radix_scatter<kOutCsr, kDigitKey, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kScatterSmem);
-  cudaFuncSetAttribute(k_radix_scatter<false, kDigitKey, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_radix_scatter<kOutNext, kDigitKey, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kScatterSmem);
   unsigned long long *src_k = keys, *dst_k = keys_tmp;
   uint32_t *src_v = vals, *dst_v = vals_tmp;
@@ -276,15 +309,92 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
     k_radix_hist<kDigitKey><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist, 0);
     scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
     if (p == passes - 1) {
-      k_radix_scatter<true, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+      k_radix_scatter<kOutCsr, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
           src_k, src_v, count, shift, dbits, ntiles, offs, nullptr, nullptr, out_col, out_val, col_mask, 0);
     } else {
-      k_radix_scatter<false, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+      k_radix_scatter<kOutNext, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
           src_k, src_v, count, shift, dbits, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0, 0);
       std::swap(src_k, dst_k);
       std::swap(src_v, dst_v);
     }
     if (launches) *launches += 5;  // histogram, 3-launch scan, scatter
+  }
+  dfree(ctx, mem);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("radix sort: kernel launch failed: ") + cudaGetErrorString(e));
+    return LNE_ERR_CUDA;
+  }
+  return LNE_OK;
+}
+
+int radix_sort_sym_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* vals, unsigned long long* keys_tmp,
+                       uint32_t* vals_tmp, int64_t count, int cbits, const int64_t* upoff, const int64_t* looff,
+                       int64_t nnz, int32_t* out_col, float* out_val, int* launches) {
+  if (count <= 0) return LNE_OK;
+  if (cbits < 1 || cbits > 31) {
+    set_error("radix sort: cbits must be in [1, 31]");
+    return LNE_ERR_INVALID;
+  }
+  cudaStream_t st = ctx->stream;
+  const int64_t ntiles = (count + kRadixTile - 1) / kRadixTile;
+  if (ntiles > 0x7fffffffLL) {
+    set_error("radix sort: too many items");
+    return LNE_ERR_UNSUPPORTED;
+  }
+  const int key_bits = 2 * cbits;
+  const int passes1 = (key_bits + 7) / 8, dbits1 = (key_bits + passes1 - 1) / passes1;
+  const int passes2 = (cbits + 7) / 8, dbits2 = (cbits + passes2 - 1) / passes2;
+  const int bins = 1 << std::max(dbits1, dbits2);
+  const int64_t cells = (int64_t)bins * ntiles;
+  char* mem = nullptr;
+  const size_t hist_bytes = (sizeof(int64_t) * (size_t)(cells + 1) + 255) & ~(size_t)255;
+  const size_t scan_bytes = (scan_tmp_bytes(cells) + 255) & ~(size_t)255;
+  int rc = dalloc(ctx, (void**)&mem, 2 * hist_bytes + scan_bytes, "radix histograms");
+  if (rc) return rc;
+  int64_t* hist = (int64_t*)mem;
+  int64_t* offs = (int64_t*)(mem + hist_bytes);
+  void* scan_tmp = mem + 2 * hist_bytes;
+  for (auto kern : {k_radix_scatter<kOutNext, kDigitKey, true>, k_radix_scatter<kOutUpper, kDigitKey, true>,
+                    k_radix_scatter<kOutLower, kDigitKey, true>})
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
+  const unsigned long long cmask = (1ULL << cbits) - 1;
+  unsigned long long *src_k = keys, *dst_k = keys_tmp;
+  uint32_t *src_v = vals, *dst_v = vals_tmp;
+  // the upper items by (u, v); the last pass places them and writes their
+  // transposes (v, u) to the other buffers
+  for (int p = 0; p < passes1; ++p) {
+    const int shift = p * dbits1, dbits = dbits1;
+    const int64_t c = (int64_t)(1 << dbits) * ntiles;
+    k_radix_hist<kDigitKey><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist, 0);
+    scan_exclusive_i64(hist, offs, c, scan_tmp, st);
+    if (p == passes1 - 1)
+      k_radix_scatter<kOutUpper, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, dbits, ntiles, offs, dst_k, dst_v, out_col, out_val, cmask, 0, upoff, cbits, nnz,
+          ctx->d_flags);
+    else
+      k_radix_scatter<kOutNext, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, dbits, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0, 0);
+    std::swap(src_k, dst_k);
+    std::swap(src_v, dst_v);
+    if (launches) *launches += 5;
+  }
+  // the transposes, already ordered by u, stably by v: the lower triangle
+  for (int p = 0; p < passes2; ++p) {
+    const int shift = cbits + p * dbits2, dbits = dbits2;
+    const int64_t c = (int64_t)(1 << dbits) * ntiles;
+    k_radix_hist<kDigitKey><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(src_k, count, shift, dbits, ntiles, hist, 0);
+    scan_exclusive_i64(hist, offs, c, scan_tmp, st);
+    if (p == passes2 - 1)
+      k_radix_scatter<kOutLower, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, dbits, ntiles, offs, nullptr, nullptr, out_col, out_val, cmask, 0, looff, cbits,
+          nnz, ctx->d_flags);
+    else
+      k_radix_scatter<kOutNext, kDigitKey, true><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+          src_k, src_v, count, shift, dbits, ntiles, offs, dst_k, dst_v, nullptr, nullptr, 0, 0);
+    std::swap(src_k, dst_k);
+    std::swap(src_v, dst_v);
+    if (launches) *launches += 5;
   }
   dfree(ctx, mem);
   cudaError_t e = cudaGetLastError();
@@ -316,12 +426,12 @@ int partition_by_slot(lne_ctx* ctx, const unsigned long long* keys, unsigned lon
   int64_t* offs = (int64_t*)(mem + hist_bytes);
   void* scan_tmp = mem + 2 * hist_bytes;
   cudaStream_t st = ctx->stream;
-  cudaFuncSetAttribute(k_radix_scatter<false, kDigitSlot, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_radix_scatter<kOutNext, kDigitSlot, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kScatterSmem);
   k_radix_hist<kDigitSlot><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(keys, count, shift, dbits, ntiles, hist,
                                                                        hmask);
   scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
-  k_radix_scatter<false, kDigitSlot, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+  k_radix_scatter<kOutNext, kDigitSlot, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
       keys, nullptr, count, shift, dbits, ntiles, offs, out, nullptr, nullptr, nullptr, 0, hmask);
   if (launches) *launches += 5;
   dfree(ctx, mem);
@@ -358,7 +468,7 @@ int partition_by_top_bits(lne_ctx* ctx, unsigned long long* keys, unsigned long 
   int64_t* offs = (int64_t*)(mem + hist_bytes);
   void* scan_tmp = mem + 2 * hist_bytes;
   cudaStream_t st = ctx->stream;
-  cudaFuncSetAttribute(k_radix_scatter<false, kDigitKey, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_radix_scatter<kOutNext, kDigitKey, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kScatterSmem);
   unsigned long long *src = keys, *dst = tmp;
   for (int p = 0; p < passes; ++p) {
@@ -367,7 +477,7 @@ int partition_by_top_bits(lne_ctx* ctx, unsigned long long* keys, unsigned long 
     const int shift = 64 - top_bits + p * dbits;
     k_radix_hist<kDigitKey><<<hist_grid(ntiles), kRadixThreads, 0, st>>>(src, count, shift, dbits, ntiles, hist, 0);
     scan_exclusive_i64(hist, offs, cells, scan_tmp, st);
-    k_radix_scatter<false, kDigitKey, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
+    k_radix_scatter<kOutNext, kDigitKey, false><<<(unsigned)ntiles, kRadixThreads, kScatterSmem, st>>>(
         src, nullptr, count, shift, dbits, ntiles, offs, dst, nullptr, nullptr, nullptr, 0, 0);
     std::swap(src, dst);
     if (launches) *launches += 5;

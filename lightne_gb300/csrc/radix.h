@@ -17,6 +17,19 @@ int radix_sort_pairs_to_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* va
                             uint32_t* vals_tmp, int64_t count, int key_bits, unsigned long long col_mask,
                             int32_t* out_col, float* out_val, int* launches);
 
+// The symmetric CSR from `count` upper-triangle items (u << cbits | v with
+// u <= v, float bits): a stable LSD sort by (u, v) whose last pass writes
+// each entry (u, v) to out_col/out_val at upoff[u] + its sorted position and
+// its transpose (v << cbits | u) to the scratch buffers, then a stable sort
+// of the transposes by v (ceil(cbits / 8) passes) whose last pass writes
+// each off-diagonal (v, u) at looff[v] + its sorted position.  upoff/looff
+// place a row's lower entries before its diagonal and upper ones; nnz
+// bounds the positions (kFlagSortOverflow otherwise).  keys/vals are
+// overwritten; keys_tmp/vals_tmp are scratch of the same size.
+int radix_sort_sym_csr(lne_ctx* ctx, unsigned long long* keys, uint32_t* vals, unsigned long long* keys_tmp,
+                       uint32_t* vals_tmp, int64_t count, int cbits, const int64_t* upoff, const int64_t* looff,
+                       int64_t nnz, int32_t* out_col, float* out_val, int* launches);
+
 // Reorders `count` pair keys by the top min(8, table_bits) bits of their
 // pair-table slot (hash64_2(key) & (2^table_bits - 1)) into `out`, so that
 // consecutive inserts touch one slice of the table.  Stable.

@@ -692,11 +692,15 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 }
 
 // Trunc-log map (PathEmbed.h:203-218) fused with the per-row counts of the
-// CSR build (PathEmbed.h:226-288).  Every kept entry (u, v) is appended to
-// the item list as key u << cbits | v with the float bits of its log value,
-// and, unless -upper or u == v, also as (v, u) (PathEmbed.h:300-311).  The
-// append order depends on scheduling; the keys are distinct, so the radix
-// sort by key that follows makes the CSR independent of it.
+// CSR build (PathEmbed.h:226-288).  Every kept pair (u, v), u <= v, is
+// appended to the item list once, as key u << cbits | v with the float bits
+// of its log value; its entry (v, u) of the lower triangle (PathEmbed.h:
+// 300-311, unless -upper or u == v) is not written but counted: rowcnt[u]
+// counts row u's upper entries (diagonal included), lowcnt[v] row v's lower
+// ones, diag[u] marks a kept diagonal entry.  The append order depends on
+// scheduling; the keys are distinct, so the radix sort by key that follows
+// (and, for the lower triangle, the sort of its transpose) makes the CSR
+// independent of it.
 //
 // Counts (-sample 0): adj = ((w * factor) / d_u) / d_v is reproduced
 // exactly by integer arithmetic (the reference's three double roundings),
@@ -750,6 +754,8 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
                                                   const Vertex* __restrict__ vd, double factor, int upper,
                                                   const LogTable* __restrict__ ltab,
                                                   unsigned long long* __restrict__ rowcnt,
+                                                  unsigned long long* __restrict__ lowcnt,
+                                                  uint8_t* __restrict__ diag,
                                                   unsigned long long* __restrict__ kept_total,
                                                   unsigned long long* __restrict__ n_items, int cbits,
                                                   uint64_t max_items, unsigned long long* __restrict__ okeys,
@@ -779,10 +785,12 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
     if (have) o = trunclog_entry<WEIGHTED>(key, raw, vd, factor, xf, upper, tab);
     if (o.nitem) {
       atomicAdd(&rowcnt[o.u], 1ULL);
-      if (o.nitem == 2) atomicAdd(&rowcnt[o.v], 1ULL);
+      if (o.nitem == 2) atomicAdd(&lowcnt[o.v], 1ULL);
+      if (o.u == o.v) diag[o.u] = 1;
       ++kept;
     }
-    unsigned incl = o.nitem;
+    const unsigned one = o.nitem ? 1u : 0u;
+    unsigned incl = one;
 #pragma unroll
     for (int s = 1; s < 32; s <<= 1) {
       const unsigned t = __shfl_up_sync(kFullMask, incl, s);
@@ -792,16 +800,11 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
     unsigned long long base = 0;
     if (lane == 31 && wtot) base = atomicAdd(n_items, (unsigned long long)wtot);
     base = __shfl_sync(kFullMask, base, 31);
-    if (o.nitem) {
-      const uint64_t pos = base + incl - o.nitem;
-      if (pos + o.nitem <= max_items) {
-        const uint32_t fb = __float_as_uint(o.f);
+    if (one) {
+      const uint64_t pos = base + incl - 1;
+      if (pos < max_items) {
         okeys[pos] = ((unsigned long long)o.u << cbits) | o.v;
-        ovals[pos] = fb;
-        if (o.nitem == 2) {
-          okeys[pos + 1] = ((unsigned long long)o.v << cbits) | o.u;
-          ovals[pos + 1] = fb;
-        }
+        ovals[pos] = __float_as_uint(o.f);
       } else {
         atomicOr(&flags[kFlagSortOverflow], 1);
       }
@@ -834,10 +837,12 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
       if (have) o = trunclog_entry<WEIGHTED>(sl.key, sl.val, vd, factor, xf, upper, tab);
       if (o.nitem) {
         atomicAdd(&rowcnt[o.u], 1ULL);
-        if (o.nitem == 2) atomicAdd(&rowcnt[o.v], 1ULL);
+        if (o.nitem == 2) atomicAdd(&lowcnt[o.v], 1ULL);
+        if (o.u == o.v) diag[o.u] = 1;
         ++kept;
       }
-      unsigned incl = o.nitem;
+      const unsigned one = o.nitem ? 1u : 0u;
+      unsigned incl = one;
 #pragma unroll
       for (int sh = 1; sh < 32; sh <<= 1) {
         const unsigned t = __shfl_up_sync(kFullMask, incl, sh);
@@ -853,16 +858,11 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
       __syncthreads();
       unsigned before = 0;
       for (int w = 0; w < wid; ++w) before += wsum[w];
-      if (o.nitem) {
-        const uint64_t pos = bbase + before + incl - o.nitem;
-        if (pos + o.nitem <= max_items) {
-          const uint32_t fb = __float_as_uint(o.f);
+      if (one) {
+        const uint64_t pos = bbase + before + incl - 1;
+        if (pos < max_items) {
           okeys[pos] = ((unsigned long long)o.u << cbits) | o.v;
-          ovals[pos] = fb;
-          if (o.nitem == 2) {
-            okeys[pos + 1] = ((unsigned long long)o.v << cbits) | o.u;
-            ovals[pos + 1] = fb;
-          }
+          ovals[pos] = __float_as_uint(o.f);
         } else {
           atomicOr(&flags[kFlagSortOverflow], 1);
         }
@@ -899,6 +899,30 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
   if (qn > 0) flush(qn);
   for (int o = 16; o > 0; o >>= 1) kept += __shfl_down_sync(kFullMask, kept, o);
   if (lane == 0 && kept) atomicAdd(kept_total, kept);
+}
+
+// Counts of the symmetric CSR from the trunc-log's counts: full[r] = row r's
+// entries (upper, diagonal included, plus lower); tcnt[r] = entries of row r
+// in the transposed upper triangle (the lower ones plus the diagonal).
+__global__ void k_sym_counts(const unsigned long long* __restrict__ up, const unsigned long long* __restrict__ lo,
+                             const uint8_t* __restrict__ diag, int64_t n, int64_t* __restrict__ full,
+                             int64_t* __restrict__ tcnt) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    full[r] = (int64_t)(up[r] + lo[r]);
+    tcnt[r] = (int64_t)lo[r] + diag[r];
+  }
+}
+
+// Final CSR position of an entry = offset of its row + its position in the
+// sorted (upper or transposed) item array: row r's lower entries come first
+// (columns < r), then its diagonal and upper entries.
+__global__ void k_sym_offsets(const int64_t* __restrict__ row_ptr, const unsigned long long* __restrict__ lo,
+                              const int64_t* __restrict__ upstart, const int64_t* __restrict__ tstart, int64_t n,
+                              int64_t* __restrict__ upoff, int64_t* __restrict__ looff) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    upoff[r] = row_ptr[r] + (int64_t)lo[r] - upstart[r];
+    looff[r] = row_ptr[r] - tstart[r];
+  }
 }
 
 static unsigned grid_for(int64_t items, int threads, int64_t cap_blocks) {
@@ -1487,18 +1511,23 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   // Item keys: row << cbits | col with cbits bits per vertex id.
   int cbits = 1;
   while (cbits < 32 && ((int64_t)1 << cbits) < n) ++cbits;
-  const uint64_t max_items = 2 * (uint64_t)h_cnt[2] + 1;  // each distinct pair gives at most 2 entries
+  const uint64_t max_items = (uint64_t)h_cnt[2] + 1;  // one item per kept pair
   unsigned long long* rowcnt = nullptr;
+  unsigned long long* lowcnt = nullptr;
+  uint8_t* diag = nullptr;
   int64_t* row_ptr = nullptr;
   void* scan_tmp = nullptr;
   unsigned long long* ikeys = nullptr;
   uint32_t* ivals = nullptr;
   if ((rc = S.get((void**)&rowcnt, sizeof(unsigned long long) * n, "row counts"))) return rc;
+  if ((rc = S.get((void**)&lowcnt, sizeof(unsigned long long) * n + n, "lower row counts"))) return rc;
+  diag = reinterpret_cast<uint8_t*>(lowcnt + n);
   if ((rc = S.get(&scan_tmp, scan_tmp_bytes(n), "scan scratch"))) return rc;
   if ((rc = S.get((void**)&ikeys, sizeof(unsigned long long) * max_items, "csr items"))) return rc;
   if ((rc = S.get((void**)&ivals, sizeof(uint32_t) * max_items, "csr item values"))) return rc;
   if ((rc = dalloc(ctx, (void**)&row_ptr, sizeof(int64_t) * (n + 1), "row_ptr"))) return rc;
   LNE_CUDA_TRY(cudaMemsetAsync(rowcnt, 0, sizeof(unsigned long long) * n, st));
+  LNE_CUDA_TRY(cudaMemsetAsync(lowcnt, 0, sizeof(unsigned long long) * n + n, st));
   // the trunc-log reads the pair table, or the dense distinct pairs of the
   // sliced aggregation (every slot occupied)
   const Slot* tsrc = sliced ? uniq : table;
@@ -1506,62 +1535,111 @@ extern "C" int lne_sparsify(lne_ctx* ctx, const lne_graph* g, const lne_sparsify
   const unsigned tgrid = grid_for((int64_t)tcap, 256, (int64_t)ctx->num_sms * 16);
   if (p->sample)
     k_trunclog<true, false><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
-                                            (const LogTable*)ctx->log_table, rowcnt, counters + 3, counters + 4,
+                                            (const LogTable*)ctx->log_table, rowcnt, lowcnt, diag, counters + 3, counters + 4,
                                             cbits, max_items, ikeys, ivals, ctx->d_flags);
   else if (sliced)
     k_trunclog<false, true><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
-                                                   (const LogTable*)ctx->log_table, rowcnt, counters + 3,
+                                                   (const LogTable*)ctx->log_table, rowcnt, lowcnt, diag, counters + 3,
                                                    counters + 4, cbits, max_items, ikeys, ivals, ctx->d_flags);
   else
     k_trunclog<false, false><<<tgrid, 256, 0, st>>>(tsrc, tcap, g->vdata, factor, p->upper,
-                                                    (const LogTable*)ctx->log_table, rowcnt, counters + 3,
+                                                    (const LogTable*)ctx->log_table, rowcnt, lowcnt, diag, counters + 3,
                                                     counters + 4, cbits, max_items, ikeys, ivals, ctx->d_flags);
   if (table) S.release(table);
   if (uniq) S.release(uniq);
   cudaEventRecord(ev.e[2], st);
-  scan_exclusive_i64((const int64_t*)rowcnt, row_ptr, n, scan_tmp, st);
+  // Row pointers and, for the full matrix, each row's offsets for the two
+  // sorts: [full | tcnt | upstart | tstart | upoff | looff]
+  int64_t* offs = nullptr;
+  int64_t *upoff = nullptr, *looff = nullptr;
+  int extra_launches = 3;  // the row pointer scan
+  if (!p->upper) {
+    if ((rc = dalloc(ctx, (void**)&offs, sizeof(int64_t) * (6 * (size_t)n + 2), "csr offsets"))) {
+      dfree(ctx, row_ptr);
+      return rc;
+    }
+    int64_t* full = offs;
+    int64_t* tcnt = offs + n;
+    int64_t* upstart = offs + 2 * n;
+    int64_t* tstart = offs + 3 * n + 1;
+    upoff = offs + 4 * n + 2;
+    looff = offs + 5 * n + 2;
+    const unsigned og = grid_for(n, 256, (int64_t)ctx->num_sms * 16);
+    k_sym_counts<<<og, 256, 0, st>>>(rowcnt, lowcnt, diag, n, full, tcnt);
+    scan_exclusive_i64(full, row_ptr, n, scan_tmp, st);
+    scan_exclusive_i64((const int64_t*)rowcnt, upstart, n, scan_tmp, st);
+    scan_exclusive_i64(tcnt, tstart, n, scan_tmp, st);
+    k_sym_offsets<<<og, 256, 0, st>>>(row_ptr, lowcnt, upstart, tstart, n, upoff, looff);
+    extra_launches += 2 + 6;
+  } else {
+    scan_exclusive_i64((const int64_t*)rowcnt, row_ptr, n, scan_tmp, st);
+  }
   int64_t nnz = 0;
-  unsigned long long tail[2] = {0, 0};  // kept upper entries, appended items
+  unsigned long long tail[2] = {0, 0};  // kept pairs, appended items
   LNE_CUDA_TRY(cudaMemcpyAsync(&nnz, row_ptr + n, 8, cudaMemcpyDeviceToHost, st));
   LNE_CUDA_TRY(cudaMemcpyAsync(tail, counters + 3, sizeof(tail), cudaMemcpyDeviceToHost, st));
   LNE_CUDA_TRY(cudaMemcpyAsync(h_flags, ctx->d_flags, sizeof(h_flags), cudaMemcpyDeviceToHost, st));
   LNE_CUDA_TRY(cudaStreamSynchronize(st));
   LNE_CUDA_TRY(cudaGetLastError());
   const unsigned long long kept = tail[0];
-  if (h_flags[kFlagSortOverflow] || tail[1] != (unsigned long long)nnz) {
+  const int64_t items = (int64_t)tail[1];
+  if (h_flags[kFlagSortOverflow] || tail[1] != kept || (p->upper && items != nnz) || items > nnz) {
     dfree(ctx, row_ptr);
+    dfree(ctx, offs);
     set_error("lne_sparsify: CSR item count does not match the row counts (internal sizing error)");
     return LNE_ERR_UNSUPPORTED;
   }
   S.release(rowcnt);
+  S.release(lowcnt);
   S.release(scan_tmp);
 
-  // Sort the items by (row, col) and write the CSR columns and values.
-  // (Placing the items into their rows at atomic cursors and sorting each
-  // row, as the hash-range rounds do, measured slower here: the cursor
-  // atomics and scattered 4-byte writes ran at ~29G entries/s, and the
-  // per-row sorts cost more than the radix passes they replace.)
+  // Sort the upper-triangle items by (row, col), writing each entry at its
+  // final CSR position, and (full matrix) sort their transpose by row to
+  // place the lower triangle: ceil(2 cbits / 8) + ceil(cbits / 8) passes over
+  // one item per kept pair instead of sorting both orientations.  (Placing the items into
+  // their rows at atomic cursors and sorting each row, as the hash-range
+  // rounds do, measured slower here: the cursor atomics and scattered 4-byte
+  // writes ran at ~29G entries/s, and the per-row sorts cost more than the
+  // radix passes they replace.)
   int32_t* col = nullptr;
   float* val = nullptr;
   unsigned long long* tkeys = nullptr;
   uint32_t* tvals = nullptr;
   if ((rc = dalloc(ctx, (void**)&col, sizeof(int32_t) * (nnz > 0 ? nnz : 1), "csr col")) ||
       (rc = dalloc(ctx, (void**)&val, sizeof(float) * (nnz > 0 ? nnz : 1), "csr val")) ||
-      (rc = S.get((void**)&tkeys, sizeof(unsigned long long) * (nnz > 0 ? nnz : 1), "sort keys")) ||
-      (rc = S.get((void**)&tvals, sizeof(uint32_t) * (nnz > 0 ? nnz : 1), "sort values"))) {
+      (rc = S.get((void**)&tkeys, sizeof(unsigned long long) * (items > 0 ? items : 1), "sort keys")) ||
+      (rc = S.get((void**)&tvals, sizeof(uint32_t) * (items > 0 ? items : 1), "sort values"))) {
+    dfree(ctx, row_ptr);
+    dfree(ctx, col);
+    dfree(ctx, val);
+    dfree(ctx, offs);
+    return rc;
+  }
+  // sampling and aggregation, [table sum, block sum,] trunc-log, scans
+  int launches = launches_sample + (sliced ? 0 : 2) + 1 + extra_launches;
+  if (p->upper)
+    rc = radix_sort_pairs_to_csr(ctx, ikeys, ivals, tkeys, tvals, items, 2 * cbits, ((1ULL << cbits) - 1), col, val,
+                                 &launches);
+  else
+    rc = radix_sort_sym_csr(ctx, ikeys, ivals, tkeys, tvals, items, cbits, upoff, looff, nnz, col, val, &launches);
+  dfree(ctx, offs);
+  if (rc) {
     dfree(ctx, row_ptr);
     dfree(ctx, col);
     dfree(ctx, val);
     return rc;
   }
-  // sampling and aggregation, [table sum, block sum,] trunc-log, 3 scan
-  int launches = launches_sample + (sliced ? 0 : 2) + 4;
-  if ((rc = radix_sort_pairs_to_csr(ctx, ikeys, ivals, tkeys, tvals, nnz, 2 * cbits, ((1ULL << cbits) - 1), col,
-                                    val, &launches))) {
-    dfree(ctx, row_ptr);
-    dfree(ctx, col);
-    dfree(ctx, val);
-    return rc;
+  {
+    int fl[kFlagWords];
+    LNE_CUDA_TRY(cudaMemcpyAsync(fl, ctx->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st));
+    LNE_CUDA_TRY(cudaStreamSynchronize(st));
+    if (fl[kFlagSortOverflow]) {
+      dfree(ctx, row_ptr);
+      dfree(ctx, col);
+      dfree(ctx, val);
+      set_error("lne_sparsify: CSR entries do not match their rows (internal error)");
+      return LNE_ERR_UNSUPPORTED;
+    }
   }
   cudaEventRecord(ev.e[3], st);
   cudaError_t le = cudaGetLastError();
