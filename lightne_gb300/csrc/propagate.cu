@@ -202,7 +202,7 @@ struct EpiFirst {
     store_f32<N>(L1, ld, r, e0, l1);
     if (L1b) store_16<HT, N>(L1b, ld, r, e0, l1);
     if (fin.base)
-      fin.apply<N>(r, e0, ld, c, cv);
+      fin.template apply<N>(r, e0, ld, c, cv);
     else if (conv)
       store_f32<N>(conv, ld, r, e0, cv);
   }
@@ -263,7 +263,7 @@ struct EpiStep {
       cv[i] = fmaf(ck, l2[i], cv[i]);
     }
     if (fin.base) {
-      fin.apply<N>(r, e0, ld, c, cv);
+      fin.template apply<N>(r, e0, ld, c, cv);
     } else {
       store_f32<N>(L2, ld, r, e0, l2);
       if (L2b) store_16<HT, N>(L2b, ld, r, e0, l2);

@@ -147,47 +147,47 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
           acc.a[k][e] = (acc.a[k][e] + g1) + g2;
         }
     }
-    return;
-  }
-  for (int64_t base = j0; base < j1; base += 32) {
-    const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);
-    const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;
-    const float v = Rows::kHasVal ? (lane < cnt ? R.v(base + lane) : 0.f) : 1.f;
-    for (int t0 = 0; t0 < cnt; t0 += P * kUnroll) {
-      uint32_t cc[kUnroll];
-      float vv[kUnroll];
-      float x[kUnroll][VPL][E];
+  } else {
+    for (int64_t base = j0; base < j1; base += 32) {
+      const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);
+      const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;
+      const float v = Rows::kHasVal ? (lane < cnt ? R.v(base + lane) : 0.f) : 1.f;
+      for (int t0 = 0; t0 < cnt; t0 += P * kUnroll) {
+        uint32_t cc[kUnroll];
+        float vv[kUnroll];
+        float x[kUnroll][VPL][E];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
-        const int t = t0 + u * P + grp;
-        cc[u] = __shfl_sync(kFull, c, t & 31);
-        vv[u] = Rows::kHasVal ? __shfl_sync(kFull, v, t & 31) : 1.f;
-        const XT* xr = X + (int64_t)cc[u] * ldx;
+        for (int u = 0; u < kUnroll; ++u) {
+          const int t = t0 + u * P + grp;
+          cc[u] = __shfl_sync(kFull, c, t & 31);
+          vv[u] = Rows::kHasVal ? __shfl_sync(kFull, v, t & 31) : 1.f;
+          const XT* xr = X + (int64_t)cc[u] * ldx;
 #pragma unroll
-        for (int k = 0; k < VPL; ++k) {
-          const int ch = gl + G * k;
-          if (t < cnt && ch < C) {
-            Vec16<XT>::load(xr + ch * E, x[u][k]);
-          } else {
+          for (int k = 0; k < VPL; ++k) {
+            const int ch = gl + G * k;
+            if (t < cnt && ch < C) {
+              Vec16<XT>::load(xr + ch * E, x[u][k]);
+            } else {
 #pragma unroll
-            for (int e = 0; e < E; ++e) x[u][k][e] = 0.f;
+              for (int e = 0; e < E; ++e) x[u][k][e] = 0.f;
+            }
           }
         }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+          for (int k = 0; k < VPL; ++k)
+#pragma unroll
+            for (int e = 0; e < E; ++e) acc.a[k][e] = fmaf(vv[u], x[u][k][e], acc.a[k][e]);
       }
-#pragma unroll
-      for (int u = 0; u < kUnroll; ++u)
-#pragma unroll
-        for (int k = 0; k < VPL; ++k)
-#pragma unroll
-          for (int e = 0; e < E; ++e) acc.a[k][e] = fmaf(vv[u], x[u][k][e], acc.a[k][e]);
     }
+#pragma unroll
+    for (int o = G; o < 32; o <<= 1)
+#pragma unroll
+      for (int k = 0; k < VPL; ++k)
+#pragma unroll
+        for (int e = 0; e < E; ++e) acc.a[k][e] += __shfl_xor_sync(kFull, acc.a[k][e], o);
   }
-#pragma unroll
-  for (int o = G; o < 32; o <<= 1)
-#pragma unroll
-    for (int k = 0; k < VPL; ++k)
-#pragma unroll
-      for (int e = 0; e < E; ++e) acc.a[k][e] += __shfl_xor_sync(kFull, acc.a[k][e], o);
 }
 
 // Main kernel: short rows call the epilogue directly; chunks of long rows
