@@ -9,9 +9,9 @@
 // Within an item the warp is split into P = 32/G groups of G lanes; lane gl
 // of a group owns the 16-byte column vectors gl, gl+G, ... of the row, and
 // group g takes the nonzeros t with t % P == g.  Column ids (and values) are
-// loaded 32 at a time, one per lane, and broadcast with shuffles; the
-// gathers of kUnroll nonzeros are issued before their FMAs so that every
-// lane keeps several 16-byte loads in flight.
+// loaded up to 32 at a time, one per lane, and broadcast with shuffles; the
+// gathers of several nonzeros are issued before their FMAs so that every
+// lane keeps several 16-byte loads in flight (SpmmTune).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -66,6 +66,31 @@ struct GraphRows {  // graph adjacency: {offset, degree} per vertex, unit values
   static constexpr bool kHasVal = false;
 };
 
+// Gather depth of the raw-staged path (FP8 operands, 9-lane groups and
+// 128-element 16-bit rows): each lane issues the gathers of kU nonzeros
+// before their FMAs, kept as raw 16-byte words (4 registers each).  Column
+// ids are loaded in batches of kBatch <= 32, a multiple of the P kU
+// nonzeros a warp takes per step, so that no step of a batch runs
+// part-empty.  Measured at n = 1.14M, nnz = 351M: a 144-element FP16 row
+// at kU = 3 (batch 27) 11.8 ms against 13.5 at kU = 2 with batches of 32;
+// 144-element FP8 rows at kU = 5 (batch 30) 9.2 against 10.0 at 4;
+// 128-element 16-bit rows on the graph (the propagation) at kU = 5 (batch
+// 30) 14.3 against 16.3 widened at the load 2 deep.  Deeper staging spills
+// or, at 3 CTAs per SM, loses more warps than it gains in flight.  Other
+// operands are widened at the load and staged kUnroll deep.
+template <typename XT, int G, int VPL>
+struct SpmmTune {
+  static constexpr int E = Vec16<XT>::E;
+  static constexpr int P = 32 / G;
+  static constexpr bool kRaw = E == 16 || (G & (G - 1)) != 0 || (E == 8 && G == 16 && VPL == 1);
+  static constexpr int kWant = (G == 9 && VPL == 2)                               ? 3
+                               : VPL == 1 && (G == 9 || (G == 16 && E == 8)) ? 5
+                                                                                  : (VPL >= 4 ? 1 : 4 / VPL);
+  static constexpr int kU = kWant * P <= 32 ? kWant : 32 / P;
+  static constexpr int kBatch = (32 / (P * kU)) * (P * kU);
+  static_assert(kBatch >= 1 && kBatch <= 32, "a batch of column ids is one per lane");
+};
+
 template <typename XT, int VPL>
 struct Acc {
   static constexpr int E = Vec16<XT>::E;
@@ -85,21 +110,19 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
                                                 int64_t ldx, int C, Acc<XT, VPL>& acc) {
   constexpr int P = 32 / G;
   constexpr int E = Vec16<XT>::E;
-  // nonzeros whose gathers are in flight per lane: about 16 staged floats
-  constexpr int kStaged = 16 / (VPL * E);
-  constexpr int kUnroll = kStaged < 1 ? 1 : (kStaged > 4 ? 4 : kStaged);
   const int lane = threadIdx.x & 31;
   const int grp = lane / G, gl = lane % G;
-  if constexpr (E == 16 || (G & (G - 1)) != 0) {
-    // 16 elements per vector (FP8), or a group of 9 lanes: the gathers of
-    // 4 / VPL nonzeros are staged as raw 16-byte words (4 registers each),
-    // widened at the FMAs
-    constexpr int kU = VPL >= 4 ? 1 : 4 / VPL;
+  if constexpr (SpmmTune<XT, G, VPL>::kRaw) {
+    // FP8 vectors, a group of 9 lanes or 16 lanes of 16-bit vectors: the
+    // gathers of kU nonzeros are staged as raw 16-byte words, widened at
+    // the FMAs
+    constexpr int kU = SpmmTune<XT, G, VPL>::kU;
     // G = 9 (a 144-element row: 9 FP8 vectors, or 18 BF16 / FP16 vectors
     // at two per lane): three groups of 9 lanes, lanes 27..31 idle
     const bool in_grp = grp < P;
-    for (int64_t base = j0; base < j1; base += 32) {
-      const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);
+    constexpr int kB = SpmmTune<XT, G, VPL>::kBatch;
+    for (int64_t base = j0; base < j1; base += kB) {
+      const int cnt = (int)((j1 - base) < kB ? (j1 - base) : kB);
       const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;
       const float v = Rows::kHasVal ? (lane < cnt ? R.v(base + lane) : 0.f) : 1.f;
       for (int t0 = 0; t0 < cnt; t0 += P * kU) {
@@ -148,6 +171,9 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
         }
     }
   } else {
+    // nonzeros whose gathers are in flight per lane: about 16 staged floats
+    constexpr int kStaged = 16 / (VPL * E);
+    constexpr int kUnroll = kStaged < 1 ? 1 : (kStaged > 4 ? 4 : kStaged);
     for (int64_t base = j0; base < j1; base += 32) {
       const int cnt = (int)((j1 - base) < 32 ? (j1 - base) : 32);
       const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;
