@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "dense_common.cuh"
 #include "lne_internal.h"
 
@@ -71,19 +73,22 @@ struct GraphRows {  // graph adjacency: {offset, degree} per vertex, unit values
 // before their FMAs, kept as raw 16-byte words (4 registers each).  Column
 // ids are loaded in batches of kBatch <= 32, a multiple of the P kU
 // nonzeros a warp takes per step, so that no step of a batch runs
-// part-empty.  Measured at n = 1.14M, nnz = 351M: a 144-element FP16 row
-// at kU = 3 (batch 27) 11.8 ms against 13.5 at kU = 2 with batches of 32;
-// 144-element FP8 rows at kU = 5 (batch 30) 9.2 against 10.0 at 4;
-// 128-element 16-bit rows on the graph (the propagation) at kU = 5 (batch
-// 30) 14.3 against 16.3 widened at the load 2 deep.  Deeper staging spills
-// or, at 3 CTAs per SM, loses more warps than it gains in flight.  Other
-// operands are widened at the load and staged kUnroll deep.
+// part-empty, and a step whose nonzeros are all in the batch loads without
+// predicates.  Measured at n = 1.14M, nnz = 351M (`B = A Q`, the sketch
+// product, the 19 SpMMs of the propagation), unpredicated full steps
+// included: a 144-element FP16 row at kU = 2 (batch 30) 11.1 ms against
+// 11.6 at 3 and 12.8 at 4; 144-element FP8 rows at kU = 5 (batch 30) 8.0
+// against 8.4 at 4 and 9.2 at 6; 128-element 16-bit rows on the graph
+// (the propagation) at kU = 5 (batch 30) 13.0 against 13.2 at 4 and 13.3
+// at 6.  Deeper staging spills (64 registers a thread at 4 CTAs of 256 per
+// SM); compiled for 3 CTAs per SM it lost more warps than it gained in
+// flight.  Other operands are widened at the load and staged kUnroll deep.
 template <typename XT, int G, int VPL>
 struct SpmmTune {
   static constexpr int E = Vec16<XT>::E;
   static constexpr int P = 32 / G;
   static constexpr bool kRaw = E == 16 || (G & (G - 1)) != 0 || (E == 8 && G == 16 && VPL == 1);
-  static constexpr int kWant = (G == 9 && VPL == 2)                               ? 3
+  static constexpr int kWant = (G == 9 && VPL == 2)                               ? 2
                                : VPL == 1 && (G == 9 || (G == 16 && E == 8)) ? 5
                                                                                   : (VPL >= 4 ? 1 : 4 / VPL);
   static constexpr int kU = kWant * P <= 32 ? kWant : 32 / P;
@@ -121,11 +126,16 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
     // at two per lane): three groups of 9 lanes, lanes 27..31 idle
     const bool in_grp = grp < P;
     constexpr int kB = SpmmTune<XT, G, VPL>::kBatch;
+    // a step whose P kU nonzeros are all in the batch, on a slab that fills
+    // the lane layout, loads without predicates: lanes past the groups
+    // (27..31) read rows of valid columns too and their sums are not used
+    const bool full_cols = C == G * VPL;
     for (int64_t base = j0; base < j1; base += kB) {
       const int cnt = (int)((j1 - base) < kB ? (j1 - base) : kB);
       const uint32_t c = lane < cnt ? R.c(base + lane) : 0u;
       const float v = Rows::kHasVal ? (lane < cnt ? R.v(base + lane) : 0.f) : 1.f;
-      for (int t0 = 0; t0 < cnt; t0 += P * kU) {
+      auto step = [&](int t0, auto checked) {
+        constexpr bool kChecked = decltype(checked)::value;
         uint4 raw[kU][VPL];
         float vv[kU];
 #pragma unroll
@@ -137,8 +147,11 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
 #pragma unroll
           for (int k = 0; k < VPL; ++k) {
             const int ch = gl + G * k;
-            raw[u][k] = (in_grp && t < cnt && ch < C) ? __ldg(reinterpret_cast<const uint4*>(xr + ch * E))
-                                                       : make_uint4(0, 0, 0, 0);
+            if constexpr (kChecked)
+              raw[u][k] = (in_grp && t < cnt && ch < C) ? __ldg(reinterpret_cast<const uint4*>(xr + ch * E))
+                                                         : make_uint4(0, 0, 0, 0);
+            else
+              raw[u][k] = __ldg(reinterpret_cast<const uint4*>(xr + ch * E));
           }
         }
 #pragma unroll
@@ -147,9 +160,21 @@ __device__ __forceinline__ void spmm_accumulate(const Rows& R, int64_t j0, int64
           for (int k = 0; k < VPL; ++k) {
             float x[E];
             Vec16<XT>::unpack(raw[u][k], x);
+            // paired FP32 FMAs: each element rounded as by fmaf
 #pragma unroll
-            for (int e = 0; e < E; ++e) acc.a[k][e] = fmaf(vv[u], x[e], acc.a[k][e]);
+            for (int e = 0; e < E; e += 2) {
+              const float2 r = __ffma2_rn(make_float2(vv[u], vv[u]), make_float2(x[e], x[e + 1]),
+                                          make_float2(acc.a[k][e], acc.a[k][e + 1]));
+              acc.a[k][e] = r.x;
+              acc.a[k][e + 1] = r.y;
+            }
           }
+      };
+      for (int t0 = 0; t0 < cnt; t0 += P * kU) {
+        if (full_cols && t0 + P * kU <= cnt)
+          step(t0, std::false_type{});
+        else
+          step(t0, std::true_type{});
       }
     }
     if constexpr ((G & (G - 1)) == 0) {
