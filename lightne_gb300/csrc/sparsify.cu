@@ -712,6 +712,9 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 // The slots of a warp's stretch of the table are compacted into a per-warp
 // queue first (about a third of the slots are occupied), so that the
 // log evaluation runs with all 32 lanes busy.
+// Pairs a thread of the dense trunc-log evaluates per round.
+static constexpr int kTruncLogPer = 4;
+
 template <bool WEIGHTED>
 struct TruncLogOut {
   unsigned nitem;  // 0, 1 or 2 CSR entries
@@ -823,26 +826,38 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   if (DENSE) {
     // every slot occupied (the distinct pairs of the sliced aggregation):
-    // block-uniform rounds of 256 consecutive pairs, whose items are placed
-    // with one atomic on the item count per round (per warp, the atomics on
-    // that one counter serialise in L2)
+    // block-uniform rounds of kTruncLogPer x 256 consecutive pairs, each
+    // thread evaluating kTruncLogPer of them (their vertex-record gathers in
+    // flight together), whose items are placed with one atomic on the item
+    // count per round (per warp, the atomics on that one counter serialise
+    // in L2)
     __shared__ unsigned wsum[8];
     __shared__ unsigned long long bbase;
-    for (uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x; b0 < cap; b0 += stride) {
-      const uint64_t i = b0 + threadIdx.x;
-      const bool have = i < cap;
-      const Slot sl = have ? T[i] : Slot{kEmptyKey, 0ULL};
-      TruncLogOut<WEIGHTED> o;
-      o.nitem = 0;
-      if (have) o = trunclog_entry<WEIGHTED>(sl.key, sl.val, vd, factor, xf, upper, tab);
-      if (o.nitem) {
-        atomicAdd(&rowcnt[o.u], 1ULL);
-        if (o.nitem == 2) atomicAdd(&lowcnt[o.v], 1ULL);
-        if (o.u == o.v) diag[o.u] = 1;
-        ++kept;
+    constexpr int kPer = kTruncLogPer;
+    const uint64_t span = (uint64_t)blockDim.x * kPer;
+    for (uint64_t b0 = (uint64_t)blockIdx.x * span; b0 < cap; b0 += (uint64_t)gridDim.x * span) {
+      TruncLogOut<WEIGHTED> o[kPer];
+      unsigned mine = 0;
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        const uint64_t i = b0 + (uint64_t)q * blockDim.x + threadIdx.x;
+        o[q].nitem = 0;
+        if (i < cap) {
+          const Slot sl = T[i];
+          o[q] = trunclog_entry<WEIGHTED>(sl.key, sl.val, vd, factor, xf, upper, tab);
+        }
       }
-      const unsigned one = o.nitem ? 1u : 0u;
-      unsigned incl = one;
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        if (o[q].nitem) {
+          atomicAdd(&rowcnt[o[q].u], 1ULL);
+          if (o[q].nitem == 2) atomicAdd(&lowcnt[o[q].v], 1ULL);
+          if (o[q].u == o[q].v) diag[o[q].u] = 1;
+          ++kept;
+          ++mine;
+        }
+      }
+      unsigned incl = mine;
 #pragma unroll
       for (int sh = 1; sh < 32; sh <<= 1) {
         const unsigned t = __shfl_up_sync(kFullMask, incl, sh);
@@ -858,13 +873,17 @@ __global__ void __launch_bounds__(256) k_trunclog(const Slot* __restrict__ T, ui
       __syncthreads();
       unsigned before = 0;
       for (int w = 0; w < wid; ++w) before += wsum[w];
-      if (one) {
-        const uint64_t pos = bbase + before + incl - 1;
-        if (pos < max_items) {
-          okeys[pos] = ((unsigned long long)o.u << cbits) | o.v;
-          ovals[pos] = __float_as_uint(o.f);
-        } else {
-          atomicOr(&flags[kFlagSortOverflow], 1);
+      uint64_t pos = bbase + before + incl - mine;
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        if (o[q].nitem) {
+          if (pos < max_items) {
+            okeys[pos] = ((unsigned long long)o[q].u << cbits) | o[q].v;
+            ovals[pos] = __float_as_uint(o[q].f);
+          } else {
+            atomicOr(&flags[kFlagSortOverflow], 1);
+          }
+          ++pos;
         }
       }
       __syncthreads();  // wsum and bbase are rewritten in the next round
