@@ -224,6 +224,9 @@ def run_reference(args, ws, rank):
 # ---------------------------------------------------------------------------
 def pipeline_step(ctx, g, w, precision, seed):
     from lightne_gb300.api import chebyshev_expansion, generate_trunc_log_matrix_v2, get_embedding_dense, randsvd
+    # the 16-bit forms run one FP64 Jacobi sweep after the FP32 ones in both
+    # core SVDs; the FP32 form sweeps in FP64 until they converge
+    ctx.set_core_svd_fp64(1 if precision == "fp32" else 0)
     ratio = float(np.float32(w["sample_ratio"]))
     csr, s1 = generate_trunc_log_matrix_v2(ctx, g, seed, walk_len=w["walk_len"], table_size=w["tablesz"],
                                            sample_ratio=ratio)
@@ -895,6 +898,7 @@ def accuracy(ctx, g, w, off, nbrs, csr_host, forms):
     d_rp, d_col, d_val = (torch.from_numpy(a).cuda() for a in (rp, col, val))
     csr = CSR.wrap_device(ctx, n, int(rp[-1]), d_rp.data_ptr(), d_col.data_ptr(), d_val.data_ptr())
     for form in forms:
+        ctx.set_core_svd_fp64(1 if form == "fp32" else 0)  # as in pipeline_step
         emb, S, _ = randsvd(ctx, csr, w["rank"], w["dim"], precision=form, seed=SVD_SEED)
         e = emb.double().cpu().numpy()
         y, _ = chebyshev_expansion(ctx, g, ref32, w["dim"], order=w["order"], precision=form)

@@ -110,6 +110,14 @@ int lne_ctx_set_sparsify_rounds(lne_ctx* ctx, int32_t mode, int32_t row_sort_max
  * many as shared memory holds (1,310,720); a row is swept once per window
  * of the column range.  The output is the same either way. */
 int lne_ctx_set_row_sort_window(lne_ctx* ctx, int64_t cols);
+/* FP64 sweeps of the r x r core SVDs of lne_randsvd (mklredsvd.cc:353-371,
+ * LAPACKE_sgesvd in the reference) and lne_dense_embed
+ * (SpectralPropagation.h:16-43), which start from a one-sided Jacobi in
+ * FP32 (columns orthogonal to |cos| <= 4e-6): mode 1 runs FP64 sweeps until
+ * they converge, mode 0 one FP64 sweep (|cos| to about its square).  -1
+ * (the default): one in the 16-bit forms of lne_randsvd, else until they
+ * converge.  lne_core_svd always runs them to convergence. */
+int lne_ctx_set_core_svd_fp64(lne_ctx* ctx, int32_t mode);
 /* Wait for all work queued on the context's stream. */
 int lne_ctx_synchronize(lne_ctx* ctx);
 /* Kernels the pipeline entry points (lne_sparsify, lne_randsvd,

@@ -149,6 +149,7 @@ SIGNATURES = {
     "lne_ctx_set_sparsify_batch": (ctypes.c_int, [VP, I64]),
     "lne_ctx_set_sparsify_rounds": (ctypes.c_int, [VP, I32, I32]),
     "lne_ctx_set_row_sort_window": (ctypes.c_int, [VP, I64]),
+    "lne_ctx_set_core_svd_fp64": (ctypes.c_int, [VP, I32]),
     "lne_device_alloc": (ctypes.c_int, [VP, I64, PVP]),
     "lne_device_free": (ctypes.c_int, [VP, VP]),
     "lne_copy_to_host": (ctypes.c_int, [VP, VP, VP, I64]),

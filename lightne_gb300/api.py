@@ -65,6 +65,13 @@ class Context:
         2048; 0: as many as shared memory holds)."""
         check(_lib.load().lne_ctx_set_row_sort_window(self.handle, cols))
 
+    def set_core_svd_fp64(self, mode: int = -1) -> None:
+        """FP64 Jacobi sweeps in the core SVDs of lne_randsvd and
+        lne_dense_embed after the FP32 ones: 1 until they converge, 0 one
+        sweep, -1 (default) one in the 16-bit forms of lne_randsvd, else
+        until they converge."""
+        check(_lib.load().lne_ctx_set_core_svd_fp64(self.handle, mode))
+
     def close(self) -> None:
         if self.handle:
             _lib.load().lne_ctx_destroy(self.handle)

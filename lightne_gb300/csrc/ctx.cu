@@ -296,6 +296,12 @@ int lne_ctx_set_row_sort_window(lne_ctx* ctx, int64_t cols) {
   return LNE_OK;
 }
 
+int lne_ctx_set_core_svd_fp64(lne_ctx* ctx, int32_t mode) {
+  LNE_CHECK_ARG(ctx != nullptr && mode >= -1 && mode <= 1, "lne_ctx_set_core_svd_fp64: mode must be -1, 0 or 1");
+  ctx->core_svd_fp64 = mode;
+  return LNE_OK;
+}
+
 int lne_ctx_launch_count(const lne_ctx* ctx, int64_t* out) {
   LNE_CHECK_ARG(ctx != nullptr && out != nullptr, "lne_ctx_launch_count: NULL argument");
   *out = ctx->launch_count;

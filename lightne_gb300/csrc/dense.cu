@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps(int r, double* __restrict
     }
     if (__ldcg(rotated + sweep) == 0) break;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep + 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep < max_sweeps ? sweep + 1 : max_sweeps;
 }
 
 constexpr int kJacobiPer = 5;  // column elements per lane held in registers (r <= 160)
@@ -826,7 +826,7 @@ __global__ void __launch_bounds__(256) k_jacobi_sweeps_dsmem(int r, double* __re
     if (c < r)
       for (int i = threadIdx.x; i < r; i += blockDim.x) Wc[(int64_t)c * r + i] = jcols[(int64_t)s * r + i];
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep + 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *sweeps_out = sweep < max_sweeps ? sweep + 1 : max_sweeps;
 }
 
 // FP32 preconditioning of the FP64 sweeps (r <= 32 * kJacobiPer, one CTA):
@@ -1069,13 +1069,16 @@ static bool jacobi_precond_applies(lne_ctx* ctx, int r) {
 
 int jacobi_svd_launches(lne_ctx* ctx, int r) { return jacobi_precond_applies(ctx, r) ? 7 : 3; }
 
-int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out, int* sweeps32_out) {
+int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out, int* sweeps32_out,
+               int fp64_sweep_cap) {
   if (r > 1024) {
     set_error("jacobi_svd: rank above 1024 is not supported");
     return LNE_ERR_UNSUPPORTED;
   }
   const int kMaxSweeps = kJacobiMaxSweeps;
   const bool pre = jacobi_precond_applies(ctx, r);
+  // after the FP32 preconditioning, at most fp64_sweep_cap FP64 sweeps
+  const int max_sweeps = pre && fp64_sweep_cap > 0 && fp64_sweep_cap < kMaxSweeps ? fp64_sweep_cap : kMaxSweeps;
   const size_t rr = (size_t)r * r;
   double* Wc = nullptr;
   int rc;
@@ -1132,7 +1135,7 @@ int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps
       cudaGetLastError();
       continue;
     }
-    e = cudaLaunchKernelEx(&cfg, kern, r, Wc, rotated, kMaxSweeps, d_sw);
+    e = cudaLaunchKernelEx(&cfg, kern, r, Wc, rotated, max_sweeps, d_sw);
     if (e == cudaSuccess) break;
     cudaGetLastError();
   }

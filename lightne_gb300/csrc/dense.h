@@ -47,10 +47,20 @@ int cholesky_inv(lne_ctx* ctx, double* G, int r, double shift, float* W);
 // U (r x r FP64, columns = left singular vectors, sorted by singular value,
 // descending), S (r, FP64).  For r <= 160 the FP64 sweeps start from an
 // FP32 Jacobi preconditioning; *sweeps32_out (may be NULL) gets its sweeps
-// (0 without it), *sweeps_out the FP64 sweeps.
-int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out, int* sweeps32_out = nullptr);
+// (0 without it), *sweeps_out the FP64 sweeps.  fp64_sweep_cap > 0 caps
+// the FP64 sweeps after the preconditioning (r <= 160); 0: until they
+// converge.  One FP64 sweep takes the FP32 stopping level (|cos| <= 4e-6)
+// to about its square.
+int jacobi_svd(lne_ctx* ctx, double* C, int r, double* U, double* S, int* sweeps_out, int* sweeps32_out = nullptr,
+               int fp64_sweep_cap = 0);
 // Kernel launches of one jacobi_svd call.
 int jacobi_svd_launches(lne_ctx* ctx, int r);
+// The FP64 sweep cap of the pipeline's core SVDs (the context's setting;
+// `full_by_default` says what the automatic setting does for the caller).
+inline int core_svd_sweep_cap(const lne_ctx* ctx, bool full_by_default) {
+  const bool full = ctx->core_svd_fp64 < 0 ? full_by_default : ctx->core_svd_fp64 != 0;
+  return full ? 0 : 1;
+}
 
 // tcgen05 tensor-core versions (3xTF32, FP32-level accuracy) of gram and
 // gemm_tall for up to 256 columns; gram/gemm_tall use them when they apply.

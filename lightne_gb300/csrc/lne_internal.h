@@ -78,6 +78,11 @@ struct lne_ctx {
   // columns at a time (0: as many as shared memory holds)
   int row_sort_warp_max = 1024;
   int64_t row_sort_window_cols = 0;
+  // FP64 Jacobi sweeps after the FP32 preconditioning in the core SVDs of
+  // lne_randsvd and lne_dense_embed: 1 until they converge, 0 one sweep,
+  // -1 (the default) one in the 16-bit forms of lne_randsvd, else until
+  // they converge
+  int core_svd_fp64 = -1;
   // kernels launched by the entry points that ran on this context (each
   // adds its own count when it returns successfully)
   int64_t launch_count = 0;

@@ -289,7 +289,10 @@ extern "C" int lne_randsvd(lne_ctx* ctx, const lne_csr* Acsr, const lne_randsvd_
     return rc;
   if ((rc = gram(ctx, Y, ld, r, Bm, ld, r, n, C))) return rc;
   int sweeps = 0, sweeps32 = 0;
-  if ((rc = jacobi_svd(ctx, C, r, U, S, &sweeps, &sweeps32))) return rc;
+  // FP64 sweeps to convergence in the FP32 form, one in the 16-bit forms
+  // (unless the context says otherwise)
+  const int cap = core_svd_sweep_cap(ctx, !low);
+  if ((rc = jacobi_svd(ctx, C, r, U, S, &sweeps, &sweeps32, cap))) return rc;
   launches += 2 + jacobi_svd_launches(ctx, r);  // Gram + reduction, Jacobi
   // emb = Z * (U_C[:, :dim] * diag(sqrt(S[:dim])))
   if ((rc = B.get(&Wf, (size_t)r * dim, "U sqrt(S)"))) return rc;
@@ -380,7 +383,7 @@ extern "C" int lne_dense_embed(lne_ctx* ctx, const float* d_x, int64_t n, int64_
   if ((rc = cholqr3(ctx, Q, T, n, ld, d, Copy16(), &launches))) return rc;
   if ((rc = gram(ctx, Q, ld, d, X, ld, d, n, C))) return rc;
   int sweeps = 0;
-  if ((rc = jacobi_svd(ctx, C, d, U, S, &sweeps))) return rc;
+  if ((rc = jacobi_svd(ctx, C, d, U, S, &sweeps, nullptr, core_svd_sweep_cap(ctx, true)))) return rc;
   k_scale_cols<<<(d * d + 255) / 256, 256, 0, st>>>(U, S, d, d, W);
   if ((rc = gemm_tall(ctx, Q, ld, d, W, d, n, d_emb, d))) return rc;
   // get_embedding_dense normalises unconditionally (SpectralPropagation.h:40)

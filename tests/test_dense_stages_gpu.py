@@ -45,7 +45,34 @@ def test_randsvd_matches_fp64(ctx, netsmf_matrix, precision, tol, normalize):
     err = lo.procrustes_rel_error(e, ref)
     assert err < tol, err
     assert lo.rel_sv_error(S[:dim], Sref[:dim]) < tol
-    assert st["jacobi_sweeps"] > 0
+    # FP64 sweeps after the FP32 ones: until they converge in the FP32 form,
+    # one in the 16-bit forms (by default)
+    assert st["jacobi_sweeps_fp32"] > 0
+    assert st["jacobi_sweeps"] > 0 if precision == "fp32" else st["jacobi_sweeps"] == 1
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_core_svd_one_fp64_sweep(ctx, netsmf_matrix, precision):
+    # one FP64 sweep after the FP32 ones gives the embedding of the FP64
+    # sweeps run to convergence, to far below the forms' tolerances
+    csr, A, _ = netsmf_matrix
+    rank, dim, seed = 48, 32, 777
+    out = {}
+    try:
+        for mode in (1, 0):
+            ctx.set_core_svd_fp64(mode)
+            out[mode] = randsvd(ctx, csr, rank, dim, precision=precision, seed=seed)
+    finally:
+        ctx.set_core_svd_fp64(-1)
+    (e1, S1, st1), (e0, S0, st0) = out[1], out[0]
+    assert st0["jacobi_sweeps"] == 1 and st1["jacobi_sweeps"] >= 1
+    assert lo.procrustes_rel_error(e0.double().cpu().numpy(), e1.double().cpu().numpy()) < 1e-5
+    assert lo.rel_sv_error(S0[:dim], S1[:dim]) < 1e-8
+    if precision == "fp32":
+        om = gaussian(ctx, seed, 0, A.shape[0], rank)
+        P = gaussian(ctx, seed, 1, rank, rank)
+        ref, _ = lo.randsvd(A, om.double().cpu().numpy(), P.double().cpu().numpy(), dim)
+        assert lo.procrustes_rel_error(e0.double().cpu().numpy(), ref) < 1e-4
 
 
 def test_random_project_only(ctx, netsmf_matrix):
@@ -115,3 +142,11 @@ def test_dense_embed_matches_fp64(ctx, dim):
     assert lo.rel_sv_error(S, Sref) < 1e-4
     nr = np.linalg.norm(emb.double().cpu().numpy(), axis=1)
     np.testing.assert_allclose(nr, 1.0, rtol=1e-5)
+    # with one FP64 sweep
+    try:
+        ctx.set_core_svd_fp64(0)
+        emb0, S0 = get_embedding_dense(ctx, x.astype(np.float32), dim)
+    finally:
+        ctx.set_core_svd_fp64(-1)
+    assert lo.procrustes_rel_error(emb0.double().cpu().numpy(), ref) < 1e-4
+    assert lo.rel_sv_error(S0, Sref) < 1e-4

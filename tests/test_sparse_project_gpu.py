@@ -80,4 +80,5 @@ def test_randsvd_sparse_project_matches_fp64(ctx, netsmf_matrix, precision, tol)
     err = lo.procrustes_rel_error(e, ref)
     assert err < tol, err
     assert lo.rel_sv_error(S[:dim], Sref[:dim]) < tol
-    assert st["jacobi_sweeps"] > 0
+    assert st["jacobi_sweeps_fp32"] > 0
+    assert st["jacobi_sweeps"] > 0 if precision == "fp32" else st["jacobi_sweeps"] == 1
