@@ -115,7 +115,7 @@ __device__ __forceinline__ bool tc_kloop(uint8_t* smem, TcShared* sh, uint32_t t
     const uint32_t parity = (uint32_t)((last / kStages) & 1);
     if (!tc::mbar_wait(tc::smem_addr(&sh->mbar[last % kStages]), parity, kWaitCycles, abort)) ok = false;
   }
-  // block-uniform verdict: the epilogue's tcgen05.ld is warp-synchronous
+  // one outcome for the whole block: the epilogue's tcgen05.ld is warp-synchronous
   ok = __syncthreads_and(ok ? 1 : 0) != 0;
   tc::fence_after_sync();
   return ok;

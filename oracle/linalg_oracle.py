@@ -2,7 +2,7 @@
 
 FP64 NumPy/SciPy restatement of the reference's dense stages, used as the
 checker of the device randomized SVD, spectral propagation and dense
-embedding.  Parity for these stages is judged by error metrics, not bit
+embedding.  Parity for these stages is measured by error metrics, not bit
 patterns: the reference's arithmetic runs in Intel MKL (not in the reference
 tree, no pinned version; README.md:22-37 asks for a conda/Parallel Studio
 MKL), whose summation order and VSL SFMT19937 Gaussian stream cannot be
