@@ -135,20 +135,25 @@ void scan_exclusive_i64(const int64_t* counts, int64_t* out, int64_t n, void* tm
 // Graph upload: validate the CSR on the device and derive {offset, degree}
 // pairs plus the source vertex of every directed entry.
 // ---------------------------------------------------------------------------
+// The maximum degree is reduced per warp first: one atomic per warp rather
+// than a million on one address.
 __global__ void k_graph_build(const int64_t* __restrict__ off, int64_t n, int64_t m_dir,
                               Vertex* __restrict__ vdata, int* __restrict__ bad,
                               unsigned long long* __restrict__ maxdeg) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int64_t a = off[i], b = off[i + 1];
-  if (a < 0 || b < a || b > m_dir) {
-    atomicExch(bad, 1);
-    vdata[i] = Vertex{0u, 0u, 1ull};
-    return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t d = 0;
+  if (i < n) {
+    const int64_t a = off[i], b = off[i + 1];
+    if (a < 0 || b < a || b > m_dir) {
+      atomicExch(bad, 1);
+      vdata[i] = Vertex{0u, 0u, 1ull};
+    } else {
+      d = (uint32_t)(b - a);  // m_dir < 2^32
+      vdata[i] = Vertex{(uint32_t)a, d, gm_magic(d > 0 ? d : 1u)};
+    }
   }
-  const uint32_t d = (uint32_t)(b - a);
-  vdata[i] = Vertex{(uint32_t)a, d, gm_magic(d > 0 ? d : 1u)};
-  atomicMax(maxdeg, (unsigned long long)(b - a));
+  const uint32_t wmax = __reduce_max_sync(0xffffffffu, d);
+  if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(maxdeg, (unsigned long long)wmax);
 }
 
 // Also rejects an entry whose target has no neighbours: the graph must be
