@@ -711,8 +711,8 @@ __global__ void k_trunc_log_values(const double* __restrict__ x, int64_t n, doub
 //
 // The slots of a warp's stretch of the table are compacted into a per-warp
 // queue first (about a third of the slots are occupied), so that the
-// log evaluation runs with all 32 lanes busy.
-// Pairs a thread of the dense trunc-log evaluates per round.
+// log evaluation runs with all 32 lanes busy.  On the dense distinct pairs
+// each thread evaluates kTruncLogPer pairs per round.
 static constexpr int kTruncLogPer = 4;
 
 template <bool WEIGHTED>
